@@ -1,0 +1,180 @@
+/*
+ * dfsph_gb300.h — C ABI of the GB300-native DFSPH step.
+ *
+ * Plain C: pointers, sizes and status codes; no C++ or torch types cross this
+ * boundary, nothing throws across it and nothing traps on the device. Every
+ * entry point returns DFSPH_OK (0) or a DFSPH_ERR_* code; the message of the
+ * last failure on a context is available from dfsph_last_error().
+ *
+ * Each declaration names the reference interface of Qervas/water_simulation
+ * that it replaces (file:line within that project). The C++ façade in
+ * include/water/ (ParticleStore, DFSPHSolver, CellGrid, load_scene,
+ * sample_aabb_boundary) is written on top of these calls.
+ *
+ * Memory arguments carry a `mem` flag: DFSPH_MEM_HOST for host pointers
+ * (pageable or pinned), DFSPH_MEM_DEVICE for device pointers of the context's
+ * device. All device work runs on the context's stream.
+ */
+#ifndef DFSPH_GB300_H
+#define DFSPH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define DFSPH_OK                    0
+#define DFSPH_ERR_INVALID_ARGUMENT  1  /* bad pointer / size / enum          */
+#define DFSPH_ERR_CUDA              2  /* a CUDA runtime call failed          */
+#define DFSPH_ERR_OUT_OF_RANGE      3  /* count beyond capacity (std::out_of_range in the reference) */
+#define DFSPH_ERR_STATE             4  /* call not valid in the current state */
+#define DFSPH_ERR_DEVICE_TIMEOUT    5  /* a bounded device wait gave up       */
+#define DFSPH_ERR_NONFINITE         6  /* NaN/Inf detected in the state       */
+#define DFSPH_ERR_NO_DEVICE         7  /* no CUDA device / driver             */
+
+#define DFSPH_MEM_HOST   0
+#define DFSPH_MEM_DEVICE 1
+
+/* arithmetic of the step */
+#define DFSPH_PRECISION_FP32        0  /* plain FP32                                        */
+#define DFSPH_PRECISION_FP32_KAHAN  1  /* FP32 state, compensated density sums               */
+#define DFSPH_PRECISION_FP64        2  /* the same kernels instantiated in FP64 (GPU oracle) */
+
+/* ---- configuration ----------------------------------------------------- */
+/* Mirrors water::solvers::DFSPHSolver::Config
+ * (solvers/dfsph/include/water/solvers/dfsph.h:19-33) field for field, then
+ * the GB300 extensions. dfsph_config_init() fills the reference defaults. */
+typedef struct dfsph_config {
+    float    rest_density;          /* 1000                                   */
+    float    particle_radius;       /* 0.0015                                 */
+    float    smoothing_length;      /* 0.003 (cell length = this)             */
+    float    viscosity;             /* XSPH epsilon, 1e-3; <= 0 disables XSPH  */
+    float    damping;               /* 0.5 1/s                                */
+    float    surface_tension;       /* accepted, unused (as in the reference) */
+    float    gravity[3];            /* (0, -9.81, 0)                          */
+    uint32_t max_density_iters;     /* 100                                    */
+    uint32_t max_divergence_iters;  /* 100 in the reference Config, where it is
+                                       unused; set 0 for the reference's step */
+    float    eta_density;           /* 1e-3; 0 => exactly max_density_iters    */
+    float    eta_divergence;        /* 1e-3                                   */
+    float    domain_min[3];         /* (0,0,0)                                */
+    float    domain_max[3];         /* (1,1,1)                                */
+    /* GB300 extensions */
+    uint32_t precision;             /* DFSPH_PRECISION_*                      */
+    uint32_t capacity;              /* max fluid particles (ParticleStore capacity) */
+    uint32_t boundary_capacity;     /* max boundary particles                 */
+    uint32_t record_diagnostics;    /* 1 => keep per-step neighbour counts     */
+} dfsph_config;
+
+typedef struct dfsph_ctx dfsph_ctx;
+
+/* Fields readable with dfsph_get_field(), always in the caller's ORIGINAL
+ * particle order (the order of dfsph_set_fluid), except the grid arrays. */
+#define DFSPH_FIELD_POSITION          0  /* float[3*n]  ParticleStore::positions()              */
+#define DFSPH_FIELD_VELOCITY          1  /* float[3*n]  ParticleStore::velocities()             */
+#define DFSPH_FIELD_DENSITY           2  /* float[n]    "dfsph_density"     (dfsph.cu:80)         */
+#define DFSPH_FIELD_ALPHA             3  /* float[n]    "dfsph_alpha"       (dfsph.cu:81)         */
+#define DFSPH_FIELD_KAPPA             4  /* float[n]    "dfsph_kappa"       (dfsph.cu:82)         */
+#define DFSPH_FIELD_DENSITY_ADV       5  /* float[n]    "dfsph_density_adv" (dfsph.cu:83)         */
+#define DFSPH_FIELD_CELL_KEY          6  /* uint32[n]   cell key of each particle at the last grid build */
+#define DFSPH_FIELD_SORTED_INDEX      7  /* uint32[n]   CellGrid::sorted_indices()                */
+#define DFSPH_FIELD_CELL_START        8  /* uint32[C+1] CellGrid::cell_start()                    */
+#define DFSPH_FIELD_NBR_FLUID         9  /* uint32[n]   fluid candidates visited by the 27-cell stencil (needs record_diagnostics) */
+#define DFSPH_FIELD_NBR_BOUNDARY     10  /* uint32[n]   boundary candidates visited                */
+#define DFSPH_FIELD_BOUNDARY_MASS    11  /* float[nb]   "dfsph_boundary_mass" (dfsph.cu:91-92), boundary input order */
+#define DFSPH_FIELD_KAPPA_V          12  /* float[n]    divergence-solver kappa                    */
+#define DFSPH_FIELD_BOUNDARY_CELL_START   13  /* uint32[C+1] boundary CellGrid::cell_start()      */
+#define DFSPH_FIELD_BOUNDARY_SORTED_INDEX 14  /* uint32[nb] boundary CellGrid::sorted_indices()   */
+
+/* Scalars readable with dfsph_get_scalar(). */
+#define DFSPH_SCALAR_MAX_VELOCITY          0  /* DFSPHSolver::max_velocity() (dfsph.h:40) */
+#define DFSPH_SCALAR_PARTICLE_MASS         1  /* DFSPHSolver::particle_mass() (dfsph.h:44) */
+#define DFSPH_SCALAR_LAST_DENSITY_ITERS    2  /* DFSPHSolver::last_density_iters() (dfsph.h:50) */
+#define DFSPH_SCALAR_LAST_DIVERGENCE_ITERS 3
+#define DFSPH_SCALAR_DENSITY_ERROR         4  /* last mean max(0, rho*-rho0), FP64 sum */
+#define DFSPH_SCALAR_DIVERGENCE_ERROR      5  /* last mean max(0, rho_dot),  FP64 sum */
+#define DFSPH_SCALAR_TOTAL_CELLS           6  /* CellGrid::total_cells() (cell_grid.h:28-33) */
+#define DFSPH_SCALAR_STENCIL_INV_CELL      7  /* device reciprocal that centres the stencil */
+#define DFSPH_SCALAR_FLUID_COUNT           8
+#define DFSPH_SCALAR_BOUNDARY_COUNT        9
+#define DFSPH_SCALAR_KERNEL_LAUNCHES      10  /* kernels launched by this context so far */
+#define DFSPH_SCALAR_FLAGS                11  /* bit0: a convergence sum was NaN; bit1: more than
+                                                 4096 out-of-grid particles, kept in arrival order */
+
+/* Reference defaults of DFSPHSolver::Config (dfsph.h:19-33). */
+int dfsph_config_init(dfsph_config* cfg);
+
+/* Replaces the DFSPHSolver constructor (solvers/dfsph/src/dfsph.cu:71-100)
+ * minus the caller-owned stores: grid geometry of make_grid (dfsph.cu:55-65),
+ * particle mass rho0*(2r)^3 (dfsph.cu:76-78) and every device buffer, sized for
+ * cfg->capacity fluid and cfg->boundary_capacity boundary particles.
+ * `stream` is a cudaStream_t (NULL = the legacy default stream). */
+int dfsph_create(const dfsph_config* cfg, int device, void* stream, dfsph_ctx** out);
+void dfsph_destroy(dfsph_ctx* ctx);
+int dfsph_set_stream(dfsph_ctx* ctx, void* stream);
+
+/* Boundary particles: the boundary ParticleStore's positions, the boundary grid
+ * built once and the Akinci mass m_b = rho0 / max(sum W, 1e-9)
+ * (dfsph.cu:90-99,102-116; dfsph_kernels.cu:40-65). n = 0 removes the boundary. */
+int dfsph_set_boundary(dfsph_ctx* ctx, const float* xyz, uint32_t n, int mem);
+
+/* Fluid state: ParticleStore::resize + the position/velocity uploads of
+ * sim_cli (apps/sim_cli/main.cpp:180-184). `vel` may be NULL (zero velocity,
+ * as a freshly registered attribute). n > capacity => DFSPH_ERR_OUT_OF_RANGE
+ * (ParticleStore::resize, core/src/particle_store.cu:11-17). */
+int dfsph_set_fluid(dfsph_ctx* ctx, const float* xyz, const float* vel, uint32_t n, int mem);
+
+/* DFSPHSolver::step(dt) (dfsph.cu:120-133), n_steps times, on the state held
+ * by the context. Asynchronous unless a convergence check needs the host
+ * (eta > 0); results stay on the device. */
+int dfsph_step(dfsph_ctx* ctx, float dt, uint32_t n_steps);
+
+/* One DFSPHSolver::step(dt) on caller-owned ParticleStore buffers: AoS float3
+ * device arrays in the caller's order, read at entry and written back at exit
+ * together with the four solver attributes (any attribute pointer may be NULL).
+ * This is the entry the C++ façade's DFSPHSolver::step uses. */
+int dfsph_step_store(dfsph_ctx* ctx, float* pos, float* vel, uint32_t n, float dt,
+                     float* density, float* alpha, float* kappa, float* density_adv);
+
+/* Field readback (density_at/alpha_at/boundary_mass_at, dfsph.cu:330-353, as
+ * whole arrays). dst_bytes is checked against the field's size. */
+int dfsph_get_field(dfsph_ctx* ctx, int field, void* dst, size_t dst_bytes, int mem);
+int dfsph_get_scalar(dfsph_ctx* ctx, int which, double* out);
+
+/* Wait for the context's stream; returns a pending device error if any. */
+int dfsph_synchronize(dfsph_ctx* ctx);
+
+const char* dfsph_last_error(const dfsph_ctx* ctx);
+const char* dfsph_status_string(int status);
+
+/* ---- stand-alone pieces -------------------------------------------------- */
+
+/* water::solvers::sample_aabb_boundary (solvers/dfsph/src/boundary_sampler.cpp:6-32;
+ * declaration solvers/dfsph/include/water/solvers/boundary_sampler.h:24-25).
+ * Writes min(count, cap) points to out (xyz, host) and returns count (>= 0). */
+int64_t dfsph_sample_aabb_boundary(const float lo[3], const float hi[3], float spacing,
+                                   int n_layers, float* out, int64_t cap);
+
+/* make_grid geometry (dfsph.cu:55-65). */
+int dfsph_grid_geometry(const dfsph_config* cfg, float origin[3], int dims[3]);
+
+/* CellGrid::build (core/src/cell_grid.cu:73-138) on device arrays: keys
+ * (sorted, as CellGrid leaves cell_ids_), sorted_indices[n] and
+ * cell_start[dims.x*dims.y*dims.z + 1]; sorted_keys_dev and sorted_indices_dev
+ * may be NULL. Temporaries are stream-ordered allocations on `stream`; the call
+ * returns after the work is enqueued there. n = 0 leaves cell_start untouched,
+ * as CellGrid::build does for count == 0 (cell_grid.cu:74-77). */
+int dfsph_build_cell_grid(const float* xyz_dev, uint32_t n, const float origin[3],
+                          const int dims[3], float cell_length, uint32_t* sorted_keys_dev,
+                          uint32_t* sorted_indices_dev, uint32_t* cell_start_dev,
+                          void* stream);
+
+
+#ifdef __cplusplus
+}  /* extern "C" */
+#endif
+
+#endif /* DFSPH_GB300_H */

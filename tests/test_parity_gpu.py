@@ -1,0 +1,252 @@
+"""Parity of the CUDA step (through the C ABI) with the CPU oracle.
+
+Bit-exact: cell keys, sorted permutation, cell_start and the per-particle
+neighbour-candidate counts of every step, compared from identical inputs (the
+GPU state of step k is handed to a fresh FP32 oracle, which takes the device's
+stencil reciprocal, and both take step k+1).
+
+Tolerances (FP32 GPU vs FP32 oracle from identical inputs, one step):
+  density, alpha   1e-5 relative to rho0 / relative
+  positions        1e-6 m
+  velocities       2e-4 m/s
+Trajectories are compared with the FP64 oracle (see test_trajectory_vs_fp64).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from water_simulation_gb300 import _lib, scenes
+from water_simulation_gb300.solver import Solver, solver_for
+
+pytestmark = pytest.mark.gpu
+
+STRUCT = [(_lib.FIELD_CELL_KEY, O.F_CELL_KEY), (_lib.FIELD_SORTED_INDEX, O.F_SORTED_INDEX),
+          (_lib.FIELD_CELL_START, O.F_CELL_START), (_lib.FIELD_NBR_FLUID, O.F_NBR_FLUID),
+          (_lib.FIELD_NBR_BOUNDARY, O.F_NBR_BOUNDARY)]
+
+
+def oracle_for(scene, gpu, x=None, v=None, precision=32):
+    inv = gpu.scalar(_lib.SCALAR_STENCIL_INV_CELL)
+    c = O.config_from(scene.config(), stencil_inv_cell=inv)
+    return O.Oracle(c, scene.fluid if x is None else x, scene.velocity if v is None else v,
+                    scene.boundary if scene.nb else None, precision=precision)
+
+
+def assert_structure_equal(gpu, ora, ctx=""):
+    for fg, fo in STRUCT:
+        a, b = gpu.field(fg), ora.field(fo)
+        if not np.array_equal(a, b):
+            bad = np.nonzero(a != b)[0]
+            raise AssertionError(f"{ctx} field {fg}: {len(bad)} mismatches, first at {bad[:5]}: "
+                                 f"{a[bad[:5]]} vs {b[bad[:5]]}")
+
+
+def assert_fields_close(gpu, ora, ctx="", rho_tol=1e-5, x_tol=1e-6, v_tol=2e-4):
+    rho = gpu.field(_lib.FIELD_DENSITY).astype(np.float64)
+    assert np.abs(rho - ora.field(O.F_DENSITY)).max() / 1000.0 < rho_tol, ctx
+    a, ao = gpu.field(_lib.FIELD_ALPHA).astype(np.float64), ora.field(O.F_ALPHA)
+    assert (np.abs(a - ao) / np.maximum(np.abs(ao), 1e-12)).max() < 1e-4, ctx
+    x = gpu.positions().astype(np.float64)
+    assert np.abs(x - ora.field(O.F_POSITION)).max() < x_tol, ctx
+    v = gpu.velocities().astype(np.float64)
+    assert np.abs(v - ora.field(O.F_VELOCITY)).max() < v_tol, ctx
+
+
+@pytest.mark.parametrize("dims,seed,sigma", [((8, 8, 8), 3, 0.0), ((10, 6, 9), 4, 0.3), ((12, 12, 12), 5, 0.1)])
+def test_one_step_parity_with_boundary(dims, seed, sigma):
+    sc = scenes.falling_block(dims, seed=seed, velocity_sigma=sigma)
+    gpu = solver_for(sc, diagnostics=True)
+    ora = oracle_for(sc, gpu)
+    gpu.step(sc.dt)
+    ora.step(sc.dt)
+    assert_structure_equal(gpu, ora)
+    assert_fields_close(gpu, ora)
+    mb = gpu.field(_lib.FIELD_BOUNDARY_MASS).astype(np.float64)
+    assert np.abs(mb - ora.field(O.F_BOUNDARY_MASS)).max() / mb.max() < 1e-5
+    assert np.array_equal(gpu.field(_lib.FIELD_BOUNDARY_SORTED_INDEX), ora.field(O.F_BOUNDARY_SORTED_INDEX))
+    assert np.array_equal(gpu.field(_lib.FIELD_BOUNDARY_CELL_START), ora.field(O.F_BOUNDARY_CELL_START))
+    assert gpu.last_density_iters() == ora.last_density_iters() == sc.max_density_iters
+    assert gpu.max_velocity() == pytest.approx(ora.max_velocity(), rel=1e-4, abs=1e-6)
+
+
+def test_structure_parity_every_step_for_50_steps():
+    sc = scenes.falling_block((10, 10, 10), seed=9, velocity_sigma=0.2)
+    gpu = solver_for(sc, diagnostics=True)
+    for k in range(50):
+        x, v = gpu.positions(), gpu.velocities()
+        ora = oracle_for(sc, gpu, x, v)
+        gpu.step(sc.dt)
+        ora.step(sc.dt)
+        assert_structure_equal(gpu, ora, f"step {k}")
+        assert_fields_close(gpu, ora, f"step {k}")
+        ora.close()
+
+
+def test_particles_on_cell_faces_and_out_of_grid():
+    # positions exactly on cell faces, far outside the grid, and many in one cell
+    sc = scenes.falling_block((6, 6, 6), seed=2)
+    l = 2 * sc.radius
+    pts = sc.fluid.copy()
+    pts[:20, 0] = np.float32(0.4)            # on a face of the x = 0.4 cells
+    pts[20:40] = np.float32([0.5, 0.5, 0.5])   # 20 particles at one point
+    pts[40:45] = np.float32([3.0, 0.5, 0.5])   # out of the grid (sentinel key)
+    pts[45:50] = np.float32([-0.5, -0.5, 2.0])
+    pts[50:60, 1] = np.float32(-l)            # exactly on the grid origin face
+    sc.fluid = pts
+    gpu = solver_for(sc, diagnostics=True)
+    ora = oracle_for(sc, gpu)
+    gpu.step(sc.dt)
+    ora.step(sc.dt)
+    assert_structure_equal(gpu, ora)
+    keys = gpu.field(_lib.FIELD_CELL_KEY)
+    assert (keys[40:50] == gpu.total_cells).all()
+    cs = gpu.field(_lib.FIELD_CELL_START)
+    assert cs[-1] == sc.n - 10
+    assert_fields_close(gpu, ora, v_tol=1e-3)
+
+
+def test_random_cloud_structure_matches():
+    rng = np.random.default_rng(123)
+    sc = scenes.falling_block((4, 4, 4), seed=1)
+    sc.fluid = rng.uniform(-0.05, 1.05, size=(5000, 3)).astype(np.float32)
+    sc.velocity = np.zeros_like(sc.fluid)
+    gpu = solver_for(sc, diagnostics=True)
+    ora = oracle_for(sc, gpu)
+    gpu.step(sc.dt)
+    ora.step(sc.dt)
+    assert_structure_equal(gpu, ora)
+
+
+def test_trajectory_vs_fp64_oracle():
+    """50 steps of a falling block: FP32 GPU vs the FP64 oracle. Reported
+    tolerance: density within 1e-3 of rho0, positions within 1e-4 m."""
+    sc = scenes.falling_block((10, 10, 10), seed=21)
+    gpu = solver_for(sc)
+    ora = oracle_for(sc, gpu, precision=64)
+    gpu.step(sc.dt, 50)
+    ora.step(sc.dt, 50)
+    rho = gpu.field(_lib.FIELD_DENSITY).astype(np.float64)
+    err_rho = np.abs(rho - ora.field(O.F_DENSITY)).max() / 1000.0
+    err_x = np.abs(gpu.positions() - ora.field(O.F_POSITION)).max()
+    print(f"50-step FP32 vs FP64: max|drho|/rho0 = {err_rho:.3e}, max|dx| = {err_x:.3e}")
+    assert err_rho < 1e-3
+    assert err_x < 1e-4
+
+
+def test_fp64_build_matches_fp64_oracle():
+    sc = scenes.falling_block((8, 8, 8), seed=13, velocity_sigma=0.1)
+    gpu = solver_for(sc, precision=_lib.PRECISION_FP64, diagnostics=True)
+    ora = oracle_for(sc, gpu, precision=64)
+    for _ in range(5):
+        gpu.step(sc.dt)
+        ora.step(sc.dt)
+    assert np.abs(gpu.field(_lib.FIELD_DENSITY) - ora.field(O.F_DENSITY)).max() / 1000.0 < 1e-6
+    assert np.abs(gpu.positions() - ora.field(O.F_POSITION)).max() < 1e-6
+
+
+def test_kahan_precision_mode_runs_and_agrees():
+    sc = scenes.falling_block((8, 8, 8), seed=14)
+    a = solver_for(sc, precision=_lib.PRECISION_FP32_KAHAN)
+    b = solver_for(sc, precision=_lib.PRECISION_FP32)
+    a.step(sc.dt, 5)
+    b.step(sc.dt, 5)
+    assert np.abs(a.field(_lib.FIELD_DENSITY) - b.field(_lib.FIELD_DENSITY)).max() < 0.05
+
+
+def test_isolated_particle_density_and_fall():
+    # tests/unit/test_dfsph_density.cu:16-36 and :81-109 through the C ABI
+    sc = scenes.falling_block((1, 1, 1), boundary=False)
+    sc.fluid = np.array([[0.5, 0.5, 0.5]], np.float32)
+    sc.velocity = np.zeros((1, 3), np.float32)
+    sc.radius = 0.01
+    c = sc.config()
+    c.smoothing_length = 0.04
+    c.viscosity = 0.0
+    s = Solver(c)
+    s.set_fluid(sc.fluid, sc.velocity)
+    s.step(0.001)
+    expected = s.particle_mass() / (3.14159265358979323846 * 0.04 ** 3)
+    assert s.density_at(0) == pytest.approx(expected, rel=1e-4)
+    s.step(0.01, 49)
+    p = s.positions()[0]
+    assert p[1] < 0.5 and p[0] == pytest.approx(0.5, rel=0.01) and p[2] == pytest.approx(0.5, rel=0.01)
+
+
+def test_step_store_matches_resident_step():
+    import torch
+
+    sc = scenes.falling_block((9, 9, 9), seed=15, velocity_sigma=0.1)
+    a = solver_for(sc)
+    b = solver_for(sc)
+    pos = torch.tensor(sc.fluid, device="cuda")
+    vel = torch.tensor(sc.velocity, device="cuda")
+    rho = torch.zeros(sc.n, device="cuda")
+    for _ in range(3):
+        a.step(sc.dt)
+        b.step_store(pos.data_ptr(), vel.data_ptr(), sc.n, sc.dt, rho.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(a.positions(), pos.cpu().numpy())
+    assert np.array_equal(a.velocities(), vel.cpu().numpy())
+    assert np.array_equal(a.field(_lib.FIELD_DENSITY), rho.cpu().numpy())
+
+
+def test_edge_cases_through_the_abi():
+    sc = scenes.falling_block((4, 4, 4), seed=3)
+    s = solver_for(sc)
+    # dt must be positive
+    with pytest.raises(_lib.DfsphError):
+        s.step(0.0)
+    # capacity (ParticleStore::resize throws std::out_of_range)
+    with pytest.raises(_lib.DfsphError) as e:
+        s.set_fluid(np.zeros((sc.n + 1, 3), np.float32))
+    assert e.value.status == _lib.ERR_OUT_OF_RANGE
+    # empty fluid: step is a no-op (dfsph.cu:121-122)
+    s.set_fluid(np.zeros((0, 3), np.float32))
+    s.step(sc.dt)
+    assert s.positions().shape == (0, 3)
+    # NaN particle: the step completes, NaN shows in max_velocity
+    pts = sc.fluid.copy()
+    pts[0] = np.nan
+    s.set_fluid(pts)
+    s.step(sc.dt)
+    assert np.isnan(s.max_velocity())
+    assert np.isfinite(s.positions()[1:]).all()
+
+
+def test_settled_puddle_regression():
+    """tests/regression/test_settled_puddle.cu:119-222 on the CUDA path: a 0.4^3 m
+    block (17^3 at r = 0.012) settles within 1.5 s with adaptive dt."""
+    r = 0.012
+    s2 = 2 * r
+    xs = np.arange(0.30, 0.70 + 1e-6, s2, dtype=np.float64)
+    # the reference's float loop x += spacing (dense_block, :24-32)
+    vals = []
+    x = np.float32(0.30)
+    while x <= np.float32(0.70):
+        vals.append(x)
+        x = np.float32(x + np.float32(s2))
+    g = np.array(vals, np.float32)
+    pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    assert len(xs) == len(g) == 17
+    sc = scenes.falling_block((1, 1, 1))
+    sc.fluid, sc.velocity, sc.radius = pts, np.zeros_like(pts), r
+    sc.boundary = scenes.sample_aabb_boundary((0, 0, 0), (1, 1, 1), s2, 3)
+    sc.viscosity, sc.damping, sc.max_density_iters, sc.eta_density = 5e-2, 3.0, 10, 5e-3
+    s = solver_for(sc)
+    t, steps = 0.0, 0
+    while t < 1.5:
+        v = max(s.max_velocity(), 0.5)
+        dt = max(min(1e-3, 0.3 * r / v), 1e-5)
+        if t + dt > 1.5:
+            dt = 1.5 - t
+        s.step(dt)
+        t += dt
+        steps += 1
+    x = s.positions()
+    v = s.velocities()
+    assert np.isfinite(x).all()
+    assert np.linalg.norm(v, axis=1).max() < 5.0
+    assert x[:, 1].max() < 0.75
+    assert x[:, 1].min() >= -0.01
+    expected_mean_y = len(pts) * s2 ** 3 / 2.0
+    assert x[:, 1].mean() == pytest.approx(expected_mean_y, rel=0.5)

@@ -1,0 +1,97 @@
+"""Build recipe of the native library (libdfsph_gb300.so), in-tree.
+
+nvcc for sm_103a only; every translation unit is compiled in parallel, then
+linked into one shared library that exports the C ABI of include/dfsph_gb300.h.
+Host code is compiled with -ffp-contract=off so that host float arithmetic (grid
+geometry, boundary sampling) is identical on x86-64 and aarch64.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(PKG_DIR, "csrc")
+BUILD_DIR = os.path.join(PKG_DIR, "_build")
+LIB_PATH = os.path.join(PKG_DIR, "libdfsph_gb300.so")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_COMMON = ARCH + [
+    "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
+    "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-O2",
+    "-I", os.path.join(ROOT, "include"),
+]
+# (source, extra flags)
+CUDA_UNITS = [
+    ("capi.cu", []),
+    ("solver_fp32.cu", []),
+    ("solver_fp64.cu", []),
+    # the one unit built with the reference's fast math (see its header)
+    ("stencil_recip.cu", ["-use_fast_math"]),
+]
+CXX_UNITS = ["geometry.cpp"]
+
+
+def nvcc() -> str:
+    exe = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(exe):
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build libdfsph_gb300.so")
+    return exe
+
+
+def _sources() -> list[str]:
+    out = []
+    for d in (CSRC, os.path.join(ROOT, "include")):
+        for f in os.listdir(d):
+            if f.endswith((".cu", ".cuh", ".cpp", ".h")):
+                out.append(os.path.join(d, f))
+    return out
+
+
+def _stale(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    """Compile libdfsph_gb300.so if any source is newer; returns its path."""
+    deps = _sources()
+    if not force and not _stale(LIB_PATH, deps):
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    nv = nvcc()
+    jobs = []
+    objs = []
+    for src, extra in CUDA_UNITS:
+        obj = os.path.join(BUILD_DIR, src + ".o")
+        objs.append(obj)
+        jobs.append([nv] + NVCC_COMMON + extra + ["-c", os.path.join(CSRC, src), "-o", obj])
+    for src in CXX_UNITS:
+        obj = os.path.join(BUILD_DIR, src + ".o")
+        objs.append(obj)
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
+                     "-I", os.path.join(ROOT, "include"), "-I", "/usr/local/cuda/include",
+                     "-c", os.path.join(CSRC, src), "-o", obj])
+    with ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:
+        list(ex.map(_run, jobs))
+    tmp = LIB_PATH + ".tmp"
+    _run([nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-fPIC"])
+    os.replace(tmp, LIB_PATH)
+    if verbose:
+        print("built", LIB_PATH)
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    build(force=True, verbose=True)

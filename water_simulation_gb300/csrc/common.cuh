@@ -1,0 +1,138 @@
+// Shared device/host definitions of the GB300 DFSPH step.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+namespace dfsph {
+
+using u32 = std::uint32_t;
+using u64 = std::uint64_t;
+
+// A 4-lane vector of the working real type; 16 B for float (one LDG.128),
+// 32 B for double.
+template <class R> struct alignas(4 * sizeof(R)) R4 { R x, y, z, w; };
+
+// Status carrying exception used inside the library; converted to a status
+// code at the C ABI and never thrown across it.
+struct Error : std::runtime_error {
+    int status;
+    Error(int s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+[[noreturn]] void throw_cuda(cudaError_t e, const char* expr, const char* file, int line);
+
+#define DFSPH_CUDA(expr)                                                      \
+    do {                                                                      \
+        cudaError_t _e = (expr);                                              \
+        if (_e != cudaSuccess) ::dfsph::throw_cuda(_e, #expr, __FILE__, __LINE__); \
+    } while (0)
+
+#define DFSPH_LAUNCHED()                                                      \
+    do {                                                                      \
+        cudaError_t _e = cudaGetLastError();                                  \
+        if (_e != cudaSuccess) ::dfsph::throw_cuda(_e, "kernel launch", __FILE__, __LINE__); \
+    } while (0)
+
+// Uniform grid of the reference's make_grid (solvers/dfsph/src/dfsph.cu:55-65).
+struct GridGeom {
+    float origin[3];
+    int dims[3];
+    float cell_length;
+    u32 total;          // dims.x*dims.y*dims.z; the key of out-of-grid particles
+    float inv_bin;      // host IEEE 1.0f/cell_length: bins particles (cell_grid.cu:81)
+    float inv_stencil;  // device 1.0f/cell_length under the reference's fast math:
+                        // centres the 27-cell stencil (dfsph_kernels.cu:52,89,...)
+};
+
+GridGeom make_grid_geom(const float dmin[3], const float dmax[3], float smoothing_length);
+
+// Device-side copy of the grid with the working real type.
+template <class R> struct GridDev {
+    R ox, oy, oz;
+    int nx, ny, nz;
+    u32 total;
+    R inv_bin;
+    R inv_stencil;
+};
+
+template <class R> inline GridDev<R> to_dev(const GridGeom& g) {
+    GridDev<R> d;
+    d.ox = R(g.origin[0]); d.oy = R(g.origin[1]); d.oz = R(g.origin[2]);
+    d.nx = g.dims[0]; d.ny = g.dims[1]; d.nz = g.dims[2];
+    d.total = g.total;
+    if (sizeof(R) == sizeof(float)) {
+        d.inv_bin = R(g.inv_bin);
+        d.inv_stencil = R(g.inv_stencil);
+    } else {
+        d.inv_bin = R(1) / R(g.cell_length);
+        d.inv_stencil = R(1) / R(g.cell_length);
+    }
+    return d;
+}
+
+#ifdef __CUDACC__
+// floor + float->int with the GPU's saturating conversion (NaN -> 0), as the
+// reference's static_cast<int>(floorf(...)) compiles on the device.
+__device__ __forceinline__ int floor_to_int(float v) { return static_cast<int>(floorf(v)); }
+__device__ __forceinline__ int floor_to_int(double v) {
+    return static_cast<int>(floor(v));
+}
+
+// hash_cell (core/src/cell_grid.cu:10-22): x-major id, out of grid -> total.
+template <class R>
+__device__ __forceinline__ u32 cell_key(R px, R py, R pz, const GridDev<R>& g) {
+    const int cx = floor_to_int((px - g.ox) * g.inv_bin);
+    const int cy = floor_to_int((py - g.oy) * g.inv_bin);
+    const int cz = floor_to_int((pz - g.oz) * g.inv_bin);
+    if (cx < 0 || cx >= g.nx || cy < 0 || cy >= g.ny || cz < 0 || cz >= g.nz) return g.total;
+    return (static_cast<u32>(cx) * static_cast<u32>(g.ny) + static_cast<u32>(cy)) *
+               static_cast<u32>(g.nz) + static_cast<u32>(cz);
+}
+
+// Stencil-centre cell (dfsph_kernels.cu:15-17) clamped to [-2, dims+1]: any
+// value outside that range selects no cell on that axis, exactly as the
+// unclamped coordinate would, and the clamp keeps the +-1 arithmetic in range.
+struct Centre { int x, y, z; };
+
+template <class R>
+__device__ __forceinline__ Centre stencil_centre(R px, R py, R pz, const GridDev<R>& g) {
+    Centre c;
+    c.x = min(max(floor_to_int((px - g.ox) * g.inv_stencil), -2), g.nx + 1);
+    c.y = min(max(floor_to_int((py - g.oy) * g.inv_stencil), -2), g.ny + 1);
+    c.z = min(max(floor_to_int((pz - g.oz) * g.inv_stencil), -2), g.nz + 1);
+    return c;
+}
+
+// The reference's 27-cell stencil (ITER_NEIGHBORS, dfsph_kernels.cu:13-35)
+// visited as 9 runs: for each valid (dx, dy) the cells z-1..z+1 are adjacent
+// keys, so their particles form one contiguous range of sorted slots
+// [cs[first], cs[last+1]). Same candidate set, fewer range lookups.
+template <class R, class F>
+__device__ __forceinline__ void for_each_run(const Centre& c, const GridDev<R>& g,
+                                             const u32* __restrict__ cs, F&& f) {
+    const int z0 = max(c.z - 1, 0);
+    const int z1 = min(c.z + 1, g.nz - 1);
+    if (z0 > z1) return;
+#pragma unroll
+    for (int dx = -1; dx <= 1; ++dx) {
+        const int nx = c.x + dx;
+        if (nx < 0 || nx >= g.nx) continue;
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int ny = c.y + dy;
+            if (ny < 0 || ny >= g.ny) continue;
+            const u32 base = (static_cast<u32>(nx) * static_cast<u32>(g.ny) + static_cast<u32>(ny)) *
+                             static_cast<u32>(g.nz);
+            const u32 b = __ldg(cs + base + z0);
+            const u32 e = __ldg(cs + base + z1 + 1);
+            f(b, e);
+        }
+    }
+}
+
+#endif  // __CUDACC__
+
+}  // namespace dfsph

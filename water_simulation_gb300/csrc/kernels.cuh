@@ -1,0 +1,716 @@
+// Device kernels of the GB300 DFSPH step.
+//
+// Layout in HBM (all arrays in cell-sorted order, rebuilt every step):
+//   xk[s] = (x, y, z, kfac)   kfac = kappa / max(rho^2, 1e-9) of the running
+//                             Jacobi iteration (ping-pong between two buffers)
+//   vr[s] = (vx, vy, vz, rho)
+//   alpha[s], rho_adv[s], kap[s], kap_v[s], id[s] (original particle index)
+//   cell_start[C+1] exactly as the reference's CellGrid::cell_start()
+//   boundary: xb[s] = (x, y, z, m_b), bcs[C+1], bmask[C]
+// One thread owns one particle; every neighbour pass visits the reference's
+// 27-cell stencil as 9 contiguous runs of sorted slots, so neighbour loads walk
+// consecutive 16-byte records that the warp's other particles share in L1.
+#pragma once
+
+#include "common.cuh"
+
+namespace dfsph {
+
+template <class R> struct Phys {
+    R l;          // smoothing length (= cell length)
+    R inv_l;
+    R support2;   // (2l)^2: the spline is zero beyond it
+    R sigma;      // 1 / (pi l^3)
+    R grad_c;     // sigma / l
+    R mass;       // fluid particle mass rho0 (2r)^3
+    R rho0;
+};
+
+// Monaghan cubic spline (core/include/water/core/sph_kernels.cuh:12-41) written
+// as W = sigma w(q) and gradW = (sigma / l) w'(q) / r * r_ij for q = r/l < 2.
+template <class R> __device__ __forceinline__ R spline_w(R q) {
+    const R t = R(2) - q;
+    const R outer = R(0.25) * t * t * t;
+    const R inner = R(1) + q * q * (R(0.75) * q - R(1.5));
+    return q < R(1) ? inner : outer;
+}
+template <class R> __device__ __forceinline__ R spline_dw(R q) {
+    const R t = R(2) - q;
+    const R outer = R(-0.75) * t * t;
+    const R inner = q * (R(2.25) * q - R(3));
+    return q < R(1) ? inner : outer;
+}
+
+__device__ __forceinline__ float rsqrt_r(float v) { return rsqrtf(v); }
+__device__ __forceinline__ double rsqrt_r(double v) { return rsqrt(v); }
+
+template <class R> __device__ __forceinline__ R4<R> ld(const R4<R>* p) { return *p; }
+template <> __device__ __forceinline__ R4<float> ld(const R4<float>* p) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+    return {v.x, v.y, v.z, v.w};
+}
+
+// ---------------------------------------------------------------------------
+// Reductions: FP64 block partial sums with a deterministic last-block finish.
+// ---------------------------------------------------------------------------
+struct IterCtl {
+    double err_sum;       // sum of the last finished reduction
+    u32 stop_iter;        // iteration after which the solver stopped (~0u: running)
+    u32 blocks_done;      // last-block counter
+    u32 maxv_bits;        // max |v| as float bits (non-negative floats order as ints)
+    u32 flags;            // bit0: non-finite seen; bit1: sentinel order not canonical
+};
+
+template <int BLOCK>
+__device__ __forceinline__ double block_sum(double v, double* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int w = 0; w < BLOCK / 32; ++w) t += sh[w];
+    }
+    return t;  // valid in thread 0
+}
+
+// Thread 0 of every block calls this with the block's partial; the last block
+// to arrive sums all partials in block order, so the result does not depend on
+// block scheduling. Decides convergence: stop when (iter >= first_check) and
+// mean < threshold (dfsph.cu:254-258).
+static __device__ __forceinline__ void finish_reduction(double partial, double* partials, IterCtl* ctl,
+                                                 u32 iter, u32 first_check, double inv_n,
+                                                 double threshold) {
+    partials[blockIdx.x] = partial;
+    __threadfence();
+    const u32 done = atomicAdd(&ctl->blocks_done, 1u);
+    if (done == gridDim.x - 1) {
+        __threadfence();
+        double s = 0;
+        for (u32 b = 0; b < gridDim.x; ++b) s += *((volatile double*)&partials[b]);
+        ctl->err_sum = s;
+        ctl->blocks_done = 0;
+        if (iter >= first_check && s * inv_n < threshold) ctl->stop_iter = iter;
+        if (!(s == s)) ctl->flags |= 1u;
+    }
+}
+
+__device__ __forceinline__ bool stopped_before(const IterCtl* ctl, u32 iter) {
+    // Iteration `iter` runs only while no earlier iteration decided to stop.
+    return *((volatile const u32*)&ctl->stop_iter) < iter;
+}
+
+// ---------------------------------------------------------------------------
+// Grid build: counting sort by cell key, deterministic within a cell.
+// ---------------------------------------------------------------------------
+
+// Keys of the state in slot order, with the rank of each particle among the
+// particles of its cell (atomic, order fixed later) and the per-cell counts.
+template <class R>
+__global__ void __launch_bounds__(256) count_kernel(int n, const R4<R>* __restrict__ xk,
+                                                    GridDev<R> g, u32* __restrict__ key,
+                                                    u32* __restrict__ rank, u32* __restrict__ count) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const R4<R> p = ld(xk + s);
+    const u32 k = cell_key(p.x, p.y, p.z, g);
+    key[s] = k;
+    rank[s] = atomicAdd(count + k, 1u);
+}
+
+// Exclusive scan of count[0..m) into cell_start[0..m] in three launches without
+// inter-block waits: per-tile sums, a one-block scan of the tile sums, then the
+// per-tile scans. count is cleared on the way for the next build.
+constexpr int SCAN_BLOCK = 256;
+constexpr int SCAN_ITEMS = 16;
+constexpr int SCAN_TILE = SCAN_BLOCK * SCAN_ITEMS;
+
+static __global__ void __launch_bounds__(SCAN_BLOCK) scan_tile_sums(const u32* __restrict__ count, u32 m,
+                                                             u32* __restrict__ tile_sums) {
+    __shared__ u32 sh[SCAN_BLOCK / 32];
+    const u32 base = blockIdx.x * SCAN_TILE;
+    u32 t = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        const u32 c = base + k * SCAN_BLOCK + threadIdx.x;
+        if (c < m) t += count[c];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        u32 s = 0;
+        for (int w = 0; w < SCAN_BLOCK / 32; ++w) s += sh[w];
+        tile_sums[blockIdx.x] = s;
+    }
+}
+
+// One block: exclusive scan of n_tiles values in place; writes the total to
+// tile_sums[n_tiles].
+// It also resets the solver's iteration controls for the step when given
+// (every step's grid build runs it exactly once, before any solver kernel).
+static __global__ void __launch_bounds__(1024) scan_tile_offsets(u32* __restrict__ tile_sums, u32 n_tiles,
+                                                          IterCtl* ctl, int n_ctl) {
+    __shared__ u32 warp_tot[32];
+    __shared__ u32 carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (u32 base = 0; base < n_tiles; base += blockDim.x) {
+        const u32 i = base + threadIdx.x;
+        const u32 v = (i < n_tiles) ? tile_sums[i] : 0u;
+        u32 x = v;
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_tot[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            u32 w = (lane < (int)(blockDim.x >> 5)) ? warp_tot[lane] : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const u32 y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            warp_tot[lane] = w;  // inclusive prefix of warp totals
+        }
+        __syncthreads();
+        const u32 before = (warp > 0 ? warp_tot[warp - 1] : 0u) + carry;
+        if (i < n_tiles) tile_sums[i] = before + x - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = before + x;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        tile_sums[n_tiles] = carry;
+        for (int k = 0; k < n_ctl; ++k) {
+            ctl[k].err_sum = 0.0;
+            ctl[k].stop_iter = ~0u;
+            ctl[k].blocks_done = 0u;
+            ctl[k].maxv_bits = 0u;
+            ctl[k].flags = 0u;
+        }
+    }
+}
+
+static __global__ void __launch_bounds__(SCAN_BLOCK) scan_tiles(u32* __restrict__ count, u32 m,
+                                                         const u32* __restrict__ tile_offsets,
+                                                         u32* __restrict__ cell_start) {
+    __shared__ u32 warp_tot[SCAN_BLOCK / 32];
+    const u32 base = blockIdx.x * SCAN_TILE;
+    // Each thread owns SCAN_ITEMS consecutive cells.
+    const u32 c0 = base + threadIdx.x * SCAN_ITEMS;
+    u32 v[SCAN_ITEMS];
+    u32 t = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        const u32 c = c0 + k;
+        v[k] = (c < m) ? count[c] : 0u;
+        t += v[k];
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    u32 x = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const u32 y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    u32 wpre = 0;
+    for (int w = 0; w < warp; ++w) wpre += warp_tot[w];
+    u32 run = tile_offsets[blockIdx.x] + wpre + x - t;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        const u32 c = c0 + k;
+        if (c < m) {
+            cell_start[c] = run;
+            count[c] = 0u;
+        }
+        run += v[k];
+    }
+}
+
+// Provisional slot of every particle: cell start + atomic rank.
+static __global__ void __launch_bounds__(256) scatter_kernel(int n, const u32* __restrict__ key,
+                                                      const u32* __restrict__ rank,
+                                                      const u32* __restrict__ cell_start,
+                                                      const u32* __restrict__ id_old,
+                                                      u32* __restrict__ tmp_src, u32* __restrict__ tmp_id) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const u32 d = cell_start[key[s]] + rank[s];
+    tmp_src[d] = static_cast<u32>(s);
+    tmp_id[d] = id_old[s];
+}
+
+// Final slot = cell start + number of cell mates with a smaller original index,
+// which reproduces the reference's stable (key, index) order
+// (core/src/cell_grid.cu:98-110 sorts iota values stably). The state is
+// gathered into the new order on the way. Out-of-grid particles (key == total)
+// beyond `sentinel_cap` keep the provisional order and raise flag bit 1.
+template <class R>
+__global__ void __launch_bounds__(256) reorder_kernel(
+    int n, const u32* __restrict__ tmp_src, const u32* __restrict__ tmp_id,
+    const u32* __restrict__ key_old, const u32* __restrict__ cell_start, u32 total,
+    u32 sentinel_cap, const R4<R>* __restrict__ xk_old, const R4<R>* __restrict__ vr_old,
+    R4<R>* __restrict__ xk_new, R4<R>* __restrict__ vr_new, u32* __restrict__ id_new,
+    u32* __restrict__ key_sorted, IterCtl* ctl) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const u32 src = tmp_src[t];
+    const u32 my = tmp_id[t];
+    const u32 c = key_old[src];
+    const u32 b = cell_start[c];
+    const u32 e = (c == total) ? static_cast<u32>(n) : cell_start[c + 1];
+    u32 dst = static_cast<u32>(t);
+    if (e - b > 1) {
+        if (c == total && e - b > sentinel_cap) {
+            if (t == static_cast<int>(b)) atomicOr(&ctl->flags, 2u);
+        } else {
+            u32 r = 0;
+            for (u32 u = b; u < e; ++u) r += (tmp_id[u] < my) ? 1u : 0u;
+            dst = b + r;
+        }
+    }
+    xk_new[dst] = ld(xk_old + src);
+    vr_new[dst] = ld(vr_old + src);
+    id_new[dst] = my;
+    key_sorted[dst] = c;
+}
+
+// ---------------------------------------------------------------------------
+// Import / export between the caller's original-order AoS arrays and the
+// sorted SoA state.
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(256) import_kernel(int n, const float* __restrict__ pos,
+                                                     const float* __restrict__ vel,
+                                                     R4<R>* __restrict__ xk, R4<R>* __restrict__ vr,
+                                                     u32* __restrict__ id) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    xk[i] = {R(pos[3 * i]), R(pos[3 * i + 1]), R(pos[3 * i + 2]), R(0)};
+    if (vel)
+        vr[i] = {R(vel[3 * i]), R(vel[3 * i + 1]), R(vel[3 * i + 2]), R(0)};
+    else
+        vr[i] = {R(0), R(0), R(0), R(0)};
+    id[i] = static_cast<u32>(i);
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) export_kernel(int n, const u32* __restrict__ id,
+                                                     const R4<R>* __restrict__ xk,
+                                                     const R4<R>* __restrict__ vr,
+                                                     const R* __restrict__ alpha,
+                                                     const R* __restrict__ kap,
+                                                     const R* __restrict__ rho_adv,
+                                                     float* pos, float* vel, float* density,
+                                                     float* alpha_out, float* kappa_out,
+                                                     float* rho_adv_out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const u32 i = id[s];
+    const R4<R> p = xk[s];
+    const R4<R> v = vr[s];
+    if (pos) { pos[3 * i] = float(p.x); pos[3 * i + 1] = float(p.y); pos[3 * i + 2] = float(p.z); }
+    if (vel) { vel[3 * i] = float(v.x); vel[3 * i + 1] = float(v.y); vel[3 * i + 2] = float(v.z); }
+    if (density) density[i] = float(v.w);
+    if (alpha_out) alpha_out[i] = float(alpha[s]);
+    if (kappa_out) kappa_out[i] = float(kap[s]);
+    if (rho_adv_out) rho_adv_out[i] = float(rho_adv[s]);
+}
+
+// Scatter a per-slot array to original order (double output for FP64 reads).
+template <class T, class O>
+__global__ void __launch_bounds__(256) unsort_kernel(int n, const u32* __restrict__ id,
+                                                     const T* __restrict__ in, O* __restrict__ out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    out[id[s]] = O(in[s]);
+}
+
+template <class R, class O>
+__global__ void __launch_bounds__(256) unsort_vec_kernel(int n, const u32* __restrict__ id,
+                                                         const R4<R>* __restrict__ in, int lane,
+                                                         O* __restrict__ out) {
+    // lane < 0: xyz triple; lane in 0..3: one component
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const R4<R> v = in[s];
+    const u32 i = id[s];
+    if (lane < 0) {
+        out[3 * i] = O(v.x); out[3 * i + 1] = O(v.y); out[3 * i + 2] = O(v.z);
+    } else {
+        out[i] = O(lane == 0 ? v.x : lane == 1 ? v.y : lane == 2 ? v.z : v.w);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Boundary: Akinci mass (dfsph_kernels.cu:40-65) and the per-cell flag telling
+// whether any boundary particle lies in the 27-cell stencil of a cell.
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(128) boundary_mass_kernel(int nb, const R4<R>* __restrict__ xb_in,
+                                                            R4<R>* __restrict__ xb_out,
+                                                            const u32* __restrict__ bcs, GridDev<R> g,
+                                                            Phys<R> p) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nb) return;
+    const R4<R> pi = ld(xb_in + s);
+    const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
+    R sum_w = 0;
+    for_each_run(c, g, bcs, [&](u32 b, u32 e) {
+        for (u32 j = b; j < e; ++j) {
+            const R4<R> pj = ld(xb_in + j);
+            const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+            const R r2 = rx * rx + ry * ry + rz * rz;
+            if (r2 >= p.support2) continue;
+            const R r = r2 > R(0) ? r2 * rsqrt_r(r2) : R(0);
+            sum_w += spline_w(r * p.inv_l);
+        }
+    });
+    sum_w *= p.sigma;
+    xb_out[s] = {pi.x, pi.y, pi.z, p.rho0 / (sum_w > R(1e-9) ? sum_w : R(1e-9))};
+}
+
+template <class R>
+__global__ void __launch_bounds__(256) boundary_mask_kernel(u32 total, const u32* __restrict__ bcs,
+                                                            GridDev<R> g, unsigned char* __restrict__ mask) {
+    const u32 c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= total) return;
+    const int cz = static_cast<int>(c % static_cast<u32>(g.nz));
+    const u32 rest = c / static_cast<u32>(g.nz);
+    const int cy = static_cast<int>(rest % static_cast<u32>(g.ny));
+    const int cx = static_cast<int>(rest / static_cast<u32>(g.ny));
+    u32 any = 0;
+    for_each_run(Centre{cx, cy, cz}, g, bcs, [&](u32 b, u32 e) { any |= (e > b) ? 1u : 0u; });
+    mask[c] = static_cast<unsigned char>(any);
+}
+
+// Boundary runs of a fluid particle are visited unless its stencil centre is an
+// in-grid cell whose mask says the stencil holds no boundary particle.
+template <class R>
+__device__ __forceinline__ bool boundary_near(const Centre& c, const GridDev<R>& g,
+                                              const unsigned char* __restrict__ mask) {
+    if (c.x < 0 || c.x >= g.nx || c.y < 0 || c.y >= g.ny || c.z < 0 || c.z >= g.nz) return true;
+    const u32 cell = (static_cast<u32>(c.x) * static_cast<u32>(g.ny) + static_cast<u32>(c.y)) *
+                         static_cast<u32>(g.nz) + static_cast<u32>(c.z);
+    return __ldg(mask + cell) != 0;
+}
+
+struct BoundaryDev {
+    const void* xb;             // R4<R>*, (x, y, z, m_b), sorted
+    const u32* bcs;             // boundary cell_start
+    const unsigned char* mask;  // per cell
+    int has;
+};
+
+// ---------------------------------------------------------------------------
+// Density + alpha (density_kernel dfsph_kernels.cu:68-112 fused with
+// alpha_kernel :117-169). rho includes self (W(0)); the alpha sums skip self
+// (the gradient is zero at r = 0). KAHAN compensates the density sum.
+// ---------------------------------------------------------------------------
+template <class R, bool KAHAN, bool DIAG>
+__global__ void __launch_bounds__(128) density_alpha_kernel(
+    int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, R* __restrict__ alpha,
+    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, u32* __restrict__ nbr_f,
+    u32* __restrict__ nbr_b) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const R4<R> pi = ld(xk + i);
+    const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
+    R ws = 0, wc = 0;  // sum of W/sigma (+ compensation)
+    R gx = 0, gy = 0, gz = 0, gq = 0;
+    u32 cf = 0, cb = 0;
+    for_each_run(c, g, cs, [&](u32 b, u32 e) {
+        if (DIAG) cf += e - b;
+        for (u32 j = b; j < e; ++j) {
+            const R4<R> pj = ld(xk + j);
+            const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+            const R r2 = rx * rx + ry * ry + rz * rz;
+            if (r2 >= p.support2) continue;
+            const R rinv = r2 > R(0) ? rsqrt_r(r2) : R(0);
+            const R q = r2 * rinv * p.inv_l;
+            const R w = spline_w(q);
+            if (KAHAN) {
+                const R y = w - wc;
+                const R t = ws + y;
+                wc = (t - ws) - y;
+                ws = t;
+            } else {
+                ws += w;
+            }
+            if (r2 >= R(1e-24)) {
+                const R f = spline_dw(q) * rinv;
+                gx += f * rx; gy += f * ry; gz += f * rz;
+                gq += f * f * r2;
+            }
+        }
+    });
+    // fluid terms carry the uniform mass and sigma (and sigma/l for gradients)
+    R rho = p.mass * p.sigma * ws;
+    const R gm = p.mass * p.grad_c;
+    gx *= gm; gy *= gm; gz *= gm;
+    gq *= gm * gm;
+    if (bd.has && boundary_near(c, g, bd.mask)) {
+        const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
+        R bs = 0, bsc = 0;
+        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+            if (DIAG) cb += e - b;
+            for (u32 j = b; j < e; ++j) {
+                const R4<R> pj = ld(xb + j);
+                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+                const R r2 = rx * rx + ry * ry + rz * rz;
+                if (r2 >= p.support2) continue;
+                const R rinv = r2 > R(0) ? rsqrt_r(r2) : R(0);
+                const R q = r2 * rinv * p.inv_l;
+                const R mw = pj.w * spline_w(q);
+                if (KAHAN) {
+                    const R y = mw - bsc;
+                    const R t = bs + y;
+                    bsc = (t - bs) - y;
+                    bs = t;
+                } else {
+                    bs += mw;
+                }
+                if (r2 >= R(1e-24)) {
+                    const R f = pj.w * p.grad_c * spline_dw(q) * rinv;
+                    gx += f * rx; gy += f * ry; gz += f * rz;
+                    gq += f * f * r2;
+                }
+            }
+        });
+        rho += p.sigma * bs;
+    }
+    const R denom = gx * gx + gy * gy + gz * gz + gq;
+    R4<R> v = vr[i];
+    v.w = rho;
+    vr[i] = v;
+    alpha[i] = denom > R(1e-9) ? rho / denom : R(0);
+    if (DIAG) { nbr_f[i] = cf; nbr_b[i] = cb; }
+}
+
+// ---------------------------------------------------------------------------
+// External forces + XSPH (apply_gravity_kernel dfsph_kernels.cu:347-355, then
+// xsph_viscosity_kernel :305-341) in one Jacobi pass: v' = v e^{-d dt} + g dt
+// and, because g dt cancels in v'_j - v'_i, the XSPH term of v' equals
+// e^{-d dt} times the XSPH term of v. Reads vr_in, writes vr_out.
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(128) forces_xsph_kernel(
+    int n, const R4<R>* __restrict__ xk, const R4<R>* __restrict__ vr_in, R4<R>* __restrict__ vr_out,
+    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, R decay, R gdx, R gdy, R gdz, R eps,
+    int do_xsph) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const R4<R> vi = ld(vr_in + i);
+    R dx = 0, dy = 0, dz = 0;
+    if (do_xsph) {
+        const R4<R> pi = ld(xk + i);
+        const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
+        for_each_run(c, g, cs, [&](u32 b, u32 e) {
+            for (u32 j = b; j < e; ++j) {
+                if (j == static_cast<u32>(i)) continue;
+                const R4<R> pj = ld(xk + j);
+                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+                const R r2 = rx * rx + ry * ry + rz * rz;
+                if (r2 >= p.support2) continue;
+                const R4<R> vj = ld(vr_in + j);
+                const R rinv = r2 > R(0) ? rsqrt_r(r2) : R(0);
+                const R w = spline_w(r2 * rinv * p.inv_l);
+                const R ravg = R(0.5) * (vi.w + vj.w);
+                const R cc = w / (ravg > R(1e-9) ? ravg : R(1e-9));
+                dx += cc * (vj.x - vi.x);
+                dy += cc * (vj.y - vi.y);
+                dz += cc * (vj.z - vi.z);
+            }
+        });
+        const R s = eps * p.mass * p.sigma * decay;
+        dx *= s; dy *= s; dz *= s;
+    }
+    vr_out[i] = {vi.x * decay + gdx + dx, vi.y * decay + gdy + dy, vi.z * decay + gdz + dz, vi.w};
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi pressure iteration, first half: rho_dot = sum_j m (v_i - v_j).gradW
+// (fluid, self skipped) + sum_b m_b v_i.gradW (density_change_kernel
+// dfsph_kernels.cu:176-232). DIVERGENCE = false: rho* = rho + dt rho_dot,
+// kappa = max(0, rho* - rho0) alpha / dt^2, error term max(0, rho* - rho0).
+// DIVERGENCE = true (solver of the reference's plan): kappa_v =
+// max(0, rho_dot) alpha / dt, error term max(0, rho_dot).
+// Writes xk_out = (x, kappa / max(rho^2, 1e-9)); xk_in is not written.
+// ---------------------------------------------------------------------------
+template <class R, bool DIVERGENCE, bool REDUCE>
+__global__ void __launch_bounds__(128) pressure_rate_kernel(
+    int n, const R4<R>* __restrict__ xk_in, R4<R>* __restrict__ xk_out,
+    const R4<R>* __restrict__ vr, const R* __restrict__ alpha, R* __restrict__ rho_adv,
+    R* __restrict__ kap, const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd,
+    R dt, double* __restrict__ partials, IterCtl* ctl, u32 iter, u32 first_check, double inv_n,
+    double threshold) {
+    __shared__ double sh[4];
+    if (stopped_before(ctl, iter)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double err = 0;
+    if (i < n) {
+        const R4<R> pi = ld(xk_in + i);
+        const R4<R> vi = ld(vr + i);
+        const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
+        R rd = 0;
+        for_each_run(c, g, cs, [&](u32 b, u32 e) {
+            for (u32 j = b; j < e; ++j) {
+                if (j == static_cast<u32>(i)) continue;
+                const R4<R> pj = ld(xk_in + j);
+                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+                const R r2 = rx * rx + ry * ry + rz * rz;
+                if (r2 >= p.support2 || r2 < R(1e-24)) continue;
+                const R4<R> vj = ld(vr + j);
+                const R rinv = rsqrt_r(r2);
+                const R f = spline_dw(r2 * rinv * p.inv_l) * rinv;
+                rd += f * ((vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz);
+            }
+        });
+        rd *= p.mass * p.grad_c;
+        if (bd.has && boundary_near(c, g, bd.mask)) {
+            const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
+            R rb = 0;
+            for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+                for (u32 j = b; j < e; ++j) {
+                    const R4<R> pj = ld(xb + j);
+                    const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+                    const R r2 = rx * rx + ry * ry + rz * rz;
+                    if (r2 >= p.support2 || r2 < R(1e-24)) continue;
+                    const R rinv = rsqrt_r(r2);
+                    const R f = pj.w * spline_dw(r2 * rinv * p.inv_l) * rinv;
+                    rb += f * (vi.x * rx + vi.y * ry + vi.z * rz);
+                }
+            });
+            rd += rb * p.grad_c;
+        }
+        const R rho = vi.w;
+        R k;
+        if (!DIVERGENCE) {
+            const R rp = rho + dt * rd;
+            rho_adv[i] = rp;
+            const R over = rp - p.rho0 > R(0) ? rp - p.rho0 : R(0);
+            k = over * alpha[i] / (dt * dt);
+            err = double(over);
+        } else {
+            const R s = rd > R(0) ? rd : R(0);
+            rho_adv[i] = rd;  // the divergence solver's rho_dot scratch
+            k = s * alpha[i] / dt;
+            err = double(s);
+        }
+        kap[i] = k;
+        const R rr = rho * rho;
+        xk_out[i] = {pi.x, pi.y, pi.z, k / (rr > R(1e-9) ? rr : R(1e-9))};
+    }
+    if (REDUCE) {
+        const double t = block_sum<128>(err, sh);
+        if (threadIdx.x == 0) finish_reduction(t, partials, ctl, iter, first_check, inv_n, threshold);
+    }
+}
+
+// Second half (apply_kappa_kernel dfsph_kernels.cu:237-301):
+// v_i -= dt sum_j m (kfac_i + kfac_j) gradW over fluid (self skipped) and
+// dt sum_b m_b (kfac_i + kappa_i / max(rho0^2, 1e-9)) gradW over the boundary.
+template <class R>
+__global__ void __launch_bounds__(128) pressure_apply_kernel(
+    int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, const R* __restrict__ kap,
+    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, R dt, const IterCtl* ctl,
+    u32 iter) {
+    if (stopped_before(ctl, iter)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const R4<R> pi = ld(xk + i);
+    const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
+    R ax = 0, ay = 0, az = 0;
+    for_each_run(c, g, cs, [&](u32 b, u32 e) {
+        for (u32 j = b; j < e; ++j) {
+            if (j == static_cast<u32>(i)) continue;
+            const R4<R> pj = ld(xk + j);
+            const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+            const R r2 = rx * rx + ry * ry + rz * rz;
+            if (r2 >= p.support2 || r2 < R(1e-24)) continue;
+            const R rinv = rsqrt_r(r2);
+            const R f = (pi.w + pj.w) * spline_dw(r2 * rinv * p.inv_l) * rinv;
+            ax += f * rx; ay += f * ry; az += f * rz;
+        }
+    });
+    const R sf = -dt * p.mass * p.grad_c;
+    ax *= sf; ay *= sf; az *= sf;
+    if (bd.has && boundary_near(c, g, bd.mask)) {
+        const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
+        const R r0 = p.rho0 * p.rho0;
+        const R kb = pi.w + kap[i] / (r0 > R(1e-9) ? r0 : R(1e-9));
+        R bx = 0, by = 0, bz = 0;
+        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+            for (u32 j = b; j < e; ++j) {
+                const R4<R> pj = ld(xb + j);
+                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+                const R r2 = rx * rx + ry * ry + rz * rz;
+                if (r2 >= p.support2 || r2 < R(1e-24)) continue;
+                const R rinv = rsqrt_r(r2);
+                const R f = pj.w * spline_dw(r2 * rinv * p.inv_l) * rinv;
+                bx += f * rx; by += f * ry; bz += f * rz;
+            }
+        });
+        const R sb = -dt * kb * p.grad_c;
+        ax += sb * bx; ay += sb * by; az += sb * bz;
+    }
+    R4<R> v = vr[i];
+    v.x += ax; v.y += ay; v.z += az;
+    vr[i] = v;
+}
+
+// ---------------------------------------------------------------------------
+// Integrator (advect_kernel dfsph_kernels.cu:363-386, MAX_VELOCITY_CLAMP = 5,
+// dfsph.cu:268) fused with the max-|v| reduction (dfsph.cu:303-326) and, when
+// COUNT, the next step's cell keys and per-cell counts.
+// ---------------------------------------------------------------------------
+template <class R, bool COUNT>
+__global__ void __launch_bounds__(256) advect_kernel(
+    int n, R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, R dt, R lox, R loy, R loz, R hix,
+    R hiy, R hiz, GridDev<R> g, u32* __restrict__ key, u32* __restrict__ rank,
+    u32* __restrict__ count, IterCtl* ctl) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    u32 vbits = 0;
+    if (i < n) {
+        R4<R> v = vr[i];
+        R4<R> x = xk[i];
+        const R maxv = R(5);
+        const R sp = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+        if (sp > maxv) {
+            const R s = maxv / sp;
+            v.x *= s; v.y *= s; v.z *= s;
+        }
+        R px = x.x + v.x * dt, py = x.y + v.y * dt, pz = x.z + v.z * dt;
+        const R eps = R(1e-3);
+        if (px < lox + eps) { px = lox + eps; if (v.x < R(0)) v.x = R(0); }
+        if (py < loy + eps) { py = loy + eps; if (v.y < R(0)) v.y = R(0); }
+        if (pz < loz + eps) { pz = loz + eps; if (v.z < R(0)) v.z = R(0); }
+        if (px > hix - eps) { px = hix - eps; if (v.x > R(0)) v.x = R(0); }
+        if (py > hiy - eps) { py = hiy - eps; if (v.y > R(0)) v.y = R(0); }
+        if (pz > hiz - eps) { pz = hiz - eps; if (v.z > R(0)) v.z = R(0); }
+        vr[i] = {v.x, v.y, v.z, v.w};
+        xk[i] = {px, py, pz, R(0)};
+        const float mag = float(sqrt(v.x * v.x + v.y * v.y + v.z * v.z));
+        vbits = __float_as_uint(mag);
+        if (COUNT) {
+            const u32 k = cell_key(px, py, pz, g);
+            key[i] = k;
+            rank[i] = atomicAdd(count + k, 1u);
+        }
+    }
+    // max over the warp, then one atomic per warp (NaN bits dominate)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) vbits = max(vbits, __shfl_xor_sync(0xffffffffu, vbits, o));
+    if ((threadIdx.x & 31) == 0 && vbits) atomicMax(&ctl->maxv_bits, vbits);
+}
+
+}  // namespace dfsph

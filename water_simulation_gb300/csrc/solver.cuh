@@ -1,0 +1,463 @@
+// Host orchestration of the GB300 DFSPH step (one instantiation per working
+// real type). The stage order is DFSPHSolver::step (solvers/dfsph/src/dfsph.cu
+// :120-133): grid build, density + alpha, [divergence solve], external forces +
+// XSPH, density solve, advect + max |v|.
+#pragma once
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "solver_api.h"
+
+namespace dfsph {
+
+template <class T> struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { if (p) cudaFree(p); }
+    void alloc(size_t count) {
+        if (p) { cudaFree(p); p = nullptr; n = 0; }
+        if (count == 0) return;
+        DFSPH_CUDA(cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T)));
+        n = count;
+    }
+};
+
+inline int blocks_for(long long n, int block) { return static_cast<int>((n + block - 1) / block); }
+
+template <class R>
+class Solver final : public SolverBase {
+public:
+    using V4 = R4<R>;
+
+    Solver(const dfsph_config& cfg, int device, cudaStream_t stream)
+        : cfg_(cfg), device_(device), stream_(stream) {
+        DFSPH_CUDA(cudaSetDevice(device_));
+        geom_ = make_grid_geom(cfg_.domain_min, cfg_.domain_max, cfg_.smoothing_length);
+        geom_.inv_stencil = device_stencil_reciprocal(cfg_.smoothing_length, stream_);
+        g_ = to_dev<R>(geom_);
+        // particle mass rho0 * (2r)^3 evaluated in float (dfsph.cu:76-78)
+        const float spacing = 2.0f * cfg_.particle_radius;
+        const float v0 = spacing * spacing * spacing;
+        mass_f_ = cfg_.rest_density * v0;
+        const R l = R(cfg_.smoothing_length);
+        phys_.l = l;
+        phys_.inv_l = R(1) / l;
+        phys_.support2 = R(4) * l * l;
+        phys_.sigma = R(1) / (R(3.14159265358979323846) * l * l * l);
+        phys_.grad_c = phys_.sigma / l;
+        phys_.mass = R(mass_f_);
+        phys_.rho0 = R(cfg_.rest_density);
+
+        cap_ = cfg_.capacity;
+        bcap_ = cfg_.boundary_capacity;
+        const size_t cells = size_t(geom_.total) + 1;
+        for (int k = 0; k < 2; ++k) {
+            xk_[k].alloc(cap_);
+            vr_[k].alloc(cap_);
+            id_[k].alloc(cap_);
+        }
+        alpha_.alloc(cap_); rho_adv_.alloc(cap_); kap_.alloc(cap_); kap_v_.alloc(cap_);
+        rho_dot_.alloc(cap_);
+        key_.alloc(cap_); rank_.alloc(cap_); tmp_src_.alloc(cap_); tmp_id_.alloc(cap_);
+        key_sorted_.alloc(cap_);
+        if (cfg_.record_diagnostics) { nbr_f_.alloc(cap_); nbr_b_.alloc(cap_); }
+        count_.alloc(cells);
+        cell_start_.alloc(cells);
+        n_tiles_ = static_cast<u32>((cells + SCAN_TILE - 1) / SCAN_TILE);
+        tile_sums_.alloc(n_tiles_ + 1);
+        partials_.alloc(std::max<size_t>(1, (std::max(cap_, 1u) + 127) / 128));
+        ctl_.alloc(3);
+        staging_.alloc(std::max<size_t>(size_t(std::max(cap_, bcap_)) * 6, 6));
+        if (bcap_) {
+            for (int k = 0; k < 2; ++k) { xb_[k].alloc(bcap_); bid_[k].alloc(bcap_); }
+            bkey_.alloc(bcap_); brank_.alloc(bcap_); bkey_sorted_.alloc(bcap_);
+            btmp_src_.alloc(bcap_); btmp_id_.alloc(bcap_);
+        }
+        bcs_.alloc(cells);
+        bmask_.alloc(std::max<size_t>(geom_.total, 1));
+        DFSPH_CUDA(cudaMemsetAsync(count_.p, 0, cells * sizeof(u32), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(cell_start_.p, 0, cells * sizeof(u32), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(bcs_.p, 0, cells * sizeof(u32), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(ctl_.p, 0, 3 * sizeof(IterCtl), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(alpha_.p, 0, size_t(cap_) * sizeof(R), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(rho_adv_.p, 0, size_t(cap_) * sizeof(R), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(kap_.p, 0, size_t(cap_) * sizeof(R), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(kap_v_.p, 0, size_t(cap_) * sizeof(R), stream_));
+        if (cfg_.record_diagnostics) {
+            DFSPH_CUDA(cudaMemsetAsync(nbr_f_.p, 0, size_t(cap_) * sizeof(u32), stream_));
+            DFSPH_CUDA(cudaMemsetAsync(nbr_b_.p, 0, size_t(cap_) * sizeof(u32), stream_));
+        }
+        DFSPH_CUDA(cudaMallocHost(reinterpret_cast<void**>(&host_ctl_), 3 * sizeof(IterCtl)));
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+    }
+
+    ~Solver() override {
+        if (host_ctl_) cudaFreeHost(host_ctl_);
+    }
+
+    void set_stream(cudaStream_t s) override { stream_ = s; }
+
+    // ------------------------------------------------------------------ setup
+    void set_boundary(const float* xyz, u32 n, int mem) override {
+        if (n > bcap_) throw Error(DFSPH_ERR_OUT_OF_RANGE, "boundary count exceeds boundary_capacity");
+        nb_ = n;
+        drop_pending_counts();
+        if (n == 0) {
+            DFSPH_CUDA(cudaMemsetAsync(bcs_.p, 0, (size_t(geom_.total) + 1) * sizeof(u32), stream_));
+            return;
+        }
+        const float* src = upload(xyz, nullptr, n, mem);
+        launch_import(n, src, nullptr, xb_[0].p, vr_scratch(), bid_[0].p);
+        // sort by cell (the boundary CellGrid built once, dfsph.cu:93-97)
+        launch(count_kernel<R>, blocks_for(n, 256), 256, int(n), xb_[0].p, g_, bkey_.p, brank_.p, count_.p);
+        scan(bcs_.p, /*reset ctl*/ false);
+        launch(scatter_kernel, blocks_for(n, 256), 256, int(n), bkey_.p, brank_.p, bcs_.p, bid_[0].p,
+               btmp_src_.p, btmp_id_.p);
+        launch(reorder_kernel<R>, blocks_for(n, 256), 256, int(n), btmp_src_.p, btmp_id_.p, bkey_.p, bcs_.p,
+               geom_.total, kSentinelCap, xb_[0].p, vr_scratch(), xb_[1].p, vr_scratch2(), bid_[1].p,
+               bkey_sorted_.p, ctl_.p);
+        // Akinci mass into the w lane (dfsph_kernels.cu:40-65)
+        launch(boundary_mass_kernel<R>, blocks_for(n, 128), 128, int(n), xb_[1].p, xb_[0].p, bcs_.p, g_,
+               phys_);
+        std::swap(bid_[0].p, bid_[1].p);  // bid_[0] holds the sorted order now
+        launch(boundary_mask_kernel<R>, blocks_for(geom_.total, 256), 256, geom_.total, bcs_.p, g_,
+               bmask_.p);
+    }
+
+    void set_fluid(const float* xyz, const float* vel, u32 n, int mem) override {
+        if (n > cap_) throw Error(DFSPH_ERR_OUT_OF_RANGE, "ParticleStore::resize: count " + std::to_string(n) +
+                                                               " exceeds capacity " + std::to_string(cap_));
+        const float* pos = upload(xyz, vel, n, mem);
+        const float* v = vel ? pos + 3 * size_t(n) : nullptr;
+        if (mem == DFSPH_MEM_DEVICE) { pos = xyz; v = vel; }
+        n_ = n;
+        drop_pending_counts();
+        if (n == 0) return;
+        launch_import(n, pos, v, xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
+        counts_valid_ = false;
+        have_state_ = true;
+    }
+
+    // ------------------------------------------------------------------- step
+    void step(float dt, u32 n_steps) override {
+        for (u32 k = 0; k < n_steps; ++k) step_once(R(dt), /*count_next=*/true);
+    }
+
+    void step_store(float* pos, float* vel, u32 n, float dt, float* density, float* alpha, float* kappa,
+                    float* density_adv) override {
+        if (n > cap_) throw Error(DFSPH_ERR_OUT_OF_RANGE, "store count exceeds capacity");
+        n_ = n;
+        drop_pending_counts();
+        if (n == 0) return;  // dfsph.cu:121-122
+        launch_import(n, pos, vel, xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
+        counts_valid_ = false;
+        have_state_ = true;
+        step_once(R(dt), /*count_next=*/false);
+        launch(export_kernel<R>, blocks_for(n, 256), 256, int(n), id_[ci_].p, xk_[cx_].p, vr_[cv_].p,
+               alpha_.p, kap_.p, rho_adv_.p, pos, vel, density, alpha, kappa, density_adv);
+    }
+
+    // -------------------------------------------------------------- readback
+    void get_field(int field, void* dst, size_t bytes, int mem) override {
+        size_t need = 0;
+        const size_t n = n_, cells = size_t(geom_.total) + 1;
+        bool is_u32 = false;
+        switch (field) {
+            case DFSPH_FIELD_POSITION: case DFSPH_FIELD_VELOCITY: need = 3 * n * sizeof(float); break;
+            case DFSPH_FIELD_DENSITY: case DFSPH_FIELD_ALPHA: case DFSPH_FIELD_KAPPA:
+            case DFSPH_FIELD_DENSITY_ADV: case DFSPH_FIELD_KAPPA_V: need = n * sizeof(float); break;
+            case DFSPH_FIELD_CELL_KEY: case DFSPH_FIELD_SORTED_INDEX: case DFSPH_FIELD_NBR_FLUID:
+            case DFSPH_FIELD_NBR_BOUNDARY: need = n * sizeof(u32); is_u32 = true; break;
+            case DFSPH_FIELD_CELL_START: case DFSPH_FIELD_BOUNDARY_CELL_START:
+                need = cells * sizeof(u32); is_u32 = true; break;
+            case DFSPH_FIELD_BOUNDARY_MASS: need = size_t(nb_) * sizeof(float); break;
+            case DFSPH_FIELD_BOUNDARY_SORTED_INDEX: need = size_t(nb_) * sizeof(u32); is_u32 = true; break;
+            default: throw Error(DFSPH_ERR_INVALID_ARGUMENT, "unknown field " + std::to_string(field));
+        }
+        (void)is_u32;
+        if (bytes < need) throw Error(DFSPH_ERR_INVALID_ARGUMENT, "destination too small for field");
+        if ((field == DFSPH_FIELD_NBR_FLUID || field == DFSPH_FIELD_NBR_BOUNDARY) && !cfg_.record_diagnostics)
+            throw Error(DFSPH_ERR_STATE, "neighbour counts need record_diagnostics = 1");
+        if (need == 0) return;
+        // Produce the field in device scratch (original order), then copy out.
+        void* out = (mem == DFSPH_MEM_DEVICE) ? dst : scratch_bytes(need);
+        const int nb = blocks_for(std::max<size_t>(n, 1), 256);
+        switch (field) {
+            case DFSPH_FIELD_POSITION:
+                launch(unsort_vec_kernel<R, float>, nb, 256, int(n), id_[ci_].p, xk_[cx_].p, -1, (float*)out); break;
+            case DFSPH_FIELD_VELOCITY:
+                launch(unsort_vec_kernel<R, float>, nb, 256, int(n), id_[ci_].p, vr_[cv_].p, -1, (float*)out); break;
+            case DFSPH_FIELD_DENSITY:
+                launch(unsort_vec_kernel<R, float>, nb, 256, int(n), id_[ci_].p, vr_[cv_].p, 3, (float*)out); break;
+            case DFSPH_FIELD_ALPHA:
+                launch(unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, alpha_.p, (float*)out); break;
+            case DFSPH_FIELD_KAPPA:
+                launch(unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, kap_.p, (float*)out); break;
+            case DFSPH_FIELD_DENSITY_ADV:
+                launch(unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, rho_adv_.p, (float*)out); break;
+            case DFSPH_FIELD_KAPPA_V:
+                launch(unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, kap_v_.p, (float*)out); break;
+            case DFSPH_FIELD_CELL_KEY:
+                launch(unsort_kernel<u32, u32>, nb, 256, int(n), id_[ci_].p, key_sorted_.p, (u32*)out); break;
+            case DFSPH_FIELD_SORTED_INDEX:
+                DFSPH_CUDA(cudaMemcpyAsync(out, id_[ci_].p, need, cudaMemcpyDeviceToDevice, stream_)); break;
+            case DFSPH_FIELD_CELL_START:
+                DFSPH_CUDA(cudaMemcpyAsync(out, cell_start_.p, need, cudaMemcpyDeviceToDevice, stream_)); break;
+            case DFSPH_FIELD_BOUNDARY_CELL_START:
+                DFSPH_CUDA(cudaMemcpyAsync(out, bcs_.p, need, cudaMemcpyDeviceToDevice, stream_)); break;
+            case DFSPH_FIELD_NBR_FLUID:
+                launch(unsort_kernel<u32, u32>, nb, 256, int(n), id_[ci_].p, nbr_f_.p, (u32*)out); break;
+            case DFSPH_FIELD_NBR_BOUNDARY:
+                launch(unsort_kernel<u32, u32>, nb, 256, int(n), id_[ci_].p, nbr_b_.p, (u32*)out); break;
+            case DFSPH_FIELD_BOUNDARY_MASS:
+                launch(unsort_vec_kernel<R, float>, blocks_for(nb_, 256), 256, int(nb_), bid_[0].p, xb_[0].p, 3,
+                       (float*)out);
+                break;
+            case DFSPH_FIELD_BOUNDARY_SORTED_INDEX:
+                DFSPH_CUDA(cudaMemcpyAsync(out, bid_[0].p, need, cudaMemcpyDeviceToDevice, stream_)); break;
+        }
+        if (mem != DFSPH_MEM_DEVICE) {
+            DFSPH_CUDA(cudaMemcpyAsync(dst, out, need, cudaMemcpyDeviceToHost, stream_));
+            DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        }
+    }
+
+    double get_scalar(int which) override {
+        switch (which) {
+            case DFSPH_SCALAR_PARTICLE_MASS: return double(mass_f_);
+            case DFSPH_SCALAR_TOTAL_CELLS: return double(geom_.total);
+            case DFSPH_SCALAR_STENCIL_INV_CELL: return double(geom_.inv_stencil);
+            case DFSPH_SCALAR_FLUID_COUNT: return double(n_);
+            case DFSPH_SCALAR_BOUNDARY_COUNT: return double(nb_);
+            case DFSPH_SCALAR_KERNEL_LAUNCHES: return double(launches_);
+            default: break;
+        }
+        read_ctl();
+        switch (which) {
+            case DFSPH_SCALAR_MAX_VELOCITY: {
+                float f;
+                std::memcpy(&f, &host_ctl_[0].maxv_bits, sizeof(f));
+                return stepped_ ? double(f) : 0.0;
+            }
+            case DFSPH_SCALAR_LAST_DENSITY_ITERS:
+                return double(iters_done(host_ctl_[2], last_density_launched_));
+            case DFSPH_SCALAR_LAST_DIVERGENCE_ITERS:
+                return double(iters_done(host_ctl_[1], last_divergence_launched_));
+            case DFSPH_SCALAR_DENSITY_ERROR: return n_ ? host_ctl_[2].err_sum / double(n_) : 0.0;
+            case DFSPH_SCALAR_DIVERGENCE_ERROR: return n_ ? host_ctl_[1].err_sum / double(n_) : 0.0;
+            case DFSPH_SCALAR_FLAGS: return double(host_ctl_[0].flags | host_ctl_[1].flags | host_ctl_[2].flags);
+            default: throw Error(DFSPH_ERR_INVALID_ARGUMENT, "unknown scalar " + std::to_string(which));
+        }
+    }
+
+    void synchronize() override { DFSPH_CUDA(cudaStreamSynchronize(stream_)); }
+
+private:
+    static constexpr u32 kSentinelCap = 4096;
+
+    template <class K, class... A> void launch(K kernel, int grid, int block, A... args) {
+        if (grid <= 0) return;
+        kernel<<<grid, block, 0, stream_>>>(args...);
+        DFSPH_LAUNCHED();
+        ++launches_;
+    }
+
+    // The integrator leaves the next step's per-cell counts in count_; any new
+    // input invalidates them and count_ must be zero before the next count.
+    void drop_pending_counts() {
+        if (!counts_valid_) return;
+        DFSPH_CUDA(cudaMemsetAsync(count_.p, 0, (size_t(geom_.total) + 1) * sizeof(u32), stream_));
+        counts_valid_ = false;
+    }
+
+    // Host data goes through a device staging buffer; device data is used in place.
+    const float* upload(const float* xyz, const float* vel, u32 n, int mem) {
+        if (mem == DFSPH_MEM_DEVICE || n == 0) return xyz;
+        if (mem != DFSPH_MEM_HOST) throw Error(DFSPH_ERR_INVALID_ARGUMENT, "mem must be host or device");
+        DFSPH_CUDA(cudaMemcpyAsync(staging_.p, xyz, size_t(n) * 3 * sizeof(float), cudaMemcpyHostToDevice, stream_));
+        if (vel)
+            DFSPH_CUDA(cudaMemcpyAsync(staging_.p + 3 * size_t(n), vel, size_t(n) * 3 * sizeof(float),
+                                       cudaMemcpyHostToDevice, stream_));
+        // the caller may free its host buffer after return
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        return staging_.p;
+    }
+
+    void launch_import(u32 n, const float* pos, const float* vel, V4* xk, V4* vr, u32* id) {
+        launch(import_kernel<R>, blocks_for(n, 256), 256, int(n), pos, vel, xk, vr, id);
+    }
+
+    // Scratch 4-vectors for the boundary build: the fluid ping-pong buffers are
+    // free at that point only if no fluid state exists yet, so the boundary
+    // build uses the velocity lanes of its own xb_ buffers' partner: a
+    // dedicated pair is cheaper to reason about.
+    V4* vr_scratch() { ensure_bscratch(); return bscratch_[0].p; }
+    V4* vr_scratch2() { ensure_bscratch(); return bscratch_[1].p; }
+    void ensure_bscratch() {
+        if (bscratch_[0].n < bcap_) { bscratch_[0].alloc(bcap_); bscratch_[1].alloc(bcap_); }
+    }
+
+    void* scratch_bytes(size_t bytes) {
+        if (readback_.n < bytes) readback_.alloc(bytes);
+        return readback_.p;
+    }
+
+    void scan(u32* cell_start, bool reset_ctl) {
+        const u32 m = geom_.total + 1;
+        launch(scan_tile_sums, int(n_tiles_), SCAN_BLOCK, count_.p, m, tile_sums_.p);
+        launch(scan_tile_offsets, 1, 1024, tile_sums_.p, n_tiles_, reset_ctl ? ctl_.p : nullptr,
+               reset_ctl ? 3 : 0);
+        launch(scan_tiles, int(n_tiles_), SCAN_BLOCK, count_.p, m, tile_sums_.p, cell_start);
+    }
+
+    BoundaryDev bdev() const {
+        BoundaryDev b;
+        b.xb = xb_[0].p;
+        b.bcs = bcs_.p;
+        b.mask = bmask_.p;
+        b.has = nb_ > 0 ? 1 : 0;
+        return b;
+    }
+
+    void read_ctl() {
+        DFSPH_CUDA(cudaMemcpyAsync(host_ctl_, ctl_.p, 3 * sizeof(IterCtl), cudaMemcpyDeviceToHost, stream_));
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+    }
+
+    static u32 iters_done(const IterCtl& c, u32 launched) {
+        return c.stop_iter == ~0u ? launched : std::min(launched, c.stop_iter + 1);
+    }
+
+    // One Jacobi solve: `max_iters` iterations of (rate, apply). With eta > 0
+    // the kernels stop themselves once the mean error is below eta rho0; the
+    // host additionally stops launching after the device reports convergence.
+    template <bool DIV>
+    u32 solve(R dt, u32 max_iters, float eta, IterCtl* ctl, R* kap_out, R* adv_out) {
+        const int n = int(n_);
+        const bool adaptive = eta > 0.0f;
+        const double thr = double(eta) * double(cfg_.rest_density);
+        const u32 first_check = DIV ? 0u : 1u;  // density: from the 2nd iteration (dfsph.cu:255)
+        u32 launched = 0;
+        for (u32 it = 0; it < max_iters; ++it) {
+            if (adaptive)
+                launch(pressure_rate_kernel<R, DIV, true>, blocks_for(n, 128), 128, n, xk_[cx_].p,
+                       xk_[cx_ ^ 1].p, vr_[cv_].p, alpha_.p, adv_out, kap_out, cell_start_.p, g_, phys_,
+                       bdev(), dt, partials_.p, ctl, it, first_check, 1.0 / double(n), thr);
+            else
+                launch(pressure_rate_kernel<R, DIV, false>, blocks_for(n, 128), 128, n, xk_[cx_].p,
+                       xk_[cx_ ^ 1].p, vr_[cv_].p, alpha_.p, adv_out, kap_out, cell_start_.p, g_, phys_,
+                       bdev(), dt, partials_.p, ctl, it, first_check, 1.0 / double(n), thr);
+            cx_ ^= 1;
+            launch(pressure_apply_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p, kap_out,
+                   cell_start_.p, g_, phys_, bdev(), dt, ctl, it);
+            launched = it + 1;
+            if (adaptive && it >= first_check) {
+                // The reference reads the error back every iteration
+                // (dfsph.cu:296-299); the device already decided, the host
+                // only stops launching.
+                DFSPH_CUDA(cudaMemcpyAsync(&host_ctl_[DIV ? 1 : 2], ctl, sizeof(IterCtl),
+                                           cudaMemcpyDeviceToHost, stream_));
+                DFSPH_CUDA(cudaStreamSynchronize(stream_));
+                if (host_ctl_[DIV ? 1 : 2].stop_iter != ~0u) break;
+            }
+        }
+        return launched;
+    }
+
+    void step_once(R dt, bool count_next) {
+        if (!have_state_) throw Error(DFSPH_ERR_STATE, "no fluid state: call dfsph_set_fluid first");
+        const int n = int(n_);
+        if (n == 0) return;  // dfsph.cu:121-122
+        stepped_ = true;
+        // 1. grid build (CellGrid::build, core/src/cell_grid.cu:73-138)
+        if (!counts_valid_)
+            launch(count_kernel<R>, blocks_for(n, 256), 256, n, xk_[cx_].p, g_, key_.p, rank_.p, count_.p);
+        scan(cell_start_.p, /*reset ctl*/ true);
+        launch(scatter_kernel, blocks_for(n, 256), 256, n, key_.p, rank_.p, cell_start_.p, id_[ci_].p,
+               tmp_src_.p, tmp_id_.p);
+        launch(reorder_kernel<R>, blocks_for(n, 256), 256, n, tmp_src_.p, tmp_id_.p, key_.p, cell_start_.p,
+               geom_.total, kSentinelCap, xk_[cx_].p, vr_[cv_].p, xk_[cx_ ^ 1].p, vr_[cv_ ^ 1].p,
+               id_[ci_ ^ 1].p, key_sorted_.p, ctl_.p);
+        cx_ ^= 1; cv_ ^= 1; ci_ ^= 1;
+        counts_valid_ = false;
+        // 2. density + alpha (dfsph.cu:137-186)
+        const BoundaryDev bd = bdev();
+        const bool kahan = cfg_.precision == DFSPH_PRECISION_FP32_KAHAN;
+        if (cfg_.record_diagnostics) {
+            if (kahan)
+                launch(density_alpha_kernel<R, true, true>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
+                       alpha_.p, cell_start_.p, g_, phys_, bd, nbr_f_.p, nbr_b_.p);
+            else
+                launch(density_alpha_kernel<R, false, true>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
+                       alpha_.p, cell_start_.p, g_, phys_, bd, nbr_f_.p, nbr_b_.p);
+        } else {
+            if (kahan)
+                launch(density_alpha_kernel<R, true, false>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
+                       alpha_.p, cell_start_.p, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr);
+            else
+                launch(density_alpha_kernel<R, false, false>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
+                       alpha_.p, cell_start_.p, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr);
+        }
+        // 3. divergence solve (the reference's plan; 0 iterations = the reference)
+        last_divergence_launched_ = 0;
+        if (cfg_.max_divergence_iters > 0)
+            last_divergence_launched_ =
+                solve<true>(dt, cfg_.max_divergence_iters, cfg_.eta_divergence, ctl_.p + 1, kap_v_.p, rho_dot_.p);
+        // 4. gravity + damping + XSPH (dfsph.cu:188-213)
+        const R decay = std::exp(-R(cfg_.damping) * dt);
+        launch(forces_xsph_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p, vr_[cv_ ^ 1].p,
+               cell_start_.p, g_, phys_, decay, R(cfg_.gravity[0]) * dt, R(cfg_.gravity[1]) * dt,
+               R(cfg_.gravity[2]) * dt, R(cfg_.viscosity), cfg_.viscosity > 0.0f ? 1 : 0);
+        cv_ ^= 1;
+        // 5. density solve (dfsph.cu:215-260)
+        last_density_launched_ =
+            solve<false>(dt, cfg_.max_density_iters, cfg_.eta_density, ctl_.p + 2, kap_.p, rho_adv_.p);
+        // 6. advect + max |v| (+ next step's cell counts)
+        const R lo[3] = {R(cfg_.domain_min[0]), R(cfg_.domain_min[1]), R(cfg_.domain_min[2])};
+        const R hi[3] = {R(cfg_.domain_max[0]), R(cfg_.domain_max[1]), R(cfg_.domain_max[2])};
+        if (count_next) {
+            launch(advect_kernel<R, true>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p, dt, lo[0], lo[1],
+                   lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p);
+            counts_valid_ = true;
+        } else {
+            launch(advect_kernel<R, false>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p, dt, lo[0], lo[1],
+                   lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p);
+        }
+    }
+
+    dfsph_config cfg_;
+    int device_;
+    cudaStream_t stream_;
+    GridGeom geom_;
+    GridDev<R> g_;
+    Phys<R> phys_;
+    float mass_f_ = 0;
+    u32 cap_ = 0, bcap_ = 0, n_ = 0, nb_ = 0, n_tiles_ = 0;
+    int cx_ = 0, cv_ = 0, ci_ = 0;
+    bool counts_valid_ = false, have_state_ = false, stepped_ = false;
+    u32 last_density_launched_ = 0, last_divergence_launched_ = 0;
+    unsigned long long launches_ = 0;
+
+    DevBuf<V4> xk_[2], vr_[2], xb_[2], bscratch_[2];
+    DevBuf<u32> id_[2], bid_[2];
+    DevBuf<R> alpha_, rho_adv_, kap_, kap_v_, rho_dot_;
+    DevBuf<u32> key_, rank_, tmp_src_, tmp_id_, key_sorted_, nbr_f_, nbr_b_;
+    DevBuf<u32> bkey_, brank_, bkey_sorted_, btmp_src_, btmp_id_;
+    DevBuf<u32> count_, cell_start_, tile_sums_, bcs_;
+    DevBuf<unsigned char> bmask_;
+    DevBuf<double> partials_;
+    DevBuf<IterCtl> ctl_;
+    DevBuf<float> staging_;
+    DevBuf<unsigned char> readback_;
+    IterCtl* host_ctl_ = nullptr;
+};
+
+}  // namespace dfsph

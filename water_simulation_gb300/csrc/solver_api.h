@@ -1,0 +1,40 @@
+// Interface between the C ABI layer and the per-precision solvers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <memory>
+
+#include "../../include/dfsph_gb300.h"
+
+namespace dfsph {
+
+// The device reciprocal 1.0f / l as the reference's stencil code evaluates it
+// (compiled with the reference's -use_fast_math in its own translation unit).
+float device_stencil_reciprocal(float cell_length, cudaStream_t stream);
+
+// Polymorphic face of the per-precision solvers.
+struct SolverBase {
+    virtual ~SolverBase() = default;
+    virtual void set_stream(cudaStream_t s) = 0;
+    virtual void set_boundary(const float* xyz, std::uint32_t n, int mem) = 0;
+    virtual void set_fluid(const float* xyz, const float* vel, std::uint32_t n, int mem) = 0;
+    virtual void step(float dt, std::uint32_t n_steps) = 0;
+    virtual void step_store(float* pos, float* vel, std::uint32_t n, float dt, float* density, float* alpha,
+                            float* kappa, float* density_adv) = 0;
+    virtual void get_field(int field, void* dst, std::size_t bytes, int mem) = 0;
+    virtual double get_scalar(int which) = 0;
+    virtual void synchronize() = 0;
+};
+
+std::unique_ptr<SolverBase> make_solver_fp32(const dfsph_config& cfg, int device, cudaStream_t s);
+std::unique_ptr<SolverBase> make_solver_fp64(const dfsph_config& cfg, int device, cudaStream_t s);
+
+// CellGrid::build (core/src/cell_grid.cu:73-138) on an arbitrary grid.
+void build_cell_grid(const float* xyz, std::uint32_t n, const float origin[3], const int dims[3],
+                     float cell_length, std::uint32_t* sorted_keys, std::uint32_t* sorted_idx,
+                     std::uint32_t* cell_start, cudaStream_t st);
+
+}  // namespace dfsph

@@ -1,0 +1,174 @@
+"""Python face of the C ABI: one DFSPH context on one GPU.
+
+Mirrors the reference's water::solvers::DFSPHSolver
+(solvers/dfsph/include/water/solvers/dfsph.h:17-51) for tests, benchmarks and
+scripting: construct from a config, give it boundary and fluid particles, call
+step(dt), read fields back. All compute happens in libdfsph_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+_FIELD_DTYPE = {
+    _lib.FIELD_POSITION: (np.float32, 3),
+    _lib.FIELD_VELOCITY: (np.float32, 3),
+    _lib.FIELD_DENSITY: (np.float32, 1),
+    _lib.FIELD_ALPHA: (np.float32, 1),
+    _lib.FIELD_KAPPA: (np.float32, 1),
+    _lib.FIELD_DENSITY_ADV: (np.float32, 1),
+    _lib.FIELD_KAPPA_V: (np.float32, 1),
+    _lib.FIELD_CELL_KEY: (np.uint32, 1),
+    _lib.FIELD_SORTED_INDEX: (np.uint32, 1),
+    _lib.FIELD_NBR_FLUID: (np.uint32, 1),
+    _lib.FIELD_NBR_BOUNDARY: (np.uint32, 1),
+}
+
+
+class Solver:
+    def __init__(self, config: _lib.DfsphConfig, device: int = 0, stream: int | None = None):
+        self._lib = _lib.load()
+        self.config = config
+        ptr = ctypes.c_void_p()
+        st = self._lib.dfsph_create(ctypes.byref(config), device, ctypes.c_void_p(stream or 0), ctypes.byref(ptr))
+        _lib.check(st, None)
+        self._ctx = ptr
+        origin = (ctypes.c_float * 3)()
+        dims = (ctypes.c_int * 3)()
+        self._lib.dfsph_grid_geometry(ctypes.byref(config), origin, dims)
+        self.origin = tuple(origin)
+        self.dims = tuple(dims)
+        self.total_cells = dims[0] * dims[1] * dims[2]
+        self.n = 0
+        self.nb = 0
+
+    # -- lifecycle ---------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_ctx", None):
+            self._lib.dfsph_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, st: int) -> None:
+        _lib.check(st, self._ctx)
+
+    # -- inputs --------------------------------------------------------------
+    def set_boundary(self, xyz: np.ndarray) -> None:
+        xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+        self._check(self._lib.dfsph_set_boundary(self._ctx, xyz.ctypes.data_as(ctypes.c_void_p),
+                                                 xyz.shape[0], _lib.MEM_HOST))
+        self.nb = xyz.shape[0]
+
+    def set_fluid(self, xyz: np.ndarray, vel: np.ndarray | None = None) -> None:
+        xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+        vp = None
+        if vel is not None:
+            vel = np.ascontiguousarray(vel, dtype=np.float32).reshape(-1, 3)
+            vp = vel.ctypes.data_as(ctypes.c_void_p)
+        self._check(self._lib.dfsph_set_fluid(self._ctx, xyz.ctypes.data_as(ctypes.c_void_p), vp,
+                                              xyz.shape[0], _lib.MEM_HOST))
+        self.n = xyz.shape[0]
+
+    def set_fluid_device(self, xyz_ptr: int, vel_ptr: int | None, n: int) -> None:
+        self._check(self._lib.dfsph_set_fluid(self._ctx, ctypes.c_void_p(xyz_ptr),
+                                              ctypes.c_void_p(vel_ptr) if vel_ptr else None, n,
+                                              _lib.MEM_DEVICE))
+        self.n = n
+
+    # -- stepping ----------------------------------------------------------
+    def step(self, dt: float, n_steps: int = 1) -> None:
+        self._check(self._lib.dfsph_step(self._ctx, ctypes.c_float(dt), n_steps))
+
+    def step_store(self, pos_ptr: int, vel_ptr: int, n: int, dt: float, density_ptr=0, alpha_ptr=0,
+                   kappa_ptr=0, density_adv_ptr=0) -> None:
+        vp = lambda p: ctypes.c_void_p(p) if p else None  # noqa: E731
+        self._check(self._lib.dfsph_step_store(self._ctx, vp(pos_ptr), vp(vel_ptr), n, ctypes.c_float(dt),
+                                               vp(density_ptr), vp(alpha_ptr), vp(kappa_ptr),
+                                               vp(density_adv_ptr)))
+
+    def synchronize(self) -> None:
+        self._check(self._lib.dfsph_synchronize(self._ctx))
+
+    def set_stream(self, stream: int) -> None:
+        self._check(self._lib.dfsph_set_stream(self._ctx, ctypes.c_void_p(stream)))
+
+    # -- outputs -------------------------------------------------------------
+    def field(self, which: int) -> np.ndarray:
+        if which in (_lib.FIELD_CELL_START, _lib.FIELD_BOUNDARY_CELL_START):
+            out = np.empty(self.total_cells + 1, dtype=np.uint32)
+        elif which == _lib.FIELD_BOUNDARY_MASS:
+            out = np.empty(self.nb, dtype=np.float32)
+        elif which == _lib.FIELD_BOUNDARY_SORTED_INDEX:
+            out = np.empty(self.nb, dtype=np.uint32)
+        else:
+            dt, w = _FIELD_DTYPE[which]
+            out = np.empty((self.n, 3) if w == 3 else self.n, dtype=dt)
+        if out.size == 0:
+            return out
+        self._check(self._lib.dfsph_get_field(self._ctx, which, out.ctypes.data_as(ctypes.c_void_p),
+                                              out.nbytes, _lib.MEM_HOST))
+        return out
+
+    def field_device(self, which: int, dst_ptr: int, nbytes: int) -> None:
+        self._check(self._lib.dfsph_get_field(self._ctx, which, ctypes.c_void_p(dst_ptr), nbytes,
+                                              _lib.MEM_DEVICE))
+
+    def scalar(self, which: int) -> float:
+        v = ctypes.c_double()
+        self._check(self._lib.dfsph_get_scalar(self._ctx, which, ctypes.byref(v)))
+        return v.value
+
+    # reference accessor names (dfsph.h:40-51)
+    def max_velocity(self) -> float:
+        return self.scalar(_lib.SCALAR_MAX_VELOCITY)
+
+    def particle_mass(self) -> float:
+        return self.scalar(_lib.SCALAR_PARTICLE_MASS)
+
+    def last_density_iters(self) -> int:
+        return int(self.scalar(_lib.SCALAR_LAST_DENSITY_ITERS))
+
+    def last_divergence_iters(self) -> int:
+        return int(self.scalar(_lib.SCALAR_LAST_DIVERGENCE_ITERS))
+
+    def density_at(self, i: int) -> float:
+        return float(self.field(_lib.FIELD_DENSITY)[i])
+
+    def alpha_at(self, i: int) -> float:
+        return float(self.field(_lib.FIELD_ALPHA)[i])
+
+    def boundary_mass_at(self, i: int) -> float:
+        return float(self.field(_lib.FIELD_BOUNDARY_MASS)[i])
+
+    def kernel_launches(self) -> int:
+        return int(self.scalar(_lib.SCALAR_KERNEL_LAUNCHES))
+
+    def positions(self) -> np.ndarray:
+        return self.field(_lib.FIELD_POSITION)
+
+    def velocities(self) -> np.ndarray:
+        return self.field(_lib.FIELD_VELOCITY)
+
+
+def solver_for(scene, precision: int = _lib.PRECISION_FP32, diagnostics: bool = False, device: int = 0,
+               stream: int | None = None) -> Solver:
+    """A context loaded with a Scene's boundary and fluid."""
+    s = Solver(scene.config(precision=precision, diagnostics=diagnostics), device=device, stream=stream)
+    if scene.nb:
+        s.set_boundary(scene.boundary)
+    s.set_fluid(scene.fluid, scene.velocity)
+    return s
