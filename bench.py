@@ -3,11 +3,29 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--workload dam1m|dam128k|puddle]
 
-A step is one DFSPHSolver::step of the whole scene. The workload is the dam
-break at scale (80 x 160 x 80 = 1,024,000 fluid particles, r = 0.0025 m, 766,098
-wall particles, dt = 2.5e-4 s) in the reference's mode: 4 fixed density
-iterations (eta = 0) and no divergence iterations, synthetic seeded inputs.
-One JSON line is printed by rank 0.
+A step is one DFSPHSolver::step of the whole scene. The default workload is the
+dam break at scale: an 80 x 160 x 80 column (1,024,000 fluid particles,
+r = 0.0025 m) against the x = 0 wall of a 1.6 x 1.0 x 0.6 m tank sampled by
+766,098 wall particles, dt = 2.5e-4 s, in the reference's step: 4 fixed density
+iterations (eta = 0), no divergence iterations. Inputs are seeded synthetic
+(water_simulation_gb300.scenes). Rank 0 prints one JSON line.
+
+value      device time of K steps (CUDA events on the solver's stream), inputs
+           resident in HBM; L2 flushed (256 MB write) before every timed step.
+e2e        the same metric through the C ABI with host buffers: every step
+           uploads x, v from pinned host memory (dfsph_set_fluid), steps, and
+           reads x, v back (dfsph_get_field).
+roofline   the dominant kernel class, timed live with CUDA events during the
+           timed steps; algorithmic bytes per launch from the per-stage byte
+           counts (x, v, rho, alpha, kappa read/written once, 16 B per active
+           wall particle), against the measured HBM copy bandwidth.
+cpu_baseline  the FP32 C++/OpenMP restatement of the reference step (oracle/)
+           on all host cores, on a bounded sample of the same workload.
+ref_cuda   the reference's own CUDA kernels (compiled from its sources for
+           sm_103a, oracle/_ref) under its restated host orchestration, timed on
+           the same GPU in the same run.
+--impl reference  the reference arm: the reference step has no CPU code, so the
+           arm times the FP32 restatement (kind "port") on all host cores.
 """
 from __future__ import annotations
 
@@ -24,6 +42,13 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+FALLBACK_HBM_GBS = 6800.0
+
+# DRAM bytes (read + write) per particle of one launch of each kernel class,
+# from `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum` on the 1M dam
+# break (profiles/dfsph_kernels_dam1m.md). None until captured.
+NCU_TRAFFIC_PER_PARTICLE: dict = {}
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -33,6 +58,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="dam1m", choices=["dam1m", "dam128k", "puddle"])
     ap.add_argument("--no-ref-cuda", action="store_true", help="skip timing the reference CUDA kernels")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
 
 
@@ -48,12 +75,40 @@ def make_scene(name):
     return sc
 
 
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def algorithmic_bytes(kclass: str, n: int, nb_active: int, cells: int) -> float | None:
+    """Bytes one launch must move at minimum (x 12, v 12, rho/alpha/kappa 4 B,
+    each array once; 16 B (x, m_b) per wall particle near the fluid)."""
+    per = {
+        "density_alpha": 20 * n + 16 * nb_active,     # x -> rho, alpha
+        "pressure_rate": 40 * n + 16 * nb_active,     # x, v, rho, alpha -> kappa, rho*
+        "pressure_apply": 44 * n + 16 * nb_active,    # x, v, rho, kappa -> v
+        "forces_xsph": 40 * n,                        # x, v, rho -> v
+        "advect": 48 * n,                             # x, v -> x, v
+        "grid_count": 20 * n,                         # x -> key, rank
+        "grid_scatter": 12 * n,
+        "grid_reorder": 56 * n,                       # x, v, id -> sorted x, v, id
+        "grid_scan": 8 * (cells + 1),                 # counts -> cell_start
+    }
+    return per.get(kclass)
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
               "clocks_event_reasons.sw_power_cap")
+    NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self, index=0):
         self.index = index
@@ -83,35 +138,79 @@ class ClockSampler:
         self._t.join(timeout=10)
 
     def summary(self):
-        if not self.samples:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        smax = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for s in self.samples for k in range(4)
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [v for v in (num(s[0]) for s in self.samples) if v is not None]
+        smax = [v for v in (num(s[1]) for s in self.samples if len(s) > 1) if v is not None]
+        reasons = sorted({self.NAMES[k] for s in self.samples for k in range(4)
                           if len(s) > 3 + k and s[3 + k].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def bench_ours(args, rank, world):
+    """Replicas only: every rank steps its own copy of the scene on its own GPU."""
     import torch
 
     from water_simulation_gb300 import _build, _lib
     from water_simulation_gb300.solver import solver_for
 
     _build.build()
-    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
+    local = int(os.environ.get("LOCAL_RANK", rank)) if world > 1 else 0
+    torch.cuda.set_device(local)
     sc = make_scene(args.workload)
     stream = torch.cuda.current_stream()
-    s = solver_for(sc, stream=stream.cuda_stream)
+    s = solver_for(sc, stream=stream.cuda_stream, device=local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    # warm-up, with every kernel class profiled to find the dominant one
+    s.profile_enable((1 << _lib.KERNEL_CLASSES) - 1)
     for _ in range(args.warmup):
+        flush.zero_()
         s.step(sc.dt)
     torch.cuda.synchronize()
+    share = {}
+    for k in range(_lib.KERNEL_CLASSES):
+        share[_lib.KERNEL_NAMES[k]] = s.profile_read(k)
+    dominant = max(share, key=lambda k: share[k][0])
+    dom_id = _lib.KERNEL_NAMES.index(dominant)
+    s.profile_enable(1 << dom_id)
+    nb_active = s.active_boundary()
     l0 = s.kernel_launches()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    with ClockSampler() as clk:
+    barrier(world)
+    with ClockSampler(local) as clk:
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for k in range(args.steps):
@@ -121,12 +220,77 @@ def bench_ours(args, rank, world):
             ev[k][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
-    ms = sum(a.elapsed_time(b) for a, b in ev)
+    barrier(world)
     launches = s.kernel_launches() - l0
-    res = {"ms_total": ms, "ms_per_step": ms / args.steps, "wall_s": wall, "launches": launches,
-           "clocks": clk.summary(), "n": sc.n, "nb": sc.nb}
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    dom_ms, dom_launches = s.profile_read(dom_id)
+    s.profile_enable(0)
+    res = {"ms_total": max_over_ranks(ms, world), "wall_s": wall, "launches": launches, "clocks": clk.summary(),
+           "dominant": dominant, "dominant_ms": dom_ms, "dominant_launches": dom_launches,
+           "nb_active": nb_active,
+           "warmup_share": {k: round(v[0] / max(sum(x[0] for x in share.values()), 1e-9), 4)
+                            for k, v in share.items() if v[1]}}
+    if not args.no_e2e:
+        res["e2e"] = bench_e2e(s, sc, max(3, min(args.steps, 20)))
     s.close()
     return sc, res
+
+
+def bench_e2e(s, sc, steps):
+    """Host buffers in, host buffers out, every step, through the C ABI."""
+    import torch
+
+    from water_simulation_gb300 import _lib
+
+    x = torch.from_numpy(sc.fluid.copy()).pin_memory()
+    v = torch.from_numpy(sc.velocity.copy()).pin_memory()
+    lib = s._lib
+    import ctypes
+
+    nbytes = x.numel() * 4
+    # one untimed round trip
+    for k in range(2):
+        s._check(lib.dfsph_set_fluid(s._ctx, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(v.data_ptr()), sc.n,
+                                     _lib.MEM_HOST))
+        s.step(sc.dt)
+        s._check(lib.dfsph_get_field(s._ctx, _lib.FIELD_POSITION, ctypes.c_void_p(x.data_ptr()), nbytes,
+                                     _lib.MEM_HOST))
+        s._check(lib.dfsph_get_field(s._ctx, _lib.FIELD_VELOCITY, ctypes.c_void_p(v.data_ptr()), nbytes,
+                                     _lib.MEM_HOST))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        s._check(lib.dfsph_set_fluid(s._ctx, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(v.data_ptr()), sc.n,
+                                     _lib.MEM_HOST))
+        s.step(sc.dt)
+        s._check(lib.dfsph_get_field(s._ctx, _lib.FIELD_POSITION, ctypes.c_void_p(x.data_ptr()), nbytes,
+                                     _lib.MEM_HOST))
+        s._check(lib.dfsph_get_field(s._ctx, _lib.FIELD_VELOCITY, ctypes.c_void_p(v.data_ptr()), nbytes,
+                                     _lib.MEM_HOST))
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    return {"value": sc.n * steps / sec, "unit": "particle-steps/s", "h2d_bytes_per_step": 2 * nbytes,
+            "d2h_bytes_per_step": 2 * nbytes, "steps": steps}
+
+
+def cpu_sample(sc, steps, threads=0):
+    """The FP32 restatement of the reference step on the host cores."""
+    from oracle import oracle as O
+
+    c = O.config_from(sc.config())
+    L = O.load()
+    if threads:
+        L.oracle_set_threads(threads)
+    cores = L.oracle_max_threads()
+    o = O.Oracle(c, sc.fluid, sc.velocity, sc.boundary, precision=32)
+    o.step(sc.dt, 1)  # warm the arrays
+    t0 = time.perf_counter()
+    o.step(sc.dt, steps)
+    sec = time.perf_counter() - t0
+    o.close()
+    return {"value": sc.n * steps / sec, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{steps} full steps of the {sc.n}-particle workload after 1 untimed step",
+            "ms_per_step": 1e3 * sec / steps}
 
 
 def bench_ref_cuda(sc, steps):
@@ -134,7 +298,7 @@ def bench_ref_cuda(sc, steps):
     from oracle import reference as R
 
     if not R.available():
-        return None
+        return {"unavailable": "reference kernels (oracle/_ref fatbins) not present"}
     from water_simulation_gb300 import _lib
     from water_simulation_gb300.solver import Solver
 
@@ -147,40 +311,105 @@ def bench_ref_cuda(sc, steps):
     ms = ref.time_steps(sc.dt, steps)
     ref.close()
     return {"value": sc.n * steps / (ms * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms / steps,
-            "steps": steps}
+            "steps": steps, "kind": "reference kernels from its sources, sm_103a, same GPU"}
+
+
+def reference_arm(args, rank, world):
+    """The reference arm: the reference step has no CPU implementation, so the
+    arm times the FP32 restatement (oracle/) on all host cores, rank 0 only."""
+    if rank != 0:
+        return None
+    sc = make_scene(args.workload)
+    from oracle import oracle as O
+
+    c = O.config_from(sc.config())
+    L = O.load()
+    cores = L.oracle_max_threads()
+    o = O.Oracle(c, sc.fluid, sc.velocity, sc.boundary, precision=32)
+    budget_s = 150.0
+    for _ in range(min(args.warmup, 1)):
+        o.step(sc.dt, 1)
+    t0 = time.perf_counter()
+    done = 0
+    for _ in range(args.steps):
+        o.step(sc.dt, 1)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    sec = time.perf_counter() - t0
+    val = sc.n * done / sec
+    return {
+        "impl": "reference", "metric": "particle-steps/s @1M dam break", "value": val, "unit": "particle-steps/s",
+        "n_gpus": world, "steps": done, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * sec / max(done, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": sc.name, "particles": sc.n, "boundary_particles": sc.nb,
+                   "density_iters": sc.max_density_iters, "divergence_iters": sc.max_divergence_iters, "dt": sc.dt},
+        "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{done} full steps of the {sc.n}-particle workload (bounded to {budget_s:.0f} s)"},
+        "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
 
 
 def main():
     args = parse()
-    rank = int(os.environ.get("RANK", 0))
-    world = int(os.environ.get("WORLD_SIZE", 1))
+    rank, world = dist_setup(args)
     if args.impl == "reference":
-        print(json.dumps({"impl": "reference", "unavailable": "CPU baseline arm not wired yet"}))
+        line = reference_arm(args, rank, world)
+        if line is not None:
+            print(json.dumps(line), flush=True)
         return
     sc, res = bench_ours(args, rank, world)
+    hbm, hbm_src = peaks()
+    cells = 1
+    for d in (int(np.ceil(np.float32(np.float32(sc.domain_max[a]) - np.float32(sc.domain_min[a])) /
+                          np.float32(2 * np.float32(sc.radius)))) + 2 for a in range(3)):
+        cells *= d
+    dom = res["dominant"]
+    alg = algorithmic_bytes(dom, sc.n, res["nb_active"], cells)
+    avg_ms = res["dominant_ms"] / max(res["dominant_launches"], 1)
+    achieved = alg / (avg_ms * 1e-3) / 1e9 if alg else None
+    traffic = NCU_TRAFFIC_PER_PARTICLE.get(dom)
     line = {
         "metric": "particle-steps/s @1M dam break",
-        "value": sc.n * args.steps / (res["ms_total"] * 1e-3),
+        "value": sc.n * args.steps * world / (res["ms_total"] * 1e-3),
         "unit": "particle-steps/s",
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": res["ms_per_step"],
+        "ms_per_step": res["ms_total"] / args.steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32",
-        "data": "synthetic",
+        "data": "synthetic (seeded lattice + SplitMix64 jitter, water_simulation_gb300/scenes.py)",
         "config": {"workload": sc.name, "particles": sc.n, "boundary_particles": sc.nb,
                    "density_iters": sc.max_density_iters, "divergence_iters": sc.max_divergence_iters,
-                   "dt": sc.dt, "l2": "flushed between timed steps (256 MB write)"},
+                   "dt": sc.dt, "parallelism": f"replicas x{world}",
+                   "l2": "flushed before every timed step (256 MB write)"},
         "gpu_launches": res["launches"],
         "clocks": res["clocks"],
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None,
+                     "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else "fallback",
+                     "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_ms,
+                     "traffic": (traffic * sc.n) if traffic else None,
+                     "active_boundary_particles": res["nb_active"]},
+        "kernel_share_warmup": res["warmup_share"],
     }
-    if not args.no_ref_cuda:
-        line["ref_cuda"] = bench_ref_cuda(sc, 3 if sc.n > 500000 else 10)
+    if "e2e" in res:
+        line["e2e"] = res["e2e"]
+    if rank == 0 and not args.no_cpu:
+        try:
+            line["cpu_baseline"] = cpu_sample(sc, 1 if sc.n > 500000 else 3)
+        except Exception as e:  # the baseline is a report, not the product
+            line["cpu_baseline"] = {"unavailable": str(e)[:200]}
+    if rank == 0 and not args.no_ref_cuda:
+        try:
+            line["ref_cuda"] = bench_ref_cuda(sc, 3 if sc.n > 500000 else 10)
+        except Exception as e:
+            line["ref_cuda"] = {"unavailable": str(e)[:200]}
     if rank == 0:
-        print(json.dumps(line))
+        print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

@@ -104,6 +104,23 @@ typedef struct dfsph_ctx dfsph_ctx;
 #define DFSPH_SCALAR_FLAGS                11  /* bit0: a convergence sum was NaN; bit1: more than
                                                  4096 out-of-grid particles, kept in arrival order */
 
+#define DFSPH_SCALAR_ACTIVE_BOUNDARY      12  /* boundary particles with a fluid particle within
+                                                 2h of them (counted on demand, last grid) */
+
+/* Kernel classes for dfsph_profile_* (bit k of the mask selects class k). */
+#define DFSPH_KERNEL_GRID_COUNT       0   /* cell keys + per-cell counts          */
+#define DFSPH_KERNEL_GRID_SCAN        1   /* cell_start scan (3 launches)          */
+#define DFSPH_KERNEL_GRID_SCATTER     2   /* provisional slots                    */
+#define DFSPH_KERNEL_GRID_REORDER     3   /* canonical order + state gather       */
+#define DFSPH_KERNEL_DENSITY_ALPHA    4   /* density + alpha                      */
+#define DFSPH_KERNEL_PRESSURE_RATE    5   /* Jacobi first half (rho*, kappa)       */
+#define DFSPH_KERNEL_PRESSURE_APPLY   6   /* Jacobi second half (dv)               */
+#define DFSPH_KERNEL_FORCES_XSPH      7   /* gravity + damping + XSPH              */
+#define DFSPH_KERNEL_ADVECT           8   /* integrator + max |v| (+ next counts)  */
+#define DFSPH_KERNEL_IO               9   /* import / export / readback           */
+#define DFSPH_KERNEL_OTHER           10
+#define DFSPH_KERNEL_CLASSES         11
+
 /* Reference defaults of DFSPHSolver::Config (dfsph.h:19-33). */
 int dfsph_config_init(dfsph_config* cfg);
 
@@ -143,6 +160,14 @@ int dfsph_step_store(dfsph_ctx* ctx, float* pos, float* vel, uint32_t n, float d
  * whole arrays). dst_bytes is checked against the field's size. */
 int dfsph_get_field(dfsph_ctx* ctx, int field, void* dst, size_t dst_bytes, int mem);
 int dfsph_get_scalar(dfsph_ctx* ctx, int which, double* out);
+
+/* Per-kernel device timing with CUDA events on the context's stream (no
+ * counterpart in the reference, which has no instrumentation). Launches of the
+ * classes in `mask` are bracketed by events until the mask is cleared;
+ * dfsph_profile_read() synchronises, sums the recorded durations of one class
+ * and forgets them. */
+int dfsph_profile_enable(dfsph_ctx* ctx, uint32_t mask);
+int dfsph_profile_read(dfsph_ctx* ctx, int kernel_class, double* total_ms, uint64_t* launches);
 
 /* Wait for the context's stream; returns a pending device error if any. */
 int dfsph_synchronize(dfsph_ctx* ctx);

@@ -34,21 +34,22 @@
 #include <string>
 #include <vector>
 
+// Same layout as oracle::Config (dfsph_oracle.cpp); stencil_inv_cell unused.
+// Declared outside the anonymous namespace: the extern "C" entry points take it.
+struct RefConfig {
+    float rest_density, particle_radius, smoothing_length, viscosity, damping, surface_tension;
+    float gravity[3];
+    std::uint32_t max_density_iters, max_divergence_iters;
+    float eta_density, eta_divergence;
+    float domain_min[3], domain_max[3];
+    float stencil_inv_cell;
+};
+
 namespace {
 
 using u32 = std::uint32_t;
 struct Vec3f { float x, y, z; };
 struct Vec3i { int x, y, z; };
-
-// Same layout as oracle::Config (dfsph_oracle.cpp); stencil_inv_cell unused.
-struct RefConfig {
-    float rest_density, particle_radius, smoothing_length, viscosity, damping, surface_tension;
-    float gravity[3];
-    u32 max_density_iters, max_divergence_iters;
-    float eta_density, eta_divergence;
-    float domain_min[3], domain_max[3];
-    float stencil_inv_cell;
-};
 
 struct Fail : std::runtime_error {
     using std::runtime_error::runtime_error;

@@ -55,6 +55,22 @@ SCALAR_FLUID_COUNT = 8
 SCALAR_BOUNDARY_COUNT = 9
 SCALAR_KERNEL_LAUNCHES = 10
 SCALAR_FLAGS = 11
+SCALAR_ACTIVE_BOUNDARY = 12
+
+KERNEL_GRID_COUNT = 0
+KERNEL_GRID_SCAN = 1
+KERNEL_GRID_SCATTER = 2
+KERNEL_GRID_REORDER = 3
+KERNEL_DENSITY_ALPHA = 4
+KERNEL_PRESSURE_RATE = 5
+KERNEL_PRESSURE_APPLY = 6
+KERNEL_FORCES_XSPH = 7
+KERNEL_ADVECT = 8
+KERNEL_IO = 9
+KERNEL_OTHER = 10
+KERNEL_CLASSES = 11
+KERNEL_NAMES = ["grid_count", "grid_scan", "grid_scatter", "grid_reorder", "density_alpha", "pressure_rate",
+                "pressure_apply", "forces_xsph", "advect", "io", "other"]
 
 
 class DfsphConfig(ctypes.Structure):
@@ -96,6 +112,9 @@ _SIGNATURES = [
     ("dfsph_get_field", ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_int]),
     ("dfsph_get_scalar", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("dfsph_synchronize", ctypes.c_int, [_P]),
+    ("dfsph_profile_enable", ctypes.c_int, [_P, ctypes.c_uint32]),
+    ("dfsph_profile_read", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_uint64)]),
     ("dfsph_last_error", ctypes.c_char_p, [_P]),
     ("dfsph_status_string", ctypes.c_char_p, [ctypes.c_int]),
     ("dfsph_sample_aabb_boundary", ctypes.c_int64,

@@ -208,6 +208,22 @@ int dfsph_get_scalar(dfsph_ctx* ctx, int which, double* out) {
     });
 }
 
+int dfsph_profile_enable(dfsph_ctx* ctx, uint32_t mask) {
+    if (!ctx) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] { ctx->solver->profile_enable(mask); });
+}
+
+int dfsph_profile_read(dfsph_ctx* ctx, int kernel_class, double* total_ms, uint64_t* launches) {
+    if (!ctx || !total_ms || !launches || kernel_class < 0 || kernel_class >= DFSPH_KERNEL_CLASSES)
+        return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        unsigned long long c = 0;
+        ctx->solver->profile_read(kernel_class, total_ms, &c);
+        *launches = c;
+    });
+}
+
 int dfsph_synchronize(dfsph_ctx* ctx) {
     if (!ctx) return DFSPH_ERR_INVALID_ARGUMENT;
     return guarded(ctx, [&] {

@@ -393,6 +393,27 @@ __global__ void __launch_bounds__(256) boundary_mask_kernel(u32 total, const u32
     mask[c] = static_cast<unsigned char>(any);
 }
 
+// 1 per boundary particle that has a fluid particle within the support.
+template <class R>
+__global__ void __launch_bounds__(128) active_boundary_kernel(int nb, const R4<R>* __restrict__ xb,
+                                                              const R4<R>* __restrict__ xk,
+                                                              const u32* __restrict__ cs, GridDev<R> g,
+                                                              Phys<R> p, u32* __restrict__ out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nb) return;
+    const R4<R> pi = ld(xb + s);
+    const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
+    u32 any = 0;
+    for_each_run(c, g, cs, [&](u32 b, u32 e) {
+        for (u32 j = b; j < e && !any; ++j) {
+            const R4<R> pj = ld(xk + j);
+            const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+            if (rx * rx + ry * ry + rz * rz < p.support2) any = 1;
+        }
+    });
+    if (any) atomicAdd(out, 1u);
+}
+
 // Boundary runs of a fluid particle are visited unless its stencil centre is an
 // in-grid cell whose mask says the stencil holds no boundary particle.
 template <class R>

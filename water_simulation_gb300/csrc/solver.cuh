@@ -101,6 +101,8 @@ public:
 
     ~Solver() override {
         if (host_ctl_) cudaFreeHost(host_ctl_);
+        for (const Record& r : records_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+        for (cudaEvent_t e : free_events_) cudaEventDestroy(e);
     }
 
     void set_stream(cudaStream_t s) override { stream_ = s; }
@@ -117,18 +119,18 @@ public:
         const float* src = upload(xyz, nullptr, n, mem);
         launch_import(n, src, nullptr, xb_[0].p, vr_scratch(), bid_[0].p);
         // sort by cell (the boundary CellGrid built once, dfsph.cu:93-97)
-        launch(count_kernel<R>, blocks_for(n, 256), 256, int(n), xb_[0].p, g_, bkey_.p, brank_.p, count_.p);
+        launch(DFSPH_KERNEL_GRID_COUNT, count_kernel<R>, blocks_for(n, 256), 256, int(n), xb_[0].p, g_, bkey_.p, brank_.p, count_.p);
         scan(bcs_.p, /*reset ctl*/ false);
-        launch(scatter_kernel, blocks_for(n, 256), 256, int(n), bkey_.p, brank_.p, bcs_.p, bid_[0].p,
+        launch(DFSPH_KERNEL_GRID_SCATTER, scatter_kernel, blocks_for(n, 256), 256, int(n), bkey_.p, brank_.p, bcs_.p, bid_[0].p,
                btmp_src_.p, btmp_id_.p);
-        launch(reorder_kernel<R>, blocks_for(n, 256), 256, int(n), btmp_src_.p, btmp_id_.p, bkey_.p, bcs_.p,
+        launch(DFSPH_KERNEL_GRID_REORDER, reorder_kernel<R>, blocks_for(n, 256), 256, int(n), btmp_src_.p, btmp_id_.p, bkey_.p, bcs_.p,
                geom_.total, kSentinelCap, xb_[0].p, vr_scratch(), xb_[1].p, vr_scratch2(), bid_[1].p,
                bkey_sorted_.p, ctl_.p);
         // Akinci mass into the w lane (dfsph_kernels.cu:40-65)
-        launch(boundary_mass_kernel<R>, blocks_for(n, 128), 128, int(n), xb_[1].p, xb_[0].p, bcs_.p, g_,
+        launch(DFSPH_KERNEL_OTHER, boundary_mass_kernel<R>, blocks_for(n, 128), 128, int(n), xb_[1].p, xb_[0].p, bcs_.p, g_,
                phys_);
         std::swap(bid_[0].p, bid_[1].p);  // bid_[0] holds the sorted order now
-        launch(boundary_mask_kernel<R>, blocks_for(geom_.total, 256), 256, geom_.total, bcs_.p, g_,
+        launch(DFSPH_KERNEL_OTHER, boundary_mask_kernel<R>, blocks_for(geom_.total, 256), 256, geom_.total, bcs_.p, g_,
                bmask_.p);
     }
 
@@ -161,7 +163,7 @@ public:
         counts_valid_ = false;
         have_state_ = true;
         step_once(R(dt), /*count_next=*/false);
-        launch(export_kernel<R>, blocks_for(n, 256), 256, int(n), id_[ci_].p, xk_[cx_].p, vr_[cv_].p,
+        launch(DFSPH_KERNEL_IO, export_kernel<R>, blocks_for(n, 256), 256, int(n), id_[ci_].p, xk_[cx_].p, vr_[cv_].p,
                alpha_.p, kap_.p, rho_adv_.p, pos, vel, density, alpha, kappa, density_adv);
     }
 
@@ -192,21 +194,21 @@ public:
         const int nb = blocks_for(std::max<size_t>(n, 1), 256);
         switch (field) {
             case DFSPH_FIELD_POSITION:
-                launch(unsort_vec_kernel<R, float>, nb, 256, int(n), id_[ci_].p, xk_[cx_].p, -1, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, nb, 256, int(n), id_[ci_].p, xk_[cx_].p, -1, (float*)out); break;
             case DFSPH_FIELD_VELOCITY:
-                launch(unsort_vec_kernel<R, float>, nb, 256, int(n), id_[ci_].p, vr_[cv_].p, -1, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, nb, 256, int(n), id_[ci_].p, vr_[cv_].p, -1, (float*)out); break;
             case DFSPH_FIELD_DENSITY:
-                launch(unsort_vec_kernel<R, float>, nb, 256, int(n), id_[ci_].p, vr_[cv_].p, 3, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, nb, 256, int(n), id_[ci_].p, vr_[cv_].p, 3, (float*)out); break;
             case DFSPH_FIELD_ALPHA:
-                launch(unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, alpha_.p, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, alpha_.p, (float*)out); break;
             case DFSPH_FIELD_KAPPA:
-                launch(unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, kap_.p, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, kap_.p, (float*)out); break;
             case DFSPH_FIELD_DENSITY_ADV:
-                launch(unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, rho_adv_.p, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, rho_adv_.p, (float*)out); break;
             case DFSPH_FIELD_KAPPA_V:
-                launch(unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, kap_v_.p, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, kap_v_.p, (float*)out); break;
             case DFSPH_FIELD_CELL_KEY:
-                launch(unsort_kernel<u32, u32>, nb, 256, int(n), id_[ci_].p, key_sorted_.p, (u32*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<u32, u32>, nb, 256, int(n), id_[ci_].p, key_sorted_.p, (u32*)out); break;
             case DFSPH_FIELD_SORTED_INDEX:
                 DFSPH_CUDA(cudaMemcpyAsync(out, id_[ci_].p, need, cudaMemcpyDeviceToDevice, stream_)); break;
             case DFSPH_FIELD_CELL_START:
@@ -214,11 +216,11 @@ public:
             case DFSPH_FIELD_BOUNDARY_CELL_START:
                 DFSPH_CUDA(cudaMemcpyAsync(out, bcs_.p, need, cudaMemcpyDeviceToDevice, stream_)); break;
             case DFSPH_FIELD_NBR_FLUID:
-                launch(unsort_kernel<u32, u32>, nb, 256, int(n), id_[ci_].p, nbr_f_.p, (u32*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<u32, u32>, nb, 256, int(n), id_[ci_].p, nbr_f_.p, (u32*)out); break;
             case DFSPH_FIELD_NBR_BOUNDARY:
-                launch(unsort_kernel<u32, u32>, nb, 256, int(n), id_[ci_].p, nbr_b_.p, (u32*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<u32, u32>, nb, 256, int(n), id_[ci_].p, nbr_b_.p, (u32*)out); break;
             case DFSPH_FIELD_BOUNDARY_MASS:
-                launch(unsort_vec_kernel<R, float>, blocks_for(nb_, 256), 256, int(nb_), bid_[0].p, xb_[0].p, 3,
+                launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, blocks_for(nb_, 256), 256, int(nb_), bid_[0].p, xb_[0].p, 3,
                        (float*)out);
                 break;
             case DFSPH_FIELD_BOUNDARY_SORTED_INDEX:
@@ -238,6 +240,7 @@ public:
             case DFSPH_SCALAR_FLUID_COUNT: return double(n_);
             case DFSPH_SCALAR_BOUNDARY_COUNT: return double(nb_);
             case DFSPH_SCALAR_KERNEL_LAUNCHES: return double(launches_);
+            case DFSPH_SCALAR_ACTIVE_BOUNDARY: return double(active_boundary());
             default: break;
         }
         read_ctl();
@@ -260,14 +263,58 @@ public:
 
     void synchronize() override { DFSPH_CUDA(cudaStreamSynchronize(stream_)); }
 
+    void profile_enable(u32 mask) override { profile_mask_ = mask; }
+
+    void profile_read(int kclass, double* total_ms, unsigned long long* count) override {
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        double t = 0.0;
+        unsigned long long c = 0;
+        std::vector<Record> keep;
+        for (const Record& r : records_) {
+            if (r.kclass != kclass) { keep.push_back(r); continue; }
+            float ms = 0.0f;
+            DFSPH_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+            t += ms;
+            ++c;
+            free_events_.push_back(r.a);
+            free_events_.push_back(r.b);
+        }
+        records_.swap(keep);
+        *total_ms = t;
+        *count = c;
+    }
+
 private:
     static constexpr u32 kSentinelCap = 4096;
 
-    template <class K, class... A> void launch(K kernel, int grid, int block, A... args) {
+    template <class K, class... A> void launch(int kclass, K kernel, int grid, int block, A... args) {
         if (grid <= 0) return;
+        const bool prof = (profile_mask_ >> kclass) & 1u;
+        cudaEvent_t a = nullptr, b = nullptr;
+        if (prof) {
+            a = take_event();
+            b = take_event();
+            DFSPH_CUDA(cudaEventRecord(a, stream_));
+        }
         kernel<<<grid, block, 0, stream_>>>(args...);
         DFSPH_LAUNCHED();
         ++launches_;
+        if (prof) {
+            DFSPH_CUDA(cudaEventRecord(b, stream_));
+            records_.push_back({kclass, a, b});
+        }
+    }
+
+    struct Record { int kclass; cudaEvent_t a, b; };
+    cudaEvent_t take_event() {
+        if (free_events_.empty()) {
+            cudaEvent_t e;
+            DFSPH_CUDA(cudaEventCreate(&e));
+            return e;
+        }
+        cudaEvent_t e = free_events_.back();
+        free_events_.pop_back();
+        return e;
     }
 
     // The integrator leaves the next step's per-cell counts in count_; any new
@@ -292,7 +339,7 @@ private:
     }
 
     void launch_import(u32 n, const float* pos, const float* vel, V4* xk, V4* vr, u32* id) {
-        launch(import_kernel<R>, blocks_for(n, 256), 256, int(n), pos, vel, xk, vr, id);
+        launch(DFSPH_KERNEL_IO, import_kernel<R>, blocks_for(n, 256), 256, int(n), pos, vel, xk, vr, id);
     }
 
     // Scratch 4-vectors for the boundary build: the fluid ping-pong buffers are
@@ -305,6 +352,21 @@ private:
         if (bscratch_[0].n < bcap_) { bscratch_[0].alloc(bcap_); bscratch_[1].alloc(bcap_); }
     }
 
+    // Boundary particles with at least one fluid particle within the kernel
+    // support, against the fluid grid of the last step (a diagnostic for the
+    // algorithmic byte count of the boundary terms).
+    u32 active_boundary() {
+        if (nb_ == 0 || n_ == 0 || !stepped_) return 0;
+        u32* d = static_cast<u32*>(scratch_bytes(sizeof(u32)));
+        DFSPH_CUDA(cudaMemsetAsync(d, 0, sizeof(u32), stream_));
+        launch(DFSPH_KERNEL_OTHER, active_boundary_kernel<R>, blocks_for(nb_, 128), 128, int(nb_), xb_[0].p,
+               xk_[cx_].p, cell_start_.p, g_, phys_, d);
+        u32 h = 0;
+        DFSPH_CUDA(cudaMemcpyAsync(&h, d, sizeof(u32), cudaMemcpyDeviceToHost, stream_));
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        return h;
+    }
+
     void* scratch_bytes(size_t bytes) {
         if (readback_.n < bytes) readback_.alloc(bytes);
         return readback_.p;
@@ -312,10 +374,10 @@ private:
 
     void scan(u32* cell_start, bool reset_ctl) {
         const u32 m = geom_.total + 1;
-        launch(scan_tile_sums, int(n_tiles_), SCAN_BLOCK, count_.p, m, tile_sums_.p);
-        launch(scan_tile_offsets, 1, 1024, tile_sums_.p, n_tiles_, reset_ctl ? ctl_.p : nullptr,
+        launch(DFSPH_KERNEL_GRID_SCAN, scan_tile_sums, int(n_tiles_), SCAN_BLOCK, count_.p, m, tile_sums_.p);
+        launch(DFSPH_KERNEL_GRID_SCAN, scan_tile_offsets, 1, 1024, tile_sums_.p, n_tiles_, reset_ctl ? ctl_.p : nullptr,
                reset_ctl ? 3 : 0);
-        launch(scan_tiles, int(n_tiles_), SCAN_BLOCK, count_.p, m, tile_sums_.p, cell_start);
+        launch(DFSPH_KERNEL_GRID_SCAN, scan_tiles, int(n_tiles_), SCAN_BLOCK, count_.p, m, tile_sums_.p, cell_start);
     }
 
     BoundaryDev bdev() const {
@@ -348,15 +410,15 @@ private:
         u32 launched = 0;
         for (u32 it = 0; it < max_iters; ++it) {
             if (adaptive)
-                launch(pressure_rate_kernel<R, DIV, true>, blocks_for(n, 128), 128, n, xk_[cx_].p,
+                launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true>, blocks_for(n, 128), 128, n, xk_[cx_].p,
                        xk_[cx_ ^ 1].p, vr_[cv_].p, alpha_.p, adv_out, kap_out, cell_start_.p, g_, phys_,
                        bdev(), dt, partials_.p, ctl, it, first_check, 1.0 / double(n), thr);
             else
-                launch(pressure_rate_kernel<R, DIV, false>, blocks_for(n, 128), 128, n, xk_[cx_].p,
+                launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, false>, blocks_for(n, 128), 128, n, xk_[cx_].p,
                        xk_[cx_ ^ 1].p, vr_[cv_].p, alpha_.p, adv_out, kap_out, cell_start_.p, g_, phys_,
                        bdev(), dt, partials_.p, ctl, it, first_check, 1.0 / double(n), thr);
             cx_ ^= 1;
-            launch(pressure_apply_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p, kap_out,
+            launch(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p, kap_out,
                    cell_start_.p, g_, phys_, bdev(), dt, ctl, it);
             launched = it + 1;
             if (adaptive && it >= first_check) {
@@ -379,11 +441,11 @@ private:
         stepped_ = true;
         // 1. grid build (CellGrid::build, core/src/cell_grid.cu:73-138)
         if (!counts_valid_)
-            launch(count_kernel<R>, blocks_for(n, 256), 256, n, xk_[cx_].p, g_, key_.p, rank_.p, count_.p);
+            launch(DFSPH_KERNEL_GRID_COUNT, count_kernel<R>, blocks_for(n, 256), 256, n, xk_[cx_].p, g_, key_.p, rank_.p, count_.p);
         scan(cell_start_.p, /*reset ctl*/ true);
-        launch(scatter_kernel, blocks_for(n, 256), 256, n, key_.p, rank_.p, cell_start_.p, id_[ci_].p,
+        launch(DFSPH_KERNEL_GRID_SCATTER, scatter_kernel, blocks_for(n, 256), 256, n, key_.p, rank_.p, cell_start_.p, id_[ci_].p,
                tmp_src_.p, tmp_id_.p);
-        launch(reorder_kernel<R>, blocks_for(n, 256), 256, n, tmp_src_.p, tmp_id_.p, key_.p, cell_start_.p,
+        launch(DFSPH_KERNEL_GRID_REORDER, reorder_kernel<R>, blocks_for(n, 256), 256, n, tmp_src_.p, tmp_id_.p, key_.p, cell_start_.p,
                geom_.total, kSentinelCap, xk_[cx_].p, vr_[cv_].p, xk_[cx_ ^ 1].p, vr_[cv_ ^ 1].p,
                id_[ci_ ^ 1].p, key_sorted_.p, ctl_.p);
         cx_ ^= 1; cv_ ^= 1; ci_ ^= 1;
@@ -393,17 +455,17 @@ private:
         const bool kahan = cfg_.precision == DFSPH_PRECISION_FP32_KAHAN;
         if (cfg_.record_diagnostics) {
             if (kahan)
-                launch(density_alpha_kernel<R, true, true>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
+                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, true>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
                        alpha_.p, cell_start_.p, g_, phys_, bd, nbr_f_.p, nbr_b_.p);
             else
-                launch(density_alpha_kernel<R, false, true>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
+                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, true>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
                        alpha_.p, cell_start_.p, g_, phys_, bd, nbr_f_.p, nbr_b_.p);
         } else {
             if (kahan)
-                launch(density_alpha_kernel<R, true, false>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
+                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, false>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
                        alpha_.p, cell_start_.p, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr);
             else
-                launch(density_alpha_kernel<R, false, false>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
+                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, false>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
                        alpha_.p, cell_start_.p, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr);
         }
         // 3. divergence solve (the reference's plan; 0 iterations = the reference)
@@ -413,7 +475,7 @@ private:
                 solve<true>(dt, cfg_.max_divergence_iters, cfg_.eta_divergence, ctl_.p + 1, kap_v_.p, rho_dot_.p);
         // 4. gravity + damping + XSPH (dfsph.cu:188-213)
         const R decay = std::exp(-R(cfg_.damping) * dt);
-        launch(forces_xsph_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p, vr_[cv_ ^ 1].p,
+        launch(DFSPH_KERNEL_FORCES_XSPH, forces_xsph_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p, vr_[cv_ ^ 1].p,
                cell_start_.p, g_, phys_, decay, R(cfg_.gravity[0]) * dt, R(cfg_.gravity[1]) * dt,
                R(cfg_.gravity[2]) * dt, R(cfg_.viscosity), cfg_.viscosity > 0.0f ? 1 : 0);
         cv_ ^= 1;
@@ -424,11 +486,11 @@ private:
         const R lo[3] = {R(cfg_.domain_min[0]), R(cfg_.domain_min[1]), R(cfg_.domain_min[2])};
         const R hi[3] = {R(cfg_.domain_max[0]), R(cfg_.domain_max[1]), R(cfg_.domain_max[2])};
         if (count_next) {
-            launch(advect_kernel<R, true>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p, dt, lo[0], lo[1],
+            launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, true>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p, dt, lo[0], lo[1],
                    lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p);
             counts_valid_ = true;
         } else {
-            launch(advect_kernel<R, false>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p, dt, lo[0], lo[1],
+            launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, false>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p, dt, lo[0], lo[1],
                    lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p);
         }
     }
@@ -445,6 +507,9 @@ private:
     bool counts_valid_ = false, have_state_ = false, stepped_ = false;
     u32 last_density_launched_ = 0, last_divergence_launched_ = 0;
     unsigned long long launches_ = 0;
+    u32 profile_mask_ = 0;
+    std::vector<Record> records_;
+    std::vector<cudaEvent_t> free_events_;
 
     DevBuf<V4> xk_[2], vr_[2], xb_[2], bscratch_[2];
     DevBuf<u32> id_[2], bid_[2];

@@ -27,6 +27,8 @@ struct SolverBase {
     virtual void get_field(int field, void* dst, std::size_t bytes, int mem) = 0;
     virtual double get_scalar(int which) = 0;
     virtual void synchronize() = 0;
+    virtual void profile_enable(std::uint32_t mask) = 0;
+    virtual void profile_read(int kclass, double* total_ms, unsigned long long* count) = 0;
 };
 
 std::unique_ptr<SolverBase> make_solver_fp32(const dfsph_config& cfg, int device, cudaStream_t s);

@@ -154,6 +154,19 @@ class Solver:
     def boundary_mass_at(self, i: int) -> float:
         return float(self.field(_lib.FIELD_BOUNDARY_MASS)[i])
 
+    def profile_enable(self, mask: int) -> None:
+        self._check(self._lib.dfsph_profile_enable(self._ctx, mask))
+
+    def profile_read(self, kernel_class: int):
+        """(total milliseconds, launches) recorded for one kernel class."""
+        t = ctypes.c_double()
+        c = ctypes.c_uint64()
+        self._check(self._lib.dfsph_profile_read(self._ctx, kernel_class, ctypes.byref(t), ctypes.byref(c)))
+        return t.value, c.value
+
+    def active_boundary(self) -> int:
+        return int(self.scalar(_lib.SCALAR_ACTIVE_BOUNDARY))
+
     def kernel_launches(self) -> int:
         return int(self.scalar(_lib.SCALAR_KERNEL_LAUNCHES))
 
