@@ -1,0 +1,68 @@
+"""The oracle pinned against golden vectors of the reference's own kernels.
+
+tests/golden/ref_*.npz were produced by tests/golden/make_golden.py on a GB300:
+the reference's DFSPH kernels (compiled from its sources with its
+-use_fast_math flags) driven step by step on seeded inputs with fixed density
+iterations. The oracle replays the same inputs on the CPU.
+
+Bit-exact per step: cell keys, sorted permutation, cell_start, density
+iteration count. Fields: the reference's fast-math division/sqrt (about 2 ulp)
+and summation order set the tolerances: density 2e-5 of rho0, alpha 1e-3
+relative (or 1e-6 of the largest alpha), positions 2e-6 m, velocities 5e-4 m/s (with XSPH, whose in-place
+update races in the reference, 2e-3 m/s).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "ref_*.npz")))
+
+
+def load_case(path):
+    d = np.load(path)
+    c = O.OracleConfig()
+    for name, _ in O.OracleConfig._fields_:
+        v = d["cfg_" + name]
+        if v.shape:
+            getattr(c, name)[:] = [float(x) if v.dtype.kind == "f" else int(x) for x in v]
+        else:
+            setattr(c, name, float(v) if v.dtype.kind == "f" else int(v))
+    return d, c
+
+
+def test_goldens_present():
+    names = {os.path.basename(p) for p in GOLDEN}
+    assert {"ref_block512_noxsph.npz", "ref_block512_xsph.npz", "ref_cloud2000.npz"} <= names
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_oracle_matches_reference_goldens(path):
+    d, c = load_case(path)
+    boundary = d["boundary"] if d["boundary"].shape[0] else None
+    o = O.Oracle(c, d["fluid"], d["velocity0"], boundary, precision=32)
+    assert o.particle_mass() == pytest.approx(float(d["particle_mass"]), rel=1e-7)
+    if boundary is not None:
+        assert np.array_equal(o.field(O.F_BOUNDARY_SORTED_INDEX), d["boundary_sorted_index"])
+        assert np.array_equal(o.field(O.F_BOUNDARY_CELL_START), d["boundary_cell_start"])
+        mb = d["boundary_mass"].astype(np.float64)
+        assert np.abs(o.field(O.F_BOUNDARY_MASS) - mb).max() / mb.max() < 1e-5
+    vtol = 2e-3 if float(d["cfg_viscosity"]) > 0 else 5e-4
+    for k in range(d["position"].shape[0]):
+        o.step(float(d["dt"]))
+        assert np.array_equal(o.field(O.F_CELL_KEY), d["cell_key"][k]), k
+        assert np.array_equal(o.field(O.F_SORTED_INDEX), d["sorted_index"][k]), k
+        assert np.array_equal(o.field(O.F_CELL_START), d["cell_start"][k]), k
+        assert o.last_density_iters() == int(d["density_iters"][k])
+        assert np.abs(o.field(O.F_DENSITY) - d["density"][k]).max() / 1000.0 < 2e-5, k
+        a, ar = o.field(O.F_ALPHA), d["alpha"][k].astype(np.float64)
+        # alpha = rho / |sum grad W|^2 amplifies rounding where the gradient sum
+        # nearly cancels (scattered particles): relative 1e-3 or 1e-6 of the max
+        assert (np.abs(a - ar) <= 1e-3 * np.abs(ar) + 1e-6 * np.abs(ar).max()).all(), k
+        assert np.abs(o.field(O.F_POSITION) - d["position"][k]).max() < 2e-6, k
+        assert np.abs(o.field(O.F_VELOCITY) - d["velocity"][k]).max() < vtol, k
+        assert o.max_velocity() == pytest.approx(float(d["max_velocity"][k]), rel=1e-4, abs=1e-7)

@@ -93,5 +93,30 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB_PATH
 
 
+APPS_DIR = os.path.join(PKG_DIR, "apps")
+BIN_DIR = os.path.join(PKG_DIR, "bin")
+SIM_CLI = os.path.join(BIN_DIR, "sim_cli")
+
+
+def build_sim_cli(force: bool = False) -> str:
+    """The sim_cli driver (host C++ over the C++ façade and libdfsph_gb300.so)."""
+    lib = build(force=force)
+    src = os.path.join(APPS_DIR, "sim_cli.cpp")
+    headers = []
+    for d, _, files in os.walk(os.path.join(ROOT, "include")):
+        headers += [os.path.join(d, f) for f in files if f.endswith(".h")]
+    if not force and not _stale(SIM_CLI, [src, lib] + headers):
+        return SIM_CLI
+    os.makedirs(BIN_DIR, exist_ok=True)
+    cuda = os.path.dirname(os.path.dirname(nvcc()))
+    tmp = SIM_CLI + ".tmp"
+    _run(["g++", "-std=c++17", "-O2", "-Wall", "-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
+          "-I", os.path.join(cuda, "include"), src, "-o", tmp, "-L", PKG_DIR, "-ldfsph_gb300",
+          "-L", os.path.join(cuda, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN/.."])
+    os.replace(tmp, SIM_CLI)
+    return SIM_CLI
+
+
 if __name__ == "__main__":
     build(force=True, verbose=True)
+    build_sim_cli(force=True)

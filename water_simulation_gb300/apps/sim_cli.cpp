@@ -1,0 +1,204 @@
+// sim_cli: the reference's offline simulation driver (apps/sim_cli/main.cpp)
+// on the GB300 library: scene JSON -> lattice block -> DFSPHSolver substeps
+// per frame (CFL TimeStepper) -> optional binary frame files.
+//
+//   sim_cli --scene PATH [--frames START:END] [--record] [--out DIR]
+//           [--no-vulkan] [--damping F] [--viscosity F]
+//
+// Frame file format (read by the reference's tools/*.py): little-endian u32 N
+// followed by N x 3 float32 positions. --no-vulkan is accepted for
+// compatibility; no graphics device is ever created.
+#include <cuda_runtime.h>
+#include <sys/stat.h>
+
+#include <algorithm>
+#include <cerrno>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "water/core/cuda_check.h"
+#include "water/core/particle_store.h"
+#include "water/core/timestep.h"
+#include "water/scene/scene.h"
+#include "water/solvers/boundary_sampler.h"
+#include "water/solvers/dfsph.h"
+
+namespace {
+
+struct Args {
+    std::string scene_path;
+    int frames_start = -1;
+    int frames_end = -1;
+    bool record = false;
+    std::string out_dir = "out";
+    float damping = -1.0f;
+    float viscosity = -1.0f;
+};
+
+[[noreturn]] void usage_exit(int code) {
+    std::puts("Usage: sim_cli --scene PATH [--frames START:END] [--record] "
+              "[--out DIR] [--no-vulkan] [--damping F] [--viscosity F]");
+    std::exit(code);
+}
+
+Args parse(int argc, char** argv) {
+    Args a;
+    for (int i = 1; i < argc; ++i) {
+        const std::string s = argv[i];
+        if (s == "--scene" && i + 1 < argc) {
+            a.scene_path = argv[++i];
+        } else if (s == "--frames" && i + 1 < argc) {
+            const std::string r = argv[++i];
+            const auto colon = r.find(':');
+            if (colon == std::string::npos) {
+                std::fprintf(stderr, "--frames expects START:END\n");
+                std::exit(2);
+            }
+            a.frames_start = std::stoi(r.substr(0, colon));
+            a.frames_end = std::stoi(r.substr(colon + 1));
+        } else if (s == "--record") {
+            a.record = true;
+        } else if (s == "--out" && i + 1 < argc) {
+            a.out_dir = argv[++i];
+        } else if (s == "--no-vulkan") {
+            // accepted: this build has no graphics path
+        } else if (s == "--damping" && i + 1 < argc) {
+            a.damping = std::stof(argv[++i]);
+        } else if (s == "--viscosity" && i + 1 < argc) {
+            a.viscosity = std::stof(argv[++i]);
+        } else if (s == "-h" || s == "--help") {
+            usage_exit(0);
+        } else {
+            std::fprintf(stderr, "Unknown arg: %s\n", s.c_str());
+            std::exit(2);
+        }
+    }
+    if (a.scene_path.empty()) {
+        std::fprintf(stderr, "Error: --scene required\n");
+        std::exit(2);
+    }
+    return a;
+}
+
+// Lattice of the initial block: float loops x outer, z inner, at spacing 2r
+// (apps/sim_cli/main.cpp:65-74).
+std::vector<water::Vec3f> initial_block(const water::scene::FluidCfg& f) {
+    std::vector<water::Vec3f> pts;
+    const float spacing = 2.0f * f.particle_radius;
+    for (float x = f.initial_block_min.x; x <= f.initial_block_max.x; x += spacing)
+        for (float y = f.initial_block_min.y; y <= f.initial_block_max.y; y += spacing)
+            for (float z = f.initial_block_min.z; z <= f.initial_block_max.z; z += spacing) pts.push_back({x, y, z});
+    return pts;
+}
+
+void write_frame(const std::string& path, const water::Vec3f* p, std::size_t n) {
+    std::ofstream out(path, std::ios::binary);
+    if (!out) throw std::runtime_error("cannot open " + path + " for writing");
+    const std::uint32_t count = static_cast<std::uint32_t>(n);
+    out.write(reinterpret_cast<const char*>(&count), sizeof(count));
+    out.write(reinterpret_cast<const char*>(p), static_cast<std::streamsize>(sizeof(water::Vec3f) * n));
+    if (!out) throw std::runtime_error("short write to " + path);
+}
+
+void make_dirs(const std::string& dir) {
+    std::string cur;
+    for (std::size_t i = 0; i <= dir.size(); ++i) {
+        if (i == dir.size() || dir[i] == '/') {
+            if (!cur.empty() && mkdir(cur.c_str(), 0755) != 0 && errno != EEXIST)
+                throw std::runtime_error("cannot create directory " + cur);
+        }
+        if (i < dir.size()) cur += dir[i];
+    }
+}
+
+}  // namespace
+
+int main(int argc, char** argv) try {
+    Args args = parse(argc, argv);
+    const water::scene::Scene scene = water::scene::load_scene(args.scene_path);
+    if (args.frames_start < 0) args.frames_start = scene.output.frame_start;
+    if (args.frames_end < 0) args.frames_end = scene.output.frame_end;
+
+    std::printf("=== water_sim sim_cli (GB300) ===\n");
+    std::printf("scene:        %s\n", scene.name.c_str());
+    std::printf("frames:       %d..%d (%d total)\n", args.frames_start, args.frames_end,
+                args.frames_end - args.frames_start);
+    std::printf("solver:       %s\n", scene.fluid.solver.c_str());
+    std::printf("record:       %s%s\n", args.record ? "yes -> " : "no", args.record ? args.out_dir.c_str() : "");
+
+    const std::vector<water::Vec3f> initial = initial_block(scene.fluid);
+    if (initial.empty()) {
+        std::fprintf(stderr, "no particles\n");
+        return 1;
+    }
+    std::printf("particles:    %zu\n", initial.size());
+
+    water::ParticleStore store(initial.size());
+    store.resize(initial.size());
+    WATER_CUDA_CHECK(cudaMemcpy(store.positions(), initial.data(), sizeof(water::Vec3f) * initial.size(),
+                                cudaMemcpyHostToDevice));
+
+    water::solvers::DFSPHSolver::Config cfg;
+    cfg.rest_density = scene.fluid.rest_density;
+    cfg.particle_radius = scene.fluid.particle_radius;
+    cfg.smoothing_length = 2.0f * scene.fluid.particle_radius;
+    cfg.viscosity = (args.viscosity > 0.0f) ? args.viscosity : std::max(scene.fluid.viscosity, 1e-2f);
+    cfg.surface_tension = scene.fluid.surface_tension;
+    cfg.gravity = scene.fluid.gravity;
+    cfg.domain_min = {0.0f, 0.0f, 0.0f};
+    cfg.domain_max = {1.0f, 1.0f, 1.0f};
+    if (args.damping >= 0.0f) cfg.damping = args.damping;
+    std::printf("solver cfg:   damping=%.3f viscosity=%.4f\n", cfg.damping, cfg.viscosity);
+
+    const float spacing = 2.0f * cfg.particle_radius;
+    const std::vector<water::Vec3f> bpts =
+        water::solvers::sample_aabb_boundary(cfg.domain_min, cfg.domain_max, spacing, 3);
+    std::printf("boundary:     %zu particles (Akinci 2012, 3 layers)\n", bpts.size());
+    auto boundary = std::make_unique<water::ParticleStore>(bpts.size());
+    boundary->resize(bpts.size());
+    WATER_CUDA_CHECK(cudaMemcpy(boundary->positions(), bpts.data(), sizeof(water::Vec3f) * bpts.size(),
+                                cudaMemcpyHostToDevice));
+
+    water::solvers::DFSPHSolver solver(store, boundary.get(), cfg);
+    water::TimeStepper ts;
+
+    if (args.record) {
+        make_dirs(args.out_dir);
+        char fname[512];
+        std::snprintf(fname, sizeof(fname), "%s/frame_%04d.bin", args.out_dir.c_str(), args.frames_start);
+        write_frame(fname, initial.data(), initial.size());
+    }
+
+    const float frame_dt = 1.0f / scene.output.fps;
+    std::vector<water::Vec3f> host(store.count());
+    for (int f = args.frames_start; f < args.frames_end; ++f) {
+        float remaining = frame_dt;
+        int sub = 0;
+        while (remaining > 1e-6f && sub < 64) {
+            const float dt = ts.next_dt(std::max(solver.max_velocity(), 0.5f), cfg.particle_radius, remaining);
+            solver.step(dt);
+            remaining -= dt;
+            ++sub;
+        }
+        WATER_CUDA_CHECK(cudaDeviceSynchronize());
+        std::printf("frame %4d: substeps=%2d, max_v=%.4f m/s\n", f + 1, sub, solver.max_velocity());
+        if (args.record) {
+            WATER_CUDA_CHECK(cudaMemcpy(host.data(), store.positions(), sizeof(water::Vec3f) * store.count(),
+                                        cudaMemcpyDeviceToHost));
+            char fname[512];
+            std::snprintf(fname, sizeof(fname), "%s/frame_%04d.bin", args.out_dir.c_str(), f + 1);
+            write_frame(fname, host.data(), host.size());
+        }
+    }
+    std::printf("=== sim_cli OK ===\n");
+    return 0;
+} catch (const std::exception& e) {
+    std::fprintf(stderr, "sim_cli error: %s\n", e.what());
+    return 1;
+}
