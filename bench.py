@@ -117,24 +117,33 @@ class ClockSampler:
         self._t = None
 
     def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True,
-                                     timeout=5).stdout.strip()
-                if out:
-                    self.samples.append([x.strip() for x in out.split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            return
+        for line in self._proc.stdout:
+            if line.strip():
+                self.samples.append([x.strip() for x in line.split(",")])
+            if self._stop.is_set():
+                break
 
     def __enter__(self):
+        self._proc = None
         self._t = threading.Thread(target=self._run, daemon=True)
         self._t.start()
+        time.sleep(0.3)  # let the sampler start before the timed region
         return self
 
     def __exit__(self, *exc):
         self._stop.set()
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
         self._t.join(timeout=10)
 
     def summary(self):
@@ -169,15 +178,6 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(v, world):
-    if world <= 1:
-        return v
-    import torch
-    import torch.distributed as dist
-
-    t = torch.tensor([v], dtype=torch.float64)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
 
 
 def bench_ours(args, rank, world):
@@ -225,7 +225,10 @@ def bench_ours(args, rank, world):
     ms = sum(a.elapsed_time(b) for a, b in ev)
     dom_ms, dom_launches = s.profile_read(dom_id)
     s.profile_enable(0)
-    res = {"ms_total": max_over_ranks(ms, world), "wall_s": wall, "launches": launches, "clocks": clk.summary(),
+    from water_simulation_gb300 import replicas
+
+    ms_max, work = replicas.aggregate(ms, float(sc.n) * args.steps, world)
+    res = {"ms_total": ms_max, "work": work, "wall_s": wall, "launches": launches, "clocks": clk.summary(),
            "dominant": dominant, "dominant_ms": dom_ms, "dominant_launches": dom_launches,
            "nb_active": nb_active,
            "warmup_share": {k: round(v[0] / max(sum(x[0] for x in share.values()), 1e-9), 4)
@@ -371,7 +374,7 @@ def main():
     traffic = NCU_TRAFFIC_PER_PARTICLE.get(dom)
     line = {
         "metric": "particle-steps/s @1M dam break",
-        "value": sc.n * args.steps * world / (res["ms_total"] * 1e-3),
+        "value": res["work"] / (res["ms_total"] * 1e-3),
         "unit": "particle-steps/s",
         "n_gpus": world,
         "steps": args.steps,

@@ -158,13 +158,14 @@ TEST_CASE("DFSPHSolver: single particle falls under gravity") {
     cfg.smoothing_length = 0.04f;
     cfg.viscosity = 0.0f;
     DFSPHSolver solver(store, nullptr, cfg);
-    for (int k = 0; k < 50; ++k) solver.step(0.01f);
+    for (int k = 0; k < 5; ++k) solver.step(0.01f);
+    CHECK(solver.max_velocity() > 0.0f);  // falling, not yet at the floor clamp
+    for (int k = 5; k < 50; ++k) solver.step(0.01f);
     WATER_CUDA_CHECK(cudaDeviceSynchronize());
     Vec3f pf{};
     WATER_CUDA_CHECK(cudaMemcpy(&pf, store.positions(), sizeof(Vec3f), cudaMemcpyDeviceToHost));
     CHECK(pf.y < 0.5f);
     CHECK(check::approx(pf.x, 0.5, 0.01) && check::approx(pf.z, 0.5, 0.01));
-    CHECK(solver.max_velocity() > 0.0f);
 }
 
 TEST_CASE("DFSPHSolver: boundary masses, grids and a short drop") {

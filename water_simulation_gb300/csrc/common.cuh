@@ -116,11 +116,12 @@ __device__ __forceinline__ void for_each_run(const Centre& c, const GridDev<R>& 
     const int z0 = max(c.z - 1, 0);
     const int z1 = min(c.z + 1, g.nz - 1);
     if (z0 > z1) return;
-#pragma unroll
+    // not unrolled: one copy of the pair loop keeps the instruction cache warm
+#pragma unroll 1
     for (int dx = -1; dx <= 1; ++dx) {
         const int nx = c.x + dx;
         if (nx < 0 || nx >= g.nx) continue;
-#pragma unroll
+#pragma unroll 1
         for (int dy = -1; dy <= 1; ++dy) {
             const int ny = c.y + dy;
             if (ny < 0 || ny >= g.ny) continue;

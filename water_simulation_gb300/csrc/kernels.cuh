@@ -24,22 +24,12 @@ template <class R> struct Phys {
     R grad_c;     // sigma / l
     R mass;       // fluid particle mass rho0 (2r)^3
     R rho0;
+    R two_l;      // 2l
+    R wA2, wA3;   // W = sigma + r^2 (wA2 + wA3 r) for r < l
+    R wB;         // W = wB (2l - r)^3 for l <= r < 2l
+    R gA, gB;     // F = gA r + gB for r < l
+    R gC;         // F = gC (2l - r)^2 / r for l <= r < 2l
 };
-
-// Monaghan cubic spline (core/include/water/core/sph_kernels.cuh:12-41) written
-// as W = sigma w(q) and gradW = (sigma / l) w'(q) / r * r_ij for q = r/l < 2.
-template <class R> __device__ __forceinline__ R spline_w(R q) {
-    const R t = R(2) - q;
-    const R outer = R(0.25) * t * t * t;
-    const R inner = R(1) + q * q * (R(0.75) * q - R(1.5));
-    return q < R(1) ? inner : outer;
-}
-template <class R> __device__ __forceinline__ R spline_dw(R q) {
-    const R t = R(2) - q;
-    const R outer = R(-0.75) * t * t;
-    const R inner = q * (R(2.25) * q - R(3));
-    return q < R(1) ? inner : outer;
-}
 
 __device__ __forceinline__ float rsqrt_r(float v) { return rsqrtf(v); }
 __device__ __forceinline__ double rsqrt_r(double v) { return rsqrt(v); }
@@ -49,6 +39,37 @@ template <> __device__ __forceinline__ R4<float> ld(const R4<float>* p) {
     const float4 v = __ldg(reinterpret_cast<const float4*>(p));
     return {v.x, v.y, v.z, v.w};
 }
+
+// ---------------------------------------------------------------------------
+// Pair terms. With r = |x_i - x_j| the cubic spline and its gradient factor
+// F(r) = (sigma/l) w'(r/l) / r (so that gradW = F(r) r_ij) are, per branch,
+//   r <  l :  W = sigma + r^2 (wA2 + wA3 r)      F = gA r + gB
+//   r >= l :  W = wB (2l - r)^3                  F = gC (2l - r)^2 / r
+// with (2l - r) clamped at 0, so both vanish beyond the support without a
+// branch. r comes from rsqrt(max(r2, 1e-24)): a particle paired with itself
+// (or a coincident one) has r_ij = 0, so every gradient term it adds is exactly
+// zero, which is how the reference's explicit self-skips and its r < 1e-12
+// guard (sph_kernels.cuh:29) come out here.
+// ---------------------------------------------------------------------------
+template <class R> __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
+
+template <class R> __device__ __forceinline__ R pair_r(R r2, R& rinv) {
+    rinv = rsqrt_r(rmax(r2, R(1e-24)));
+    return r2 * rinv;
+}
+template <class R> __device__ __forceinline__ R grad_factor(R r, R rinv, const Phys<R>& p) {
+    const R t = rmax(p.two_l - r, R(0));
+    const R outer = p.gC * t * t * rinv;
+    const R inner = p.gA * r + p.gB;
+    return r < p.l ? inner : outer;
+}
+template <class R> __device__ __forceinline__ R kernel_w(R r, const Phys<R>& p) {
+    const R t = rmax(p.two_l - r, R(0));
+    const R outer = p.wB * t * t * t;
+    const R inner = p.sigma + r * r * (p.wA3 * r + p.wA2);
+    return r < p.l ? inner : outer;
+}
+
 
 // ---------------------------------------------------------------------------
 // Reductions: FP64 block partial sums with a deterministic last-block finish.
@@ -198,19 +219,37 @@ static __global__ void __launch_bounds__(1024) scan_tile_offsets(u32* __restrict
     }
 }
 
+// Padded shared-memory index: one spare word per 32 keeps both the coalesced
+// (stride-1 across threads) and the per-thread (stride-16) accesses free of
+// bank conflicts.
+__device__ __forceinline__ u32 scan_pad(u32 i) { return i + (i >> 5); }
+
 static __global__ void __launch_bounds__(SCAN_BLOCK) scan_tiles(u32* __restrict__ count, u32 m,
                                                          const u32* __restrict__ tile_offsets,
                                                          u32* __restrict__ cell_start) {
     __shared__ u32 warp_tot[SCAN_BLOCK / 32];
+    __shared__ u32 tile[SCAN_TILE + SCAN_TILE / 32];
     const u32 base = blockIdx.x * SCAN_TILE;
-    // Each thread owns SCAN_ITEMS consecutive cells.
-    const u32 c0 = base + threadIdx.x * SCAN_ITEMS;
+    // coalesced load of the tile (and clear the counts for the next build)
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        const u32 li = k * SCAN_BLOCK + threadIdx.x;
+        const u32 c = base + li;
+        u32 x = 0;
+        if (c < m) {
+            x = count[c];
+            count[c] = 0u;
+        }
+        tile[scan_pad(li)] = x;
+    }
+    __syncthreads();
+    // each thread owns SCAN_ITEMS consecutive cells of the tile
+    const u32 l0 = threadIdx.x * SCAN_ITEMS;
     u32 v[SCAN_ITEMS];
     u32 t = 0;
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k) {
-        const u32 c = c0 + k;
-        v[k] = (c < m) ? count[c] : 0u;
+        v[k] = tile[scan_pad(l0 + k)];
         t += v[k];
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -225,14 +264,19 @@ static __global__ void __launch_bounds__(SCAN_BLOCK) scan_tiles(u32* __restrict_
     u32 wpre = 0;
     for (int w = 0; w < warp; ++w) wpre += warp_tot[w];
     u32 run = tile_offsets[blockIdx.x] + wpre + x - t;
+    // exclusive prefixes back into the tile (each thread its own words), then
+    // a coalesced store
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k) {
-        const u32 c = c0 + k;
-        if (c < m) {
-            cell_start[c] = run;
-            count[c] = 0u;
-        }
+        tile[scan_pad(l0 + k)] = run;
         run += v[k];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; ++k) {
+        const u32 li = k * SCAN_BLOCK + threadIdx.x;
+        const u32 c = base + li;
+        if (c < m) cell_start[c] = tile[scan_pad(li)];
     }
 }
 
@@ -369,13 +413,10 @@ __global__ void __launch_bounds__(128) boundary_mass_kernel(int nb, const R4<R>*
         for (u32 j = b; j < e; ++j) {
             const R4<R> pj = ld(xb_in + j);
             const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-            const R r2 = rx * rx + ry * ry + rz * rz;
-            if (r2 >= p.support2) continue;
-            const R r = r2 > R(0) ? r2 * rsqrt_r(r2) : R(0);
-            sum_w += spline_w(r * p.inv_l);
+            R rinv;
+            sum_w += kernel_w(pair_r(rx * rx + ry * ry + rz * rz, rinv), p);
         }
     });
-    sum_w *= p.sigma;
     xb_out[s] = {pi.x, pi.y, pi.z, p.rho0 / (sum_w > R(1e-9) ? sum_w : R(1e-9))};
 }
 
@@ -434,8 +475,9 @@ struct BoundaryDev {
 
 // ---------------------------------------------------------------------------
 // Density + alpha (density_kernel dfsph_kernels.cu:68-112 fused with
-// alpha_kernel :117-169). rho includes self (W(0)); the alpha sums skip self
-// (the gradient is zero at r = 0). KAHAN compensates the density sum.
+// alpha_kernel :117-169): rho = sum m W (self included) + sum m_b W;
+// alpha = rho / (|sum m gradW|^2 + sum |m gradW|^2). KAHAN compensates the
+// density sums.
 // ---------------------------------------------------------------------------
 template <class R, bool KAHAN, bool DIAG>
 __global__ void __launch_bounds__(128) density_alpha_kernel(
@@ -446,7 +488,7 @@ __global__ void __launch_bounds__(128) density_alpha_kernel(
     if (i >= n) return;
     const R4<R> pi = ld(xk + i);
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
-    R ws = 0, wc = 0;  // sum of W/sigma (+ compensation)
+    R ws = 0, wc = 0;
     R gx = 0, gy = 0, gz = 0, gq = 0;
     u32 cf = 0, cb = 0;
     for_each_run(c, g, cs, [&](u32 b, u32 e) {
@@ -454,11 +496,9 @@ __global__ void __launch_bounds__(128) density_alpha_kernel(
         for (u32 j = b; j < e; ++j) {
             const R4<R> pj = ld(xk + j);
             const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-            const R r2 = rx * rx + ry * ry + rz * rz;
-            if (r2 >= p.support2) continue;
-            const R rinv = r2 > R(0) ? rsqrt_r(r2) : R(0);
-            const R q = r2 * rinv * p.inv_l;
-            const R w = spline_w(q);
+            R rinv;
+            const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
+            const R w = kernel_w(r, p);
             if (KAHAN) {
                 const R y = w - wc;
                 const R t = ws + y;
@@ -467,18 +507,14 @@ __global__ void __launch_bounds__(128) density_alpha_kernel(
             } else {
                 ws += w;
             }
-            if (r2 >= R(1e-24)) {
-                const R f = spline_dw(q) * rinv;
-                gx += f * rx; gy += f * ry; gz += f * rz;
-                gq += f * f * r2;
-            }
+            const R f = grad_factor(r, rinv, p);
+            gx += f * rx; gy += f * ry; gz += f * rz;
+            gq += f * f * (rx * rx + ry * ry + rz * rz);
         }
     });
-    // fluid terms carry the uniform mass and sigma (and sigma/l for gradients)
-    R rho = p.mass * p.sigma * ws;
-    const R gm = p.mass * p.grad_c;
-    gx *= gm; gy *= gm; gz *= gm;
-    gq *= gm * gm;
+    R rho = p.mass * ws;
+    gx *= p.mass; gy *= p.mass; gz *= p.mass;
+    gq *= p.mass * p.mass;
     if (bd.has && boundary_near(c, g, bd.mask)) {
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
         R bs = 0, bsc = 0;
@@ -488,10 +524,9 @@ __global__ void __launch_bounds__(128) density_alpha_kernel(
                 const R4<R> pj = ld(xb + j);
                 const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
                 const R r2 = rx * rx + ry * ry + rz * rz;
-                if (r2 >= p.support2) continue;
-                const R rinv = r2 > R(0) ? rsqrt_r(r2) : R(0);
-                const R q = r2 * rinv * p.inv_l;
-                const R mw = pj.w * spline_w(q);
+                R rinv;
+                const R r = pair_r(r2, rinv);
+                const R mw = pj.w * kernel_w(r, p);
                 if (KAHAN) {
                     const R y = mw - bsc;
                     const R t = bs + y;
@@ -500,14 +535,14 @@ __global__ void __launch_bounds__(128) density_alpha_kernel(
                 } else {
                     bs += mw;
                 }
-                if (r2 >= R(1e-24)) {
-                    const R f = pj.w * p.grad_c * spline_dw(q) * rinv;
-                    gx += f * rx; gy += f * ry; gz += f * rz;
-                    gq += f * f * r2;
-                }
+                const R f = pj.w * grad_factor(r, rinv, p);
+                gx += f * rx; gy += f * ry; gz += f * rz;
+                gq += f * f * r2;
             }
         });
-        rho += p.sigma * bs;
+        rho += bs;
+    } else if (DIAG && bd.has) {
+        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) { cb += e - b; });
     }
     const R denom = gx * gx + gy * gy + gz * gz + gq;
     R4<R> v = vr[i];
@@ -537,22 +572,19 @@ __global__ void __launch_bounds__(128) forces_xsph_kernel(
         const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
         for_each_run(c, g, cs, [&](u32 b, u32 e) {
             for (u32 j = b; j < e; ++j) {
-                if (j == static_cast<u32>(i)) continue;
                 const R4<R> pj = ld(xk + j);
-                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-                const R r2 = rx * rx + ry * ry + rz * rz;
-                if (r2 >= p.support2) continue;
                 const R4<R> vj = ld(vr_in + j);
-                const R rinv = r2 > R(0) ? rsqrt_r(r2) : R(0);
-                const R w = spline_w(r2 * rinv * p.inv_l);
+                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+                R rinv;
+                const R w = kernel_w(pair_r(rx * rx + ry * ry + rz * rz, rinv), p);
                 const R ravg = R(0.5) * (vi.w + vj.w);
-                const R cc = w / (ravg > R(1e-9) ? ravg : R(1e-9));
+                const R cc = w / rmax(ravg, R(1e-9));
                 dx += cc * (vj.x - vi.x);
                 dy += cc * (vj.y - vi.y);
                 dz += cc * (vj.z - vi.z);
             }
         });
-        const R s = eps * p.mass * p.sigma * decay;
+        const R s = eps * p.mass * decay;
         dx *= s; dy *= s; dz *= s;
     }
     vr_out[i] = {vi.x * decay + gdx + dx, vi.y * decay + gdy + dy, vi.z * decay + gdz + dz, vi.w};
@@ -560,12 +592,12 @@ __global__ void __launch_bounds__(128) forces_xsph_kernel(
 
 // ---------------------------------------------------------------------------
 // Jacobi pressure iteration, first half: rho_dot = sum_j m (v_i - v_j).gradW
-// (fluid, self skipped) + sum_b m_b v_i.gradW (density_change_kernel
-// dfsph_kernels.cu:176-232). DIVERGENCE = false: rho* = rho + dt rho_dot,
-// kappa = max(0, rho* - rho0) alpha / dt^2, error term max(0, rho* - rho0).
-// DIVERGENCE = true (solver of the reference's plan): kappa_v =
-// max(0, rho_dot) alpha / dt, error term max(0, rho_dot).
-// Writes xk_out = (x, kappa / max(rho^2, 1e-9)); xk_in is not written.
+// (fluid) + sum_b m_b v_i.gradW (density_change_kernel dfsph_kernels.cu:176-232).
+// DIVERGENCE = false: rho* = rho + dt rho_dot, kappa = max(0, rho* - rho0)
+// alpha / dt^2, error term max(0, rho* - rho0). DIVERGENCE = true (solver of
+// the reference's plan): kappa_v = max(0, rho_dot) alpha / dt, error term
+// max(0, rho_dot). Writes xk_out = (x, kappa / max(rho^2, 1e-9)); xk_in is
+// not written.
 // ---------------------------------------------------------------------------
 template <class R, bool DIVERGENCE, bool REDUCE>
 __global__ void __launch_bounds__(128) pressure_rate_kernel(
@@ -585,18 +617,16 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
         R rd = 0;
         for_each_run(c, g, cs, [&](u32 b, u32 e) {
             for (u32 j = b; j < e; ++j) {
-                if (j == static_cast<u32>(i)) continue;
                 const R4<R> pj = ld(xk_in + j);
-                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-                const R r2 = rx * rx + ry * ry + rz * rz;
-                if (r2 >= p.support2 || r2 < R(1e-24)) continue;
                 const R4<R> vj = ld(vr + j);
-                const R rinv = rsqrt_r(r2);
-                const R f = spline_dw(r2 * rinv * p.inv_l) * rinv;
+                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+                R rinv;
+                const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
+                const R f = grad_factor(r, rinv, p);
                 rd += f * ((vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz);
             }
         });
-        rd *= p.mass * p.grad_c;
+        rd *= p.mass;
         if (bd.has && boundary_near(c, g, bd.mask)) {
             const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
             R rb = 0;
@@ -604,32 +634,29 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
                 for (u32 j = b; j < e; ++j) {
                     const R4<R> pj = ld(xb + j);
                     const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-                    const R r2 = rx * rx + ry * ry + rz * rz;
-                    if (r2 >= p.support2 || r2 < R(1e-24)) continue;
-                    const R rinv = rsqrt_r(r2);
-                    const R f = pj.w * spline_dw(r2 * rinv * p.inv_l) * rinv;
-                    rb += f * (vi.x * rx + vi.y * ry + vi.z * rz);
+                    R rinv;
+                    const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
+                    rb += pj.w * grad_factor(r, rinv, p) * (vi.x * rx + vi.y * ry + vi.z * rz);
                 }
             });
-            rd += rb * p.grad_c;
+            rd += rb;
         }
         const R rho = vi.w;
         R k;
         if (!DIVERGENCE) {
             const R rp = rho + dt * rd;
             rho_adv[i] = rp;
-            const R over = rp - p.rho0 > R(0) ? rp - p.rho0 : R(0);
+            const R over = rmax(rp - p.rho0, R(0));
             k = over * alpha[i] / (dt * dt);
             err = double(over);
         } else {
-            const R s = rd > R(0) ? rd : R(0);
+            const R s = rmax(rd, R(0));
             rho_adv[i] = rd;  // the divergence solver's rho_dot scratch
             k = s * alpha[i] / dt;
             err = double(s);
         }
         kap[i] = k;
-        const R rr = rho * rho;
-        xk_out[i] = {pi.x, pi.y, pi.z, k / (rr > R(1e-9) ? rr : R(1e-9))};
+        xk_out[i] = {pi.x, pi.y, pi.z, k / rmax(rho * rho, R(1e-9))};
     }
     if (REDUCE) {
         const double t = block_sum<128>(err, sh);
@@ -638,7 +665,7 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
 }
 
 // Second half (apply_kappa_kernel dfsph_kernels.cu:237-301):
-// v_i -= dt sum_j m (kfac_i + kfac_j) gradW over fluid (self skipped) and
+// v_i -= dt sum_j m (kfac_i + kfac_j) gradW over fluid and
 // dt sum_b m_b (kfac_i + kappa_i / max(rho0^2, 1e-9)) gradW over the boundary.
 template <class R>
 __global__ void __launch_bounds__(128) pressure_apply_kernel(
@@ -653,35 +680,31 @@ __global__ void __launch_bounds__(128) pressure_apply_kernel(
     R ax = 0, ay = 0, az = 0;
     for_each_run(c, g, cs, [&](u32 b, u32 e) {
         for (u32 j = b; j < e; ++j) {
-            if (j == static_cast<u32>(i)) continue;
             const R4<R> pj = ld(xk + j);
             const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-            const R r2 = rx * rx + ry * ry + rz * rz;
-            if (r2 >= p.support2 || r2 < R(1e-24)) continue;
-            const R rinv = rsqrt_r(r2);
-            const R f = (pi.w + pj.w) * spline_dw(r2 * rinv * p.inv_l) * rinv;
+            R rinv;
+            const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
+            const R f = (pi.w + pj.w) * grad_factor(r, rinv, p);
             ax += f * rx; ay += f * ry; az += f * rz;
         }
     });
-    const R sf = -dt * p.mass * p.grad_c;
+    const R sf = -dt * p.mass;
     ax *= sf; ay *= sf; az *= sf;
     if (bd.has && boundary_near(c, g, bd.mask)) {
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
-        const R r0 = p.rho0 * p.rho0;
-        const R kb = pi.w + kap[i] / (r0 > R(1e-9) ? r0 : R(1e-9));
+        const R kb = pi.w + kap[i] / rmax(p.rho0 * p.rho0, R(1e-9));
         R bx = 0, by = 0, bz = 0;
         for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
             for (u32 j = b; j < e; ++j) {
                 const R4<R> pj = ld(xb + j);
                 const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-                const R r2 = rx * rx + ry * ry + rz * rz;
-                if (r2 >= p.support2 || r2 < R(1e-24)) continue;
-                const R rinv = rsqrt_r(r2);
-                const R f = pj.w * spline_dw(r2 * rinv * p.inv_l) * rinv;
+                R rinv;
+                const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
+                const R f = pj.w * grad_factor(r, rinv, p);
                 bx += f * rx; by += f * ry; bz += f * rz;
             }
         });
-        const R sb = -dt * kb * p.grad_c;
+        const R sb = -dt * kb;
         ax += sb * bx; ay += sb * by; az += sb * bz;
     }
     R4<R> v = vr[i];

@@ -55,6 +55,19 @@ public:
         phys_.grad_c = phys_.sigma / l;
         phys_.mass = R(mass_f_);
         phys_.rho0 = R(cfg_.rest_density);
+        // the cubic spline per branch in terms of r (kernels.cuh, "Pair terms")
+        {
+            const double ld = double(cfg_.smoothing_length);
+            const double sg = 1.0 / (3.14159265358979323846 * ld * ld * ld);
+            phys_.two_l = R(2.0 * ld);
+            phys_.wA2 = R(-1.5 * sg / (ld * ld));
+            phys_.wA3 = R(0.75 * sg / (ld * ld * ld));
+            phys_.wB = R(0.25 * sg / (ld * ld * ld));
+            phys_.gA = R(2.25 * sg / (ld * ld * ld));
+            phys_.gB = R(-3.0 * sg / (ld * ld));
+            phys_.gC = R(-0.75 * sg / (ld * ld * ld));
+            phys_.sigma = R(sg);
+        }
 
         cap_ = cfg_.capacity;
         bcap_ = cfg_.boundary_capacity;
