@@ -198,6 +198,25 @@ int dfsph_build_cell_grid(const float* xyz_dev, uint32_t n, const float origin[3
                           void* stream);
 
 
+/* No counterpart in the reference. The same cell-grid build as
+ * dfsph_build_cell_grid for callers that cannot allocate device memory (a
+ * host callback or graph node that must not enter the allocator, a plugin
+ * whose host owns every allocation, a fixed memory budget): it uses a scratch
+ * area compiled into the library (DFSPH_STATIC_GRID_SCRATCH_BYTES of device
+ * memory that every GPU loading the library keeps until exit) and calls no
+ * allocator. Limits: n <= DFSPH_STATIC_GRID_MAX_PARTICLES and
+ * dims.x*dims.y*dims.z <= DFSPH_STATIC_GRID_MAX_CELLS, else
+ * DFSPH_ERR_OUT_OF_RANGE. All calls share the scratch: calls that overlap on
+ * the GPU race. The first call on a device looks the scratch address up (a
+ * runtime query); make it before any stream capture. */
+#define DFSPH_STATIC_GRID_MAX_PARTICLES 131072u
+#define DFSPH_STATIC_GRID_MAX_CELLS     1048576u
+#define DFSPH_STATIC_GRID_SCRATCH_BYTES (7u * 1024u * 1024u)
+int dfsph_build_cell_grid_static(const float* xyz_dev, uint32_t n, const float origin[3],
+                                 const int dims[3], float cell_length, uint32_t* sorted_keys_dev,
+                                 uint32_t* sorted_indices_dev, uint32_t* cell_start_dev,
+                                 void* stream);
+
 #ifdef __cplusplus
 }  /* extern "C" */
 #endif

@@ -31,6 +31,7 @@ CUDA_UNITS = [
     ("solver_fp64.cu", []),
     # the one unit built with the reference's fast math (see its header)
     ("stencil_recip.cu", ["-use_fast_math"]),
+    ("static_grid.cu", []),
 ]
 CXX_UNITS = ["geometry.cpp"]
 

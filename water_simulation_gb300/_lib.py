@@ -123,6 +123,8 @@ _SIGNATURES = [
      [ctypes.POINTER(DfsphConfig), _F, ctypes.POINTER(ctypes.c_int)]),
     ("dfsph_build_cell_grid", ctypes.c_int,
      [_P, ctypes.c_uint32, _F, ctypes.POINTER(ctypes.c_int), ctypes.c_float, _P, _P, _P, _P]),
+    ("dfsph_build_cell_grid_static", ctypes.c_int,
+     [_P, ctypes.c_uint32, _F, ctypes.POINTER(ctypes.c_int), ctypes.c_float, _P, _P, _P, _P]),
 ]
 
 _lib = None
