@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--no-ref-cuda", action="store_true", help="skip timing the reference CUDA kernels")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched comparison")
     return ap.parse_args()
 
 
@@ -276,6 +277,58 @@ def bench_e2e(s, sc, steps):
             "d2h_bytes_per_step": 2 * nbytes, "steps": steps}
 
 
+def bench_batch(steps, n_scenes=64, warmup=3):
+    """64 independent falling-block scenes (2,000-60,000 particles each): one
+    batched context replaying a captured CUDA graph of two steps, against 64
+    single-scene contexts stepped one after another with plain launches."""
+    import torch
+
+    from water_simulation_gb300 import scenes
+    from water_simulation_gb300.solver import Solver, solver_for
+
+    scs, eps = scenes.batched_blocks(n_scenes=n_scenes)
+    n_total = sum(s.n for s in scs)
+    stream = torch.cuda.current_stream()
+    cfg = scs[0].config(capacity=n_total)
+    cfg.n_scenes = n_scenes
+    cfg.use_cuda_graph = 1
+    b = Solver(cfg, stream=stream.cuda_stream)
+    b.set_boundary(scs[0].boundary)
+    b.set_fluid_batch([s.fluid for s in scs], [s.velocity for s in scs])
+    b.set_scene_viscosity(eps)
+    steps = steps + (steps % 2)  # whole graph replays
+    b.step(scs[0].dt, warmup + 1)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = b.kernel_launches()
+    e0.record(stream)
+    b.step(scs[0].dt, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_batch = e0.elapsed_time(e1)
+    launches_batch = b.kernel_launches() - l0
+    b.close()
+    singles = [solver_for(s, stream=stream.cuda_stream) for s in scs]
+    for s in singles:
+        s.step(scs[0].dt, warmup)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        for s in singles:
+            s.step(scs[0].dt)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_seq = e0.elapsed_time(e1)
+    for s in singles:
+        s.close()
+    return {"scenes": n_scenes, "particles": n_total, "steps": steps,
+            "batched_particle_steps_per_s": n_total * steps / (ms_batch * 1e-3),
+            "batched_scene_steps_per_s": n_scenes * steps / (ms_batch * 1e-3),
+            "sequential_particle_steps_per_s": n_total * steps / (ms_seq * 1e-3),
+            "speedup_vs_sequential": ms_seq / ms_batch, "batched_launches": launches_batch,
+            "batched_ms_per_step": ms_batch / steps, "sequential_ms_per_step": ms_seq / steps}
+
+
 def cpu_sample(sc, steps, threads=0):
     """The FP32 restatement of the reference step on the host cores."""
     from oracle import oracle as O
@@ -406,6 +459,11 @@ def main():
             line["cpu_baseline"] = cpu_sample(sc, 1 if sc.n > 500000 else 3)
         except Exception as e:  # the baseline is a report, not the product
             line["cpu_baseline"] = {"unavailable": str(e)[:200]}
+    if rank == 0 and not args.no_batch:
+        try:
+            line["batched"] = bench_batch(20)
+        except Exception as e:
+            line["batched"] = {"unavailable": str(e)[:200]}
     if rank == 0 and not args.no_ref_cuda:
         try:
             line["ref_cuda"] = bench_ref_cuda(sc, 3 if sc.n > 500000 else 10)

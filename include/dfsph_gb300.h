@@ -67,6 +67,10 @@ typedef struct dfsph_config {
     uint32_t capacity;              /* max fluid particles (ParticleStore capacity) */
     uint32_t boundary_capacity;     /* max boundary particles                 */
     uint32_t record_diagnostics;    /* 1 => keep per-step neighbour counts     */
+    uint32_t n_scenes;              /* independent scenes stepped together (0 or 1: one);
+                                       they share geometry, wall particles and dt */
+    uint32_t use_cuda_graph;        /* 1 => dfsph_step replays a captured CUDA graph of
+                                       two steps (only with eta = 0, no profiling) */
 } dfsph_config;
 
 typedef struct dfsph_ctx dfsph_ctx;
@@ -144,6 +148,19 @@ int dfsph_set_boundary(dfsph_ctx* ctx, const float* xyz, uint32_t n, int mem);
  * (ParticleStore::resize, core/src/particle_store.cu:11-17). */
 int dfsph_set_fluid(dfsph_ctx* ctx, const float* xyz, const float* vel, uint32_t n, int mem);
 
+/* Scene batching (no counterpart in the reference: it steps one scene per
+ * solver). For a context created with n_scenes = S > 1: counts[S] particles per
+ * scene, xyz/vel concatenated scene after scene (sum(counts) <= capacity).
+ * Every scene keeps its own cell keys (scene s owns keys [s(C+1), (s+1)(C+1))),
+ * so scenes never interact; one launch per kernel steps all of them.
+ * Fields read with dfsph_get_field come back concatenated the same way. */
+int dfsph_set_fluid_batch(dfsph_ctx* ctx, uint32_t n_scenes, const uint32_t* counts, const float* xyz,
+                          const float* vel, int mem);
+/* Per-scene XSPH coefficient (host array of n_scenes). */
+int dfsph_set_scene_viscosity(dfsph_ctx* ctx, const float* viscosity, uint32_t n_scenes);
+/* Per-scene max |v| after the last step (host array of n_scenes). */
+int dfsph_get_scene_max_velocity(dfsph_ctx* ctx, float* out, uint32_t n_scenes);
+
 /* DFSPHSolver::step(dt) (dfsph.cu:120-133), n_steps times, on the state held
  * by the context. Asynchronous unless a convergence check needs the host
  * (eta > 0); results stay on the device. */
@@ -197,6 +214,15 @@ int dfsph_build_cell_grid(const float* xyz_dev, uint32_t n, const float origin[3
                           uint32_t* sorted_indices_dev, uint32_t* cell_start_dev,
                           void* stream);
 
+
+/* SpatialAccel's Morton order (core/src/spatial_accel.cu:11-40,110-179): 30-bit
+ * Morton codes of positions normalised to [scene_min, scene_max] (10 bits per
+ * axis, x highest), stably sorted; writes the sorted codes and the permutation
+ * (device arrays, either may be NULL). The sort key variant kept for comparison
+ * with the cell-key order. Temporaries are stream-ordered on `stream`. */
+int dfsph_morton_sort(const float* xyz_dev, uint32_t n, const float scene_min[3],
+                      const float scene_max[3], uint32_t* sorted_codes_dev,
+                      uint32_t* sorted_indices_dev, void* stream);
 
 /* No counterpart in the reference. The same cell-grid build as
  * dfsph_build_cell_grid for callers that cannot allocate device memory (a

@@ -646,6 +646,41 @@ long long oracle_sample_aabb_boundary(const float lo[3], const float hi[3], floa
     return count;
 }
 
+// SpatialAccel's Morton order (core/src/spatial_accel.cu:11-40,110-179): each
+// coordinate normalised by the host reciprocal of the scene extent (0 for a
+// flat axis), clamped to [0, 1023] after * 1024 and truncated; 10 bits per axis
+// interleaved x, y, z (x highest); stable sort of (code, index).
+int oracle_morton_sort(const float* xyz, u32 n, const float smin[3], const float smax[3], u32* codes_out,
+                       u32* idx_out) {
+    float inv[3];
+    for (int a = 0; a < 3; ++a) {
+        const float ext = smax[a] - smin[a];
+        inv[a] = ext > 0.0f ? 1.0f / ext : 0.0f;
+    }
+    auto spread = [](u32 v) {
+        u32 o = 0;
+        for (int k = 0; k < 10; ++k) o |= ((v >> k) & 1u) << (3 * k);
+        return o;
+    };
+    std::vector<u32> code(n), idx(n);
+    for (u32 i = 0; i < n; ++i) {
+        u32 q[3];
+        for (int a = 0; a < 3; ++a) {
+            const float t = (xyz[3 * i + a] - smin[a]) * inv[a];
+            const float c = std::fmin(std::fmax(t * 1024.0f, 0.0f), 1023.0f);
+            q[a] = static_cast<u32>(c);
+        }
+        code[i] = (spread(q[0]) << 2) | (spread(q[1]) << 1) | spread(q[2]);
+        idx[i] = i;
+    }
+    std::stable_sort(idx.begin(), idx.end(), [&](u32 a, u32 b) { return code[a] < code[b]; });
+    for (u32 s = 0; s < n; ++s) {
+        codes_out[s] = code[idx[s]];
+        idx_out[s] = idx[s];
+    }
+    return 0;
+}
+
 // make_grid geometry (dfsph.cu:55-65).
 void oracle_grid_geometry(const Config* cfg, float origin[3], int dims[3]) {
     const oracle::Grid g = oracle::make_grid(*cfg);

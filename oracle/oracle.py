@@ -120,6 +120,19 @@ def build_grid(xyz, origin, dims, cell):
     return keys, srt, cs
 
 
+def morton_sort(xyz, smin, smax):
+    L = load()
+    L.oracle_morton_sort.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float),
+                                     ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_void_p]
+    xyz = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+    n = xyz.shape[0]
+    codes = np.empty(n, np.uint32)
+    idx = np.empty(n, np.uint32)
+    L.oracle_morton_sort(xyz.ctypes.data_as(ctypes.c_void_p), n, f3(smin), f3(smax),
+                         codes.ctypes.data_as(ctypes.c_void_p), idx.ctypes.data_as(ctypes.c_void_p))
+    return codes, idx
+
+
 def W(r, l, precision=32):
     L = load()
     return L.oracle_W_f64(r, l) if precision == 64 else L.oracle_W_f32(r, l)

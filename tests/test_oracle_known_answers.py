@@ -225,3 +225,26 @@ def test_divergence_solver_reduces_compression_rate():
     assert o1.scalar(5) >= 0.0
     # velocities were corrected (kappa_v > 0 somewhere)
     assert np.abs(o1.field(O.F_VELOCITY) - o0.field(O.F_VELOCITY)).max() > 0
+
+
+# tests/unit/test_spatial_accel.cu:9-55 (Morton order of SpatialAccel::build)
+def test_morton_order_permutation_and_known_codes():
+    pts = np.array([[0.1, 0.1, 0.1], [0.9, 0.1, 0.1], [0.1, 0.9, 0.1], [0.9, 0.9, 0.1],
+                    [0.1, 0.1, 0.9], [0.9, 0.1, 0.9], [0.1, 0.9, 0.9], [0.9, 0.9, 0.9]], np.float32)
+    codes, idx = O.morton_sort(pts, (0, 0, 0), (1, 1, 1))
+    assert sorted(idx.tolist()) == list(range(8))
+    assert np.all(np.diff(codes.astype(np.int64)) >= 0)
+    # x carries the highest bit of each triple: (0.9, 0.1, 0.1) sorts after (0.1, 0.9, 0.9)
+    assert idx.tolist() == [0, 4, 2, 6, 1, 5, 3, 7]
+    # the corner (1, 1, 1) clamps to 1023 per axis: all 30 bits set
+    c, _ = O.morton_sort(np.array([[1.0, 1.0, 1.0]], np.float32), (0, 0, 0), (1, 1, 1))
+    assert c[0] == (1 << 30) - 1
+    c, i = O.morton_sort(np.array([[0.5, 0.5, 0.5]], np.float32), (0, 0, 0), (1, 1, 1))
+    assert i.tolist() == [0]
+
+
+def test_morton_order_is_stable_for_equal_codes():
+    pts = np.tile(np.array([[0.3, 0.3, 0.3], [0.2, 0.2, 0.2]], np.float32), (50, 1))
+    codes, idx = O.morton_sort(pts, (0, 0, 0), (1, 1, 1))
+    assert idx[:50].tolist() == list(range(1, 100, 2))
+    assert idx[50:].tolist() == list(range(0, 100, 2))

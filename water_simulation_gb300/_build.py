@@ -32,6 +32,7 @@ CUDA_UNITS = [
     # the one unit built with the reference's fast math (see its header)
     ("stencil_recip.cu", ["-use_fast_math"]),
     ("static_grid.cu", []),
+    ("morton.cu", []),
 ]
 CXX_UNITS = ["geometry.cpp"]
 

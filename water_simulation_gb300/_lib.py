@@ -94,6 +94,8 @@ class DfsphConfig(ctypes.Structure):
         ("capacity", ctypes.c_uint32),
         ("boundary_capacity", ctypes.c_uint32),
         ("record_diagnostics", ctypes.c_uint32),
+        ("n_scenes", ctypes.c_uint32),
+        ("use_cuda_graph", ctypes.c_uint32),
     ]
 
 
@@ -107,6 +109,9 @@ _SIGNATURES = [
     ("dfsph_set_stream", ctypes.c_int, [_P, _P]),
     ("dfsph_set_boundary", ctypes.c_int, [_P, _P, ctypes.c_uint32, ctypes.c_int]),
     ("dfsph_set_fluid", ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, ctypes.c_int]),
+    ("dfsph_set_fluid_batch", ctypes.c_int, [_P, ctypes.c_uint32, _P, _P, _P, ctypes.c_int]),
+    ("dfsph_set_scene_viscosity", ctypes.c_int, [_P, _F, ctypes.c_uint32]),
+    ("dfsph_get_scene_max_velocity", ctypes.c_int, [_P, _F, ctypes.c_uint32]),
     ("dfsph_step", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_uint32]),
     ("dfsph_step_store", ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, ctypes.c_float, _P, _P, _P, _P]),
     ("dfsph_get_field", ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_int]),
@@ -123,6 +128,7 @@ _SIGNATURES = [
      [ctypes.POINTER(DfsphConfig), _F, ctypes.POINTER(ctypes.c_int)]),
     ("dfsph_build_cell_grid", ctypes.c_int,
      [_P, ctypes.c_uint32, _F, ctypes.POINTER(ctypes.c_int), ctypes.c_float, _P, _P, _P, _P]),
+    ("dfsph_morton_sort", ctypes.c_int, [_P, ctypes.c_uint32, _F, _F, _P, _P, _P]),
     ("dfsph_build_cell_grid_static", ctypes.c_int,
      [_P, ctypes.c_uint32, _F, ctypes.POINTER(ctypes.c_int), ctypes.c_float, _P, _P, _P, _P]),
 ]

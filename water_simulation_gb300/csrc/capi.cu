@@ -71,6 +71,8 @@ int dfsph_config_init(dfsph_config* c) {
     c->capacity = 0;
     c->boundary_capacity = 0;
     c->record_diagnostics = 0;
+    c->n_scenes = 1;
+    c->use_cuda_graph = 0;
     return DFSPH_OK;
 }
 
@@ -167,6 +169,35 @@ int dfsph_set_fluid(dfsph_ctx* ctx, const float* xyz, const float* vel, uint32_t
     });
 }
 
+int dfsph_set_fluid_batch(dfsph_ctx* ctx, uint32_t n_scenes, const uint32_t* counts, const float* xyz,
+                          const float* vel, int mem) {
+    if (!ctx || !counts || n_scenes == 0 || (mem != DFSPH_MEM_HOST && mem != DFSPH_MEM_DEVICE))
+        return DFSPH_ERR_INVALID_ARGUMENT;
+    unsigned long long total = 0;
+    for (uint32_t s = 0; s < n_scenes; ++s) total += counts[s];
+    if (total > 0 && !xyz) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        ctx->solver->set_fluid_batch(n_scenes, counts, xyz, vel, mem);
+    });
+}
+
+int dfsph_set_scene_viscosity(dfsph_ctx* ctx, const float* viscosity, uint32_t n_scenes) {
+    if (!ctx || !viscosity || n_scenes == 0) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        ctx->solver->set_scene_viscosity(viscosity, n_scenes);
+    });
+}
+
+int dfsph_get_scene_max_velocity(dfsph_ctx* ctx, float* out, uint32_t n_scenes) {
+    if (!ctx || !out || n_scenes == 0) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        ctx->solver->get_scene_max_velocity(out, n_scenes);
+    });
+}
+
 int dfsph_step(dfsph_ctx* ctx, float dt, uint32_t n_steps) {
     if (!ctx) return DFSPH_ERR_INVALID_ARGUMENT;
     if (!(dt > 0.0f) || dt > 1.0e30f) {
@@ -249,6 +280,15 @@ const char* dfsph_status_string(int s) {
         case DFSPH_ERR_NO_DEVICE: return "no CUDA device";
         default: return "unknown status";
     }
+}
+
+int dfsph_morton_sort(const float* xyz_dev, uint32_t n, const float scene_min[3], const float scene_max[3],
+                      uint32_t* sorted_codes_dev, uint32_t* sorted_indices_dev, void* stream) {
+    if ((n > 0 && !xyz_dev) || !scene_min || !scene_max) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(nullptr, [&] {
+        dfsph::morton_sort(xyz_dev, n, scene_min, scene_max, sorted_codes_dev, sorted_indices_dev,
+                           static_cast<cudaStream_t>(stream));
+    });
 }
 
 int dfsph_build_cell_grid(const float* xyz_dev, uint32_t n, const float origin[3], const int dims[3],

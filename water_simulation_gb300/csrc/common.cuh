@@ -56,6 +56,11 @@ template <class R> struct GridDev {
     u32 total;
     R inv_bin;
     R inv_stencil;
+    // Scenes stepped together share the geometry; scene s owns the keys
+    // [s * cells1, (s + 1) * cells1), cells1 = total + 1 (its out-of-grid key
+    // last). slot_scene[s] is the scene of sorted slot s (null: one scene).
+    u32 cells1;
+    const unsigned short* slot_scene;
 };
 
 template <class R> inline GridDev<R> to_dev(const GridGeom& g) {
@@ -63,6 +68,8 @@ template <class R> inline GridDev<R> to_dev(const GridGeom& g) {
     d.ox = R(g.origin[0]); d.oy = R(g.origin[1]); d.oz = R(g.origin[2]);
     d.nx = g.dims[0]; d.ny = g.dims[1]; d.nz = g.dims[2];
     d.total = g.total;
+    d.cells1 = g.total + 1;
+    d.slot_scene = nullptr;
     if (sizeof(R) == sizeof(float)) {
         d.inv_bin = R(g.inv_bin);
         d.inv_stencil = R(g.inv_stencil);
@@ -79,6 +86,10 @@ template <class R> inline GridDev<R> to_dev(const GridGeom& g) {
 __device__ __forceinline__ int floor_to_int(float v) { return static_cast<int>(floorf(v)); }
 __device__ __forceinline__ int floor_to_int(double v) {
     return static_cast<int>(floor(v));
+}
+
+template <class R> __device__ __forceinline__ u32 scene_of(const GridDev<R>& g, int slot) {
+    return g.slot_scene ? static_cast<u32>(g.slot_scene[slot]) : 0u;
 }
 
 // hash_cell (core/src/cell_grid.cu:10-22): x-major id, out of grid -> total.

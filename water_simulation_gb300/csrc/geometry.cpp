@@ -10,6 +10,9 @@
 namespace dfsph {
 
 [[noreturn]] void throw_cuda(cudaError_t e, const char* expr, const char* file, int line) {
+    // reset the runtime's last-error slot, so that a recoverable error does not
+    // resurface at the next launch check
+    cudaGetLastError();
     std::string m = "CUDA error at ";
     m += file; m += ":"; m += std::to_string(line);
     m += " (";  m += expr; m += "): ";

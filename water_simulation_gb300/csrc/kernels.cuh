@@ -53,6 +53,11 @@ template <> __device__ __forceinline__ R4<float> ld(const R4<float>* p) {
 // ---------------------------------------------------------------------------
 template <class R> __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
 
+// a / b for b in [1e-9, 1e30]: the fast single-precision divide (2 ulp) where
+// the working type is float, the IEEE divide where it is double.
+__device__ __forceinline__ float fast_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double fast_div(double a, double b) { return a / b; }
+
 template <class R> __device__ __forceinline__ R pair_r(R r2, R& rinv) {
     rinv = rsqrt_r(rmax(r2, R(1e-24)));
     return r2 * rinv;
@@ -136,7 +141,7 @@ __global__ void __launch_bounds__(256) count_kernel(int n, const R4<R>* __restri
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const R4<R> p = ld(xk + s);
-    const u32 k = cell_key(p.x, p.y, p.z, g);
+    const u32 k = cell_key(p.x, p.y, p.z, g) + scene_of(g, s) * g.cells1;
     key[s] = k;
     rank[s] = atomicAdd(count + k, 1u);
 }
@@ -170,11 +175,13 @@ static __global__ void __launch_bounds__(SCAN_BLOCK) scan_tile_sums(const u32* _
 }
 
 // One block: exclusive scan of n_tiles values in place; writes the total to
-// tile_sums[n_tiles].
-// It also resets the solver's iteration controls for the step when given
-// (every step's grid build runs it exactly once, before any solver kernel).
+// tile_sums[n_tiles] and, when given, to *total_out (the closing entry of
+// cell_start). It also resets the solver's iteration controls and per-scene
+// maxima for the step when given (every step's grid build runs it exactly
+// once, before any solver kernel).
 static __global__ void __launch_bounds__(1024) scan_tile_offsets(u32* __restrict__ tile_sums, u32 n_tiles,
-                                                          IterCtl* ctl, int n_ctl) {
+                                                          u32* __restrict__ total_out, IterCtl* ctl, int n_ctl,
+                                                          u32* __restrict__ maxv_scene, int n_scenes) {
     __shared__ u32 warp_tot[32];
     __shared__ u32 carry;
     if (threadIdx.x == 0) carry = 0;
@@ -207,8 +214,10 @@ static __global__ void __launch_bounds__(1024) scan_tile_offsets(u32* __restrict
         if (threadIdx.x == blockDim.x - 1) carry = before + x;
         __syncthreads();
     }
+    for (int s = threadIdx.x; s < n_scenes; s += blockDim.x) maxv_scene[s] = 0u;
     if (threadIdx.x == 0) {
         tile_sums[n_tiles] = carry;
+        if (total_out) *total_out = carry;
         for (int k = 0; k < n_ctl; ++k) {
             ctl[k].err_sum = 0.0;
             ctl[k].stop_iter = ~0u;
@@ -296,12 +305,14 @@ static __global__ void __launch_bounds__(256) scatter_kernel(int n, const u32* _
 // Final slot = cell start + number of cell mates with a smaller original index,
 // which reproduces the reference's stable (key, index) order
 // (core/src/cell_grid.cu:98-110 sorts iota values stably). The state is
-// gathered into the new order on the way. Out-of-grid particles (key == total)
-// beyond `sentinel_cap` keep the provisional order and raise flag bit 1.
+// gathered into the new order on the way. cell_start has one closing entry
+// (= n) after the last key. Out-of-grid particles of a scene (its last key,
+// cells1 - 1 modulo cells1) beyond `sentinel_cap` keep the provisional order
+// and raise flag bit 1.
 template <class R>
 __global__ void __launch_bounds__(256) reorder_kernel(
     int n, const u32* __restrict__ tmp_src, const u32* __restrict__ tmp_id,
-    const u32* __restrict__ key_old, const u32* __restrict__ cell_start, u32 total,
+    const u32* __restrict__ key_old, const u32* __restrict__ cell_start, u32 cells1,
     u32 sentinel_cap, const R4<R>* __restrict__ xk_old, const R4<R>* __restrict__ vr_old,
     R4<R>* __restrict__ xk_new, R4<R>* __restrict__ vr_new, u32* __restrict__ id_new,
     u32* __restrict__ key_sorted, IterCtl* ctl) {
@@ -311,10 +322,10 @@ __global__ void __launch_bounds__(256) reorder_kernel(
     const u32 my = tmp_id[t];
     const u32 c = key_old[src];
     const u32 b = cell_start[c];
-    const u32 e = (c == total) ? static_cast<u32>(n) : cell_start[c + 1];
+    const u32 e = cell_start[c + 1];
     u32 dst = static_cast<u32>(t);
     if (e - b > 1) {
-        if (c == total && e - b > sentinel_cap) {
+        if ((c % cells1) == cells1 - 1 && e - b > sentinel_cap) {
             if (t == static_cast<int>(b)) atomicOr(&ctl->flags, 2u);
         } else {
             u32 r = 0;
@@ -439,19 +450,20 @@ template <class R>
 __global__ void __launch_bounds__(128) active_boundary_kernel(int nb, const R4<R>* __restrict__ xb,
                                                               const R4<R>* __restrict__ xk,
                                                               const u32* __restrict__ cs, GridDev<R> g,
-                                                              Phys<R> p, u32* __restrict__ out) {
+                                                              Phys<R> p, int n_scenes, u32* __restrict__ out) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nb) return;
     const R4<R> pi = ld(xb + s);
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
     u32 any = 0;
-    for_each_run(c, g, cs, [&](u32 b, u32 e) {
-        for (u32 j = b; j < e && !any; ++j) {
-            const R4<R> pj = ld(xk + j);
-            const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-            if (rx * rx + ry * ry + rz * rz < p.support2) any = 1;
-        }
-    });
+    for (int sc = 0; sc < n_scenes && !any; ++sc)
+        for_each_run(c, g, cs + size_t(sc) * g.cells1, [&](u32 b, u32 e) {
+            for (u32 j = b; j < e && !any; ++j) {
+                const R4<R> pj = ld(xk + j);
+                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+                if (rx * rx + ry * ry + rz * rz < p.support2) any = 1;
+            }
+        });
     if (any) atomicAdd(out, 1u);
 }
 
@@ -491,7 +503,7 @@ __global__ void __launch_bounds__(128) density_alpha_kernel(
     R ws = 0, wc = 0;
     R gx = 0, gy = 0, gz = 0, gq = 0;
     u32 cf = 0, cb = 0;
-    for_each_run(c, g, cs, [&](u32 b, u32 e) {
+    for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
         if (DIAG) cf += e - b;
         for (u32 j = b; j < e; ++j) {
             const R4<R> pj = ld(xk + j);
@@ -562,7 +574,7 @@ template <class R>
 __global__ void __launch_bounds__(128) forces_xsph_kernel(
     int n, const R4<R>* __restrict__ xk, const R4<R>* __restrict__ vr_in, R4<R>* __restrict__ vr_out,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, R decay, R gdx, R gdy, R gdz, R eps,
-    int do_xsph) {
+    const R* __restrict__ eps_scene, int do_xsph) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R4<R> vi = ld(vr_in + i);
@@ -570,7 +582,7 @@ __global__ void __launch_bounds__(128) forces_xsph_kernel(
     if (do_xsph) {
         const R4<R> pi = ld(xk + i);
         const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
-        for_each_run(c, g, cs, [&](u32 b, u32 e) {
+        for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
             for (u32 j = b; j < e; ++j) {
                 const R4<R> pj = ld(xk + j);
                 const R4<R> vj = ld(vr_in + j);
@@ -578,13 +590,14 @@ __global__ void __launch_bounds__(128) forces_xsph_kernel(
                 R rinv;
                 const R w = kernel_w(pair_r(rx * rx + ry * ry + rz * rz, rinv), p);
                 const R ravg = R(0.5) * (vi.w + vj.w);
-                const R cc = w / rmax(ravg, R(1e-9));
+                const R cc = fast_div(w, rmax(ravg, R(1e-9)));
                 dx += cc * (vj.x - vi.x);
                 dy += cc * (vj.y - vi.y);
                 dz += cc * (vj.z - vi.z);
             }
         });
-        const R s = eps * p.mass * decay;
+        const R e = eps_scene ? eps_scene[scene_of(g, i)] : eps;
+        const R s = e * p.mass * decay;
         dx *= s; dy *= s; dz *= s;
     }
     vr_out[i] = {vi.x * decay + gdx + dx, vi.y * decay + gdy + dy, vi.z * decay + gdz + dz, vi.w};
@@ -615,7 +628,7 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
         const R4<R> vi = ld(vr + i);
         const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
         R rd = 0;
-        for_each_run(c, g, cs, [&](u32 b, u32 e) {
+        for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
             for (u32 j = b; j < e; ++j) {
                 const R4<R> pj = ld(xk_in + j);
                 const R4<R> vj = ld(vr + j);
@@ -678,7 +691,7 @@ __global__ void __launch_bounds__(128) pressure_apply_kernel(
     const R4<R> pi = ld(xk + i);
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
     R ax = 0, ay = 0, az = 0;
-    for_each_run(c, g, cs, [&](u32 b, u32 e) {
+    for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
         for (u32 j = b; j < e; ++j) {
             const R4<R> pj = ld(xk + j);
             const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
@@ -721,9 +734,10 @@ template <class R, bool COUNT>
 __global__ void __launch_bounds__(256) advect_kernel(
     int n, R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, R dt, R lox, R loy, R loz, R hix,
     R hiy, R hiz, GridDev<R> g, u32* __restrict__ key, u32* __restrict__ rank,
-    u32* __restrict__ count, IterCtl* ctl) {
+    u32* __restrict__ count, IterCtl* ctl, u32* __restrict__ maxv_scene) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     u32 vbits = 0;
+    u32 scene = 0xffffffffu;  // lanes past the end form their own group
     if (i < n) {
         R4<R> v = vr[i];
         R4<R> x = xk[i];
@@ -745,11 +759,19 @@ __global__ void __launch_bounds__(256) advect_kernel(
         xk[i] = {px, py, pz, R(0)};
         const float mag = float(sqrt(v.x * v.x + v.y * v.y + v.z * v.z));
         vbits = __float_as_uint(mag);
+        scene = scene_of(g, i);
         if (COUNT) {
-            const u32 k = cell_key(px, py, pz, g);
+            const u32 k = cell_key(px, py, pz, g) + scene * g.cells1;
             key[i] = k;
             rank[i] = atomicAdd(count + k, 1u);
         }
+    }
+    if (maxv_scene) {
+        // per-scene maxima: lanes of one scene (contiguous slots) reduce
+        // together and their lowest lane does the one atomic
+        const u32 peers = __match_any_sync(0xffffffffu, scene);
+        const u32 m = __reduce_max_sync(peers, vbits);
+        if (i < n && (threadIdx.x & 31) == __ffs(peers) - 1 && m) atomicMax(maxv_scene + scene, m);
     }
     // max over the warp, then one atomic per warp (NaN bits dominate)
 #pragma unroll

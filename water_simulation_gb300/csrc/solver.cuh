@@ -2,6 +2,11 @@
 // real type). The stage order is DFSPHSolver::step (solvers/dfsph/src/dfsph.cu
 // :120-133): grid build, density + alpha, [divergence solve], external forces +
 // XSPH, density solve, advect + max |v|.
+//
+// Scenes: a context steps S >= 1 independent scenes that share the grid
+// geometry, the wall particles and dt. Scene s owns the cell keys
+// [s (C+1), (s+1)(C+1)) (its out-of-grid key last), so one counting sort orders
+// all of them, scene after scene, and one launch per kernel steps all of them.
 #pragma once
 
 #include <cmath>
@@ -43,6 +48,12 @@ public:
         geom_ = make_grid_geom(cfg_.domain_min, cfg_.domain_max, cfg_.smoothing_length);
         geom_.inv_stencil = device_stencil_reciprocal(cfg_.smoothing_length, stream_);
         g_ = to_dev<R>(geom_);
+        gb_ = g_;  // the wall grid: one "scene"
+        scenes_ = cfg_.n_scenes > 1 ? cfg_.n_scenes : 1u;
+        if (scenes_ > 65535u) throw Error(DFSPH_ERR_INVALID_ARGUMENT, "at most 65535 scenes");
+        cells1_ = geom_.total + 1;
+        if (double(scenes_) * double(cells1_) >= 4294967295.0)
+            throw Error(DFSPH_ERR_INVALID_ARGUMENT, "scenes x cells must stay below 2^32");
         // particle mass rho0 * (2r)^3 evaluated in float (dfsph.cu:76-78)
         const float spacing = 2.0f * cfg_.particle_radius;
         const float v0 = spacing * spacing * spacing;
@@ -51,14 +62,14 @@ public:
         phys_.l = l;
         phys_.inv_l = R(1) / l;
         phys_.support2 = R(4) * l * l;
-        phys_.sigma = R(1) / (R(3.14159265358979323846) * l * l * l);
-        phys_.grad_c = phys_.sigma / l;
+        phys_.grad_c = R(1) / (R(3.14159265358979323846) * l * l * l) / l;
         phys_.mass = R(mass_f_);
         phys_.rho0 = R(cfg_.rest_density);
         // the cubic spline per branch in terms of r (kernels.cuh, "Pair terms")
         {
             const double ld = double(cfg_.smoothing_length);
             const double sg = 1.0 / (3.14159265358979323846 * ld * ld * ld);
+            phys_.sigma = R(sg);
             phys_.two_l = R(2.0 * ld);
             phys_.wA2 = R(-1.5 * sg / (ld * ld));
             phys_.wA3 = R(0.75 * sg / (ld * ld * ld));
@@ -66,12 +77,11 @@ public:
             phys_.gA = R(2.25 * sg / (ld * ld * ld));
             phys_.gB = R(-3.0 * sg / (ld * ld));
             phys_.gC = R(-0.75 * sg / (ld * ld * ld));
-            phys_.sigma = R(sg);
         }
 
         cap_ = cfg_.capacity;
         bcap_ = cfg_.boundary_capacity;
-        const size_t cells = size_t(geom_.total) + 1;
+        keys_ = size_t(scenes_) * cells1_;  // fluid keys of all scenes
         for (int k = 0; k < 2; ++k) {
             xk_[k].alloc(cap_);
             vr_[k].alloc(cap_);
@@ -82,9 +92,9 @@ public:
         key_.alloc(cap_); rank_.alloc(cap_); tmp_src_.alloc(cap_); tmp_id_.alloc(cap_);
         key_sorted_.alloc(cap_);
         if (cfg_.record_diagnostics) { nbr_f_.alloc(cap_); nbr_b_.alloc(cap_); }
-        count_.alloc(cells);
-        cell_start_.alloc(cells);
-        n_tiles_ = static_cast<u32>((cells + SCAN_TILE - 1) / SCAN_TILE);
+        count_.alloc(keys_);
+        cell_start_.alloc(keys_ + 1);  // closing entry = n
+        n_tiles_ = static_cast<u32>((keys_ + SCAN_TILE - 1) / SCAN_TILE);
         tile_sums_.alloc(n_tiles_ + 1);
         partials_.alloc(std::max<size_t>(1, (std::max(cap_, 1u) + 127) / 128));
         ctl_.alloc(3);
@@ -94,11 +104,21 @@ public:
             bkey_.alloc(bcap_); brank_.alloc(bcap_); bkey_sorted_.alloc(bcap_);
             btmp_src_.alloc(bcap_); btmp_id_.alloc(bcap_);
         }
-        bcs_.alloc(cells);
+        bcs_.alloc(size_t(cells1_) + 1);
         bmask_.alloc(std::max<size_t>(geom_.total, 1));
-        DFSPH_CUDA(cudaMemsetAsync(count_.p, 0, cells * sizeof(u32), stream_));
-        DFSPH_CUDA(cudaMemsetAsync(cell_start_.p, 0, cells * sizeof(u32), stream_));
-        DFSPH_CUDA(cudaMemsetAsync(bcs_.p, 0, cells * sizeof(u32), stream_));
+        if (scenes_ > 1) {
+            slot_scene_.alloc(std::max(cap_, 1u));
+            eps_scene_.alloc(scenes_);
+            maxv_scene_.alloc(scenes_);
+            g_.slot_scene = slot_scene_.p;
+            std::vector<R> eps(scenes_, R(cfg_.viscosity));
+            DFSPH_CUDA(cudaMemcpyAsync(eps_scene_.p, eps.data(), scenes_ * sizeof(R), cudaMemcpyHostToDevice, stream_));
+            DFSPH_CUDA(cudaMemsetAsync(maxv_scene_.p, 0, scenes_ * sizeof(u32), stream_));
+            DFSPH_CUDA(cudaMemsetAsync(slot_scene_.p, 0, std::max(cap_, 1u) * sizeof(unsigned short), stream_));
+        }
+        DFSPH_CUDA(cudaMemsetAsync(count_.p, 0, keys_ * sizeof(u32), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(cell_start_.p, 0, (keys_ + 1) * sizeof(u32), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(bcs_.p, 0, (size_t(cells1_) + 1) * sizeof(u32), stream_));
         DFSPH_CUDA(cudaMemsetAsync(ctl_.p, 0, 3 * sizeof(IterCtl), stream_));
         DFSPH_CUDA(cudaMemsetAsync(alpha_.p, 0, size_t(cap_) * sizeof(R), stream_));
         DFSPH_CUDA(cudaMemsetAsync(rho_adv_.p, 0, size_t(cap_) * sizeof(R), stream_));
@@ -113,91 +133,166 @@ public:
     }
 
     ~Solver() override {
+        drop_graph();
+        if (capture_stream_) cudaStreamDestroy(capture_stream_);
         if (host_ctl_) cudaFreeHost(host_ctl_);
         for (const Record& r : records_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
         for (cudaEvent_t e : free_events_) cudaEventDestroy(e);
     }
 
-    void set_stream(cudaStream_t s) override { stream_ = s; }
+    void set_stream(cudaStream_t s) override {
+        stream_ = s;
+        drop_graph();
+    }
 
     // ------------------------------------------------------------------ setup
     void set_boundary(const float* xyz, u32 n, int mem) override {
         if (n > bcap_) throw Error(DFSPH_ERR_OUT_OF_RANGE, "boundary count exceeds boundary_capacity");
         nb_ = n;
         drop_pending_counts();
+        drop_graph();
         if (n == 0) {
-            DFSPH_CUDA(cudaMemsetAsync(bcs_.p, 0, (size_t(geom_.total) + 1) * sizeof(u32), stream_));
+            DFSPH_CUDA(cudaMemsetAsync(bcs_.p, 0, (size_t(cells1_) + 1) * sizeof(u32), stream_));
             return;
         }
         const float* src = upload(xyz, nullptr, n, mem);
         launch_import(n, src, nullptr, xb_[0].p, vr_scratch(), bid_[0].p);
         // sort by cell (the boundary CellGrid built once, dfsph.cu:93-97)
-        launch(DFSPH_KERNEL_GRID_COUNT, count_kernel<R>, blocks_for(n, 256), 256, int(n), xb_[0].p, g_, bkey_.p, brank_.p, count_.p);
-        scan(bcs_.p, /*reset ctl*/ false);
-        launch(DFSPH_KERNEL_GRID_SCATTER, scatter_kernel, blocks_for(n, 256), 256, int(n), bkey_.p, brank_.p, bcs_.p, bid_[0].p,
-               btmp_src_.p, btmp_id_.p);
-        launch(DFSPH_KERNEL_GRID_REORDER, reorder_kernel<R>, blocks_for(n, 256), 256, int(n), btmp_src_.p, btmp_id_.p, bkey_.p, bcs_.p,
-               geom_.total, kSentinelCap, xb_[0].p, vr_scratch(), xb_[1].p, vr_scratch2(), bid_[1].p,
-               bkey_sorted_.p, ctl_.p);
+        launch(DFSPH_KERNEL_GRID_COUNT, count_kernel<R>, blocks_for(n, 256), 256, int(n), xb_[0].p, gb_, bkey_.p,
+               brank_.p, count_.p);
+        scan(bcs_.p, cells1_, /*step start*/ false);
+        launch(DFSPH_KERNEL_GRID_SCATTER, scatter_kernel, blocks_for(n, 256), 256, int(n), bkey_.p, brank_.p, bcs_.p,
+               bid_[0].p, btmp_src_.p, btmp_id_.p);
+        launch(DFSPH_KERNEL_GRID_REORDER, reorder_kernel<R>, blocks_for(n, 256), 256, int(n), btmp_src_.p,
+               btmp_id_.p, bkey_.p, bcs_.p, cells1_, kSentinelCap, xb_[0].p, vr_scratch(), xb_[1].p,
+               vr_scratch2(), bid_[1].p, bkey_sorted_.p, ctl_.p);
         // Akinci mass into the w lane (dfsph_kernels.cu:40-65)
-        launch(DFSPH_KERNEL_OTHER, boundary_mass_kernel<R>, blocks_for(n, 128), 128, int(n), xb_[1].p, xb_[0].p, bcs_.p, g_,
-               phys_);
+        launch(DFSPH_KERNEL_OTHER, boundary_mass_kernel<R>, blocks_for(n, 128), 128, int(n), xb_[1].p, xb_[0].p,
+               bcs_.p, gb_, phys_);
         std::swap(bid_[0].p, bid_[1].p);  // bid_[0] holds the sorted order now
-        launch(DFSPH_KERNEL_OTHER, boundary_mask_kernel<R>, blocks_for(geom_.total, 256), 256, geom_.total, bcs_.p, g_,
-               bmask_.p);
+        launch(DFSPH_KERNEL_OTHER, boundary_mask_kernel<R>, blocks_for(geom_.total, 256), 256, geom_.total, bcs_.p,
+               gb_, bmask_.p);
     }
 
     void set_fluid(const float* xyz, const float* vel, u32 n, int mem) override {
-        if (n > cap_) throw Error(DFSPH_ERR_OUT_OF_RANGE, "ParticleStore::resize: count " + std::to_string(n) +
-                                                               " exceeds capacity " + std::to_string(cap_));
+        const u32 counts = n;
+        set_fluid_batch(1, &counts, xyz, vel, mem);
+    }
+
+    void set_fluid_batch(u32 n_scenes, const u32* counts, const float* xyz, const float* vel, int mem) override {
+        if (n_scenes != scenes_)
+            throw Error(DFSPH_ERR_INVALID_ARGUMENT, "scene count differs from the context's n_scenes (" +
+                                                        std::to_string(scenes_) + ")");
+        unsigned long long total = 0;
+        for (u32 s = 0; s < n_scenes; ++s) total += counts[s];
+        if (total > cap_)
+            throw Error(DFSPH_ERR_OUT_OF_RANGE, "ParticleStore::resize: count " + std::to_string(total) +
+                                                    " exceeds capacity " + std::to_string(cap_));
+        const u32 n = static_cast<u32>(total);
         const float* pos = upload(xyz, vel, n, mem);
         const float* v = vel ? pos + 3 * size_t(n) : nullptr;
         if (mem == DFSPH_MEM_DEVICE) { pos = xyz; v = vel; }
         n_ = n;
         drop_pending_counts();
+        drop_graph();
+        scene_counts_.assign(counts, counts + n_scenes);
+        if (scenes_ > 1 && n) {
+            // sorted order is scene-major, so slot -> scene never changes
+            std::vector<unsigned short> ss(n);
+            size_t o = 0;
+            for (u32 s = 0; s < n_scenes; ++s)
+                for (u32 k = 0; k < counts[s]; ++k) ss[o++] = static_cast<unsigned short>(s);
+            DFSPH_CUDA(cudaMemcpyAsync(slot_scene_.p, ss.data(), n * sizeof(unsigned short), cudaMemcpyHostToDevice,
+                                       stream_));
+            DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        }
         if (n == 0) return;
         launch_import(n, pos, v, xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
         counts_valid_ = false;
         have_state_ = true;
     }
 
+    void set_scene_viscosity(const float* eps, u32 n_scenes) override {
+        if (n_scenes != scenes_) throw Error(DFSPH_ERR_INVALID_ARGUMENT, "scene count mismatch");
+        if (scenes_ == 1) {
+            cfg_.viscosity = eps[0];
+            drop_graph();
+            return;
+        }
+        std::vector<R> e(eps, eps + n_scenes);
+        DFSPH_CUDA(cudaMemcpyAsync(eps_scene_.p, e.data(), n_scenes * sizeof(R), cudaMemcpyHostToDevice, stream_));
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        any_xsph_ = false;
+        for (u32 s = 0; s < n_scenes; ++s) any_xsph_ = any_xsph_ || eps[s] > 0.0f;
+        explicit_eps_ = true;
+        drop_graph();
+    }
+
+    void get_scene_max_velocity(float* out, u32 n_scenes) override {
+        if (n_scenes != scenes_) throw Error(DFSPH_ERR_INVALID_ARGUMENT, "scene count mismatch");
+        if (scenes_ == 1) {
+            out[0] = float(get_scalar(DFSPH_SCALAR_MAX_VELOCITY));
+            return;
+        }
+        std::vector<u32> bits(scenes_);
+        DFSPH_CUDA(cudaMemcpyAsync(bits.data(), maxv_scene_.p, scenes_ * sizeof(u32), cudaMemcpyDeviceToHost, stream_));
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        for (u32 s = 0; s < scenes_; ++s) std::memcpy(out + s, &bits[s], sizeof(float));
+        if (!stepped_)
+            for (u32 s = 0; s < scenes_; ++s) out[s] = 0.0f;
+    }
+
     // ------------------------------------------------------------------- step
     void step(float dt, u32 n_steps) override {
-        for (u32 k = 0; k < n_steps; ++k) step_once(R(dt), /*count_next=*/true);
+        u32 k = 0;
+        if (graph_ok()) {
+            if (!counts_valid_ && k < n_steps) {  // the first step after new input counts itself
+                step_once(R(dt), true);
+                ++k;
+            }
+            if (n_steps - k >= 2) {
+                ensure_graph(dt);
+                for (; k + 2 <= n_steps; k += 2) {
+                    DFSPH_CUDA(cudaGraphLaunch(graph_exec_, stream_));
+                    launches_ += graph_kernels_;
+                }
+            }
+        }
+        for (; k < n_steps; ++k) step_once(R(dt), /*count_next=*/true);
     }
 
     void step_store(float* pos, float* vel, u32 n, float dt, float* density, float* alpha, float* kappa,
                     float* density_adv) override {
+        if (scenes_ != 1) throw Error(DFSPH_ERR_STATE, "dfsph_step_store steps one scene");
         if (n > cap_) throw Error(DFSPH_ERR_OUT_OF_RANGE, "store count exceeds capacity");
         n_ = n;
         drop_pending_counts();
+        drop_graph();
         if (n == 0) return;  // dfsph.cu:121-122
         launch_import(n, pos, vel, xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
         counts_valid_ = false;
         have_state_ = true;
         step_once(R(dt), /*count_next=*/false);
-        launch(DFSPH_KERNEL_IO, export_kernel<R>, blocks_for(n, 256), 256, int(n), id_[ci_].p, xk_[cx_].p, vr_[cv_].p,
-               alpha_.p, kap_.p, rho_adv_.p, pos, vel, density, alpha, kappa, density_adv);
+        launch(DFSPH_KERNEL_IO, export_kernel<R>, blocks_for(n, 256), 256, int(n), id_[ci_].p, xk_[cx_].p,
+               vr_[cv_].p, alpha_.p, kap_.p, rho_adv_.p, pos, vel, density, alpha, kappa, density_adv);
     }
 
     // -------------------------------------------------------------- readback
     void get_field(int field, void* dst, size_t bytes, int mem) override {
         size_t need = 0;
-        const size_t n = n_, cells = size_t(geom_.total) + 1;
-        bool is_u32 = false;
+        const size_t n = n_;
         switch (field) {
             case DFSPH_FIELD_POSITION: case DFSPH_FIELD_VELOCITY: need = 3 * n * sizeof(float); break;
             case DFSPH_FIELD_DENSITY: case DFSPH_FIELD_ALPHA: case DFSPH_FIELD_KAPPA:
             case DFSPH_FIELD_DENSITY_ADV: case DFSPH_FIELD_KAPPA_V: need = n * sizeof(float); break;
             case DFSPH_FIELD_CELL_KEY: case DFSPH_FIELD_SORTED_INDEX: case DFSPH_FIELD_NBR_FLUID:
-            case DFSPH_FIELD_NBR_BOUNDARY: need = n * sizeof(u32); is_u32 = true; break;
-            case DFSPH_FIELD_CELL_START: case DFSPH_FIELD_BOUNDARY_CELL_START:
-                need = cells * sizeof(u32); is_u32 = true; break;
+            case DFSPH_FIELD_NBR_BOUNDARY: need = n * sizeof(u32); break;
+            case DFSPH_FIELD_CELL_START: need = keys_ * sizeof(u32); break;
+            case DFSPH_FIELD_BOUNDARY_CELL_START: need = size_t(cells1_) * sizeof(u32); break;
             case DFSPH_FIELD_BOUNDARY_MASS: need = size_t(nb_) * sizeof(float); break;
-            case DFSPH_FIELD_BOUNDARY_SORTED_INDEX: need = size_t(nb_) * sizeof(u32); is_u32 = true; break;
+            case DFSPH_FIELD_BOUNDARY_SORTED_INDEX: need = size_t(nb_) * sizeof(u32); break;
             default: throw Error(DFSPH_ERR_INVALID_ARGUMENT, "unknown field " + std::to_string(field));
         }
-        (void)is_u32;
         if (bytes < need) throw Error(DFSPH_ERR_INVALID_ARGUMENT, "destination too small for field");
         if ((field == DFSPH_FIELD_NBR_FLUID || field == DFSPH_FIELD_NBR_BOUNDARY) && !cfg_.record_diagnostics)
             throw Error(DFSPH_ERR_STATE, "neighbour counts need record_diagnostics = 1");
@@ -205,36 +300,40 @@ public:
         // Produce the field in device scratch (original order), then copy out.
         void* out = (mem == DFSPH_MEM_DEVICE) ? dst : scratch_bytes(need);
         const int nb = blocks_for(std::max<size_t>(n, 1), 256);
+        const u32* id = id_[ci_].p;
         switch (field) {
             case DFSPH_FIELD_POSITION:
-                launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, nb, 256, int(n), id_[ci_].p, xk_[cx_].p, -1, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, nb, 256, int(n), id, xk_[cx_].p, -1, (float*)out);
+                break;
             case DFSPH_FIELD_VELOCITY:
-                launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, nb, 256, int(n), id_[ci_].p, vr_[cv_].p, -1, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, nb, 256, int(n), id, vr_[cv_].p, -1, (float*)out);
+                break;
             case DFSPH_FIELD_DENSITY:
-                launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, nb, 256, int(n), id_[ci_].p, vr_[cv_].p, 3, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, nb, 256, int(n), id, vr_[cv_].p, 3, (float*)out);
+                break;
             case DFSPH_FIELD_ALPHA:
-                launch(DFSPH_KERNEL_IO, unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, alpha_.p, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<R, float>, nb, 256, int(n), id, alpha_.p, (float*)out); break;
             case DFSPH_FIELD_KAPPA:
-                launch(DFSPH_KERNEL_IO, unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, kap_.p, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<R, float>, nb, 256, int(n), id, kap_.p, (float*)out); break;
             case DFSPH_FIELD_DENSITY_ADV:
-                launch(DFSPH_KERNEL_IO, unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, rho_adv_.p, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<R, float>, nb, 256, int(n), id, rho_adv_.p, (float*)out); break;
             case DFSPH_FIELD_KAPPA_V:
-                launch(DFSPH_KERNEL_IO, unsort_kernel<R, float>, nb, 256, int(n), id_[ci_].p, kap_v_.p, (float*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<R, float>, nb, 256, int(n), id, kap_v_.p, (float*)out); break;
             case DFSPH_FIELD_CELL_KEY:
-                launch(DFSPH_KERNEL_IO, unsort_kernel<u32, u32>, nb, 256, int(n), id_[ci_].p, key_sorted_.p, (u32*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<u32, u32>, nb, 256, int(n), id, key_sorted_.p, (u32*)out); break;
             case DFSPH_FIELD_SORTED_INDEX:
-                DFSPH_CUDA(cudaMemcpyAsync(out, id_[ci_].p, need, cudaMemcpyDeviceToDevice, stream_)); break;
+                DFSPH_CUDA(cudaMemcpyAsync(out, id, need, cudaMemcpyDeviceToDevice, stream_)); break;
             case DFSPH_FIELD_CELL_START:
                 DFSPH_CUDA(cudaMemcpyAsync(out, cell_start_.p, need, cudaMemcpyDeviceToDevice, stream_)); break;
             case DFSPH_FIELD_BOUNDARY_CELL_START:
                 DFSPH_CUDA(cudaMemcpyAsync(out, bcs_.p, need, cudaMemcpyDeviceToDevice, stream_)); break;
             case DFSPH_FIELD_NBR_FLUID:
-                launch(DFSPH_KERNEL_IO, unsort_kernel<u32, u32>, nb, 256, int(n), id_[ci_].p, nbr_f_.p, (u32*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<u32, u32>, nb, 256, int(n), id, nbr_f_.p, (u32*)out); break;
             case DFSPH_FIELD_NBR_BOUNDARY:
-                launch(DFSPH_KERNEL_IO, unsort_kernel<u32, u32>, nb, 256, int(n), id_[ci_].p, nbr_b_.p, (u32*)out); break;
+                launch(DFSPH_KERNEL_IO, unsort_kernel<u32, u32>, nb, 256, int(n), id, nbr_b_.p, (u32*)out); break;
             case DFSPH_FIELD_BOUNDARY_MASS:
-                launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, blocks_for(nb_, 256), 256, int(nb_), bid_[0].p, xb_[0].p, 3,
-                       (float*)out);
+                launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, blocks_for(nb_, 256), 256, int(nb_), bid_[0].p,
+                       xb_[0].p, 3, (float*)out);
                 break;
             case DFSPH_FIELD_BOUNDARY_SORTED_INDEX:
                 DFSPH_CUDA(cudaMemcpyAsync(out, bid_[0].p, need, cudaMemcpyDeviceToDevice, stream_)); break;
@@ -276,7 +375,10 @@ public:
 
     void synchronize() override { DFSPH_CUDA(cudaStreamSynchronize(stream_)); }
 
-    void profile_enable(u32 mask) override { profile_mask_ = mask; }
+    void profile_enable(u32 mask) override {
+        profile_mask_ = mask;
+        if (mask) drop_graph();
+    }
 
     void profile_read(int kclass, double* total_ms, unsigned long long* count) override {
         DFSPH_CUDA(cudaStreamSynchronize(stream_));
@@ -302,7 +404,7 @@ private:
 
     template <class K, class... A> void launch(int kclass, K kernel, int grid, int block, A... args) {
         if (grid <= 0) return;
-        const bool prof = (profile_mask_ >> kclass) & 1u;
+        const bool prof = !capturing_ && ((profile_mask_ >> kclass) & 1u);
         cudaEvent_t a = nullptr, b = nullptr;
         if (prof) {
             a = take_event();
@@ -311,7 +413,8 @@ private:
         }
         kernel<<<grid, block, 0, stream_>>>(args...);
         DFSPH_LAUNCHED();
-        ++launches_;
+        if (capturing_) ++graph_kernels_;
+        else ++launches_;
         if (prof) {
             DFSPH_CUDA(cudaEventRecord(b, stream_));
             records_.push_back({kclass, a, b});
@@ -330,11 +433,60 @@ private:
         return e;
     }
 
+    // ---- CUDA graphs: two steps return every ping-pong buffer to where it
+    // started (each step flips x 1 + iterations times, v twice, id once), so a
+    // captured pair of steps replays with the same pointers.
+    bool graph_ok() const {
+        const bool adaptive = cfg_.eta_density > 0.0f || (cfg_.max_divergence_iters > 0 && cfg_.eta_divergence > 0.0f);
+        return cfg_.use_cuda_graph && !adaptive && profile_mask_ == 0 && have_state_ && n_ > 0;
+    }
+    void drop_graph() {
+        if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+        if (graph_) cudaGraphDestroy(graph_);
+        graph_exec_ = nullptr;
+        graph_ = nullptr;
+    }
+    void ensure_graph(float dt) {
+        if (graph_exec_ && graph_dt_ == dt) return;
+        drop_graph();
+        const int cx = cx_, cv = cv_, ci = ci_;
+        const bool counted = counts_valid_, stepped = stepped_;
+        // Capture on a private stream (the caller's may be the legacy default
+        // stream, which cannot be captured); replays go to the caller's stream.
+        if (!capture_stream_) DFSPH_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
+        const cudaStream_t caller = stream_;
+        graph_kernels_ = 0;
+        DFSPH_CUDA(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal));
+        stream_ = capture_stream_;
+        capturing_ = true;
+        try {
+            step_once(R(dt), true);
+            step_once(R(dt), true);
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(capture_stream_, &g);
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            capturing_ = false;
+            stream_ = caller;
+            cx_ = cx; cv_ = cv; ci_ = ci;
+            counts_valid_ = counted;
+            stepped_ = stepped;
+            throw;
+        }
+        capturing_ = false;
+        stream_ = caller;
+        DFSPH_CUDA(cudaStreamEndCapture(capture_stream_, &graph_));
+        if (cx_ != cx || cv_ != cv || ci_ != ci) throw Error(DFSPH_ERR_STATE, "graph capture changed buffer parity");
+        DFSPH_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
+        graph_dt_ = dt;
+    }
+
     // The integrator leaves the next step's per-cell counts in count_; any new
     // input invalidates them and count_ must be zero before the next count.
     void drop_pending_counts() {
         if (!counts_valid_) return;
-        DFSPH_CUDA(cudaMemsetAsync(count_.p, 0, (size_t(geom_.total) + 1) * sizeof(u32), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(count_.p, 0, keys_ * sizeof(u32), stream_));
         counts_valid_ = false;
     }
 
@@ -355,25 +507,22 @@ private:
         launch(DFSPH_KERNEL_IO, import_kernel<R>, blocks_for(n, 256), 256, int(n), pos, vel, xk, vr, id);
     }
 
-    // Scratch 4-vectors for the boundary build: the fluid ping-pong buffers are
-    // free at that point only if no fluid state exists yet, so the boundary
-    // build uses the velocity lanes of its own xb_ buffers' partner: a
-    // dedicated pair is cheaper to reason about.
+    // Scratch 4-vectors for the wall sort's unused velocity lane.
     V4* vr_scratch() { ensure_bscratch(); return bscratch_[0].p; }
     V4* vr_scratch2() { ensure_bscratch(); return bscratch_[1].p; }
     void ensure_bscratch() {
         if (bscratch_[0].n < bcap_) { bscratch_[0].alloc(bcap_); bscratch_[1].alloc(bcap_); }
     }
 
-    // Boundary particles with at least one fluid particle within the kernel
+    // Wall particles with at least one fluid particle within the kernel
     // support, against the fluid grid of the last step (a diagnostic for the
-    // algorithmic byte count of the boundary terms).
+    // algorithmic byte count of the wall terms).
     u32 active_boundary() {
         if (nb_ == 0 || n_ == 0 || !stepped_) return 0;
         u32* d = static_cast<u32*>(scratch_bytes(sizeof(u32)));
         DFSPH_CUDA(cudaMemsetAsync(d, 0, sizeof(u32), stream_));
         launch(DFSPH_KERNEL_OTHER, active_boundary_kernel<R>, blocks_for(nb_, 128), 128, int(nb_), xb_[0].p,
-               xk_[cx_].p, cell_start_.p, g_, phys_, d);
+               xk_[cx_].p, cell_start_.p, gb_, phys_, int(scenes_), d);
         u32 h = 0;
         DFSPH_CUDA(cudaMemcpyAsync(&h, d, sizeof(u32), cudaMemcpyDeviceToHost, stream_));
         DFSPH_CUDA(cudaStreamSynchronize(stream_));
@@ -385,12 +534,15 @@ private:
         return readback_.p;
     }
 
-    void scan(u32* cell_start, bool reset_ctl) {
-        const u32 m = geom_.total + 1;
-        launch(DFSPH_KERNEL_GRID_SCAN, scan_tile_sums, int(n_tiles_), SCAN_BLOCK, count_.p, m, tile_sums_.p);
-        launch(DFSPH_KERNEL_GRID_SCAN, scan_tile_offsets, 1, 1024, tile_sums_.p, n_tiles_, reset_ctl ? ctl_.p : nullptr,
-               reset_ctl ? 3 : 0);
-        launch(DFSPH_KERNEL_GRID_SCAN, scan_tiles, int(n_tiles_), SCAN_BLOCK, count_.p, m, tile_sums_.p, cell_start);
+    // Exclusive scan of the counts of m keys into cell_start[0..m] (closing
+    // entry included). At a step start it also resets the iteration controls.
+    void scan(u32* cell_start, size_t m, bool step_start) {
+        const u32 tiles = static_cast<u32>((m + SCAN_TILE - 1) / SCAN_TILE);
+        launch(DFSPH_KERNEL_GRID_SCAN, scan_tile_sums, int(tiles), SCAN_BLOCK, count_.p, u32(m), tile_sums_.p);
+        launch(DFSPH_KERNEL_GRID_SCAN, scan_tile_offsets, 1, 1024, tile_sums_.p, tiles, cell_start + m,
+               step_start ? ctl_.p : nullptr, step_start ? 3 : 0,
+               step_start && scenes_ > 1 ? maxv_scene_.p : nullptr, step_start && scenes_ > 1 ? int(scenes_) : 0);
+        launch(DFSPH_KERNEL_GRID_SCAN, scan_tiles, int(tiles), SCAN_BLOCK, count_.p, u32(m), tile_sums_.p, cell_start);
     }
 
     BoundaryDev bdev() const {
@@ -423,23 +575,23 @@ private:
         u32 launched = 0;
         for (u32 it = 0; it < max_iters; ++it) {
             if (adaptive)
-                launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true>, blocks_for(n, 128), 128, n, xk_[cx_].p,
-                       xk_[cx_ ^ 1].p, vr_[cv_].p, alpha_.p, adv_out, kap_out, cell_start_.p, g_, phys_,
+                launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true>, blocks_for(n, 128), 128, n,
+                       xk_[cx_].p, xk_[cx_ ^ 1].p, vr_[cv_].p, alpha_.p, adv_out, kap_out, cell_start_.p, g_, phys_,
                        bdev(), dt, partials_.p, ctl, it, first_check, 1.0 / double(n), thr);
             else
-                launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, false>, blocks_for(n, 128), 128, n, xk_[cx_].p,
-                       xk_[cx_ ^ 1].p, vr_[cv_].p, alpha_.p, adv_out, kap_out, cell_start_.p, g_, phys_,
+                launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, false>, blocks_for(n, 128), 128, n,
+                       xk_[cx_].p, xk_[cx_ ^ 1].p, vr_[cv_].p, alpha_.p, adv_out, kap_out, cell_start_.p, g_, phys_,
                        bdev(), dt, partials_.p, ctl, it, first_check, 1.0 / double(n), thr);
             cx_ ^= 1;
-            launch(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p, kap_out,
-                   cell_start_.p, g_, phys_, bdev(), dt, ctl, it);
+            launch(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p,
+                   vr_[cv_].p, kap_out, cell_start_.p, g_, phys_, bdev(), dt, ctl, it);
             launched = it + 1;
             if (adaptive && it >= first_check) {
                 // The reference reads the error back every iteration
                 // (dfsph.cu:296-299); the device already decided, the host
                 // only stops launching.
-                DFSPH_CUDA(cudaMemcpyAsync(&host_ctl_[DIV ? 1 : 2], ctl, sizeof(IterCtl),
-                                           cudaMemcpyDeviceToHost, stream_));
+                DFSPH_CUDA(cudaMemcpyAsync(&host_ctl_[DIV ? 1 : 2], ctl, sizeof(IterCtl), cudaMemcpyDeviceToHost,
+                                           stream_));
                 DFSPH_CUDA(cudaStreamSynchronize(stream_));
                 if (host_ctl_[DIV ? 1 : 2].stop_iter != ~0u) break;
             }
@@ -454,12 +606,13 @@ private:
         stepped_ = true;
         // 1. grid build (CellGrid::build, core/src/cell_grid.cu:73-138)
         if (!counts_valid_)
-            launch(DFSPH_KERNEL_GRID_COUNT, count_kernel<R>, blocks_for(n, 256), 256, n, xk_[cx_].p, g_, key_.p, rank_.p, count_.p);
-        scan(cell_start_.p, /*reset ctl*/ true);
-        launch(DFSPH_KERNEL_GRID_SCATTER, scatter_kernel, blocks_for(n, 256), 256, n, key_.p, rank_.p, cell_start_.p, id_[ci_].p,
-               tmp_src_.p, tmp_id_.p);
-        launch(DFSPH_KERNEL_GRID_REORDER, reorder_kernel<R>, blocks_for(n, 256), 256, n, tmp_src_.p, tmp_id_.p, key_.p, cell_start_.p,
-               geom_.total, kSentinelCap, xk_[cx_].p, vr_[cv_].p, xk_[cx_ ^ 1].p, vr_[cv_ ^ 1].p,
+            launch(DFSPH_KERNEL_GRID_COUNT, count_kernel<R>, blocks_for(n, 256), 256, n, xk_[cx_].p, g_, key_.p,
+                   rank_.p, count_.p);
+        scan(cell_start_.p, keys_, /*step start*/ true);
+        launch(DFSPH_KERNEL_GRID_SCATTER, scatter_kernel, blocks_for(n, 256), 256, n, key_.p, rank_.p, cell_start_.p,
+               id_[ci_].p, tmp_src_.p, tmp_id_.p);
+        launch(DFSPH_KERNEL_GRID_REORDER, reorder_kernel<R>, blocks_for(n, 256), 256, n, tmp_src_.p, tmp_id_.p,
+               key_.p, cell_start_.p, cells1_, kSentinelCap, xk_[cx_].p, vr_[cv_].p, xk_[cx_ ^ 1].p, vr_[cv_ ^ 1].p,
                id_[ci_ ^ 1].p, key_sorted_.p, ctl_.p);
         cx_ ^= 1; cv_ ^= 1; ci_ ^= 1;
         counts_valid_ = false;
@@ -468,29 +621,31 @@ private:
         const bool kahan = cfg_.precision == DFSPH_PRECISION_FP32_KAHAN;
         if (cfg_.record_diagnostics) {
             if (kahan)
-                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, true>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
-                       alpha_.p, cell_start_.p, g_, phys_, bd, nbr_f_.p, nbr_b_.p);
+                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, true>, blocks_for(n, 128), 128, n,
+                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cell_start_.p, g_, phys_, bd, nbr_f_.p, nbr_b_.p);
             else
-                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, true>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
-                       alpha_.p, cell_start_.p, g_, phys_, bd, nbr_f_.p, nbr_b_.p);
+                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, true>, blocks_for(n, 128), 128, n,
+                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cell_start_.p, g_, phys_, bd, nbr_f_.p, nbr_b_.p);
         } else {
             if (kahan)
-                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, false>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
-                       alpha_.p, cell_start_.p, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr);
+                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, false>, blocks_for(n, 128), 128, n,
+                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cell_start_.p, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr);
             else
-                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, false>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
-                       alpha_.p, cell_start_.p, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr);
+                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, false>, blocks_for(n, 128), 128, n,
+                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cell_start_.p, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr);
         }
         // 3. divergence solve (the reference's plan; 0 iterations = the reference)
         last_divergence_launched_ = 0;
         if (cfg_.max_divergence_iters > 0)
-            last_divergence_launched_ =
-                solve<true>(dt, cfg_.max_divergence_iters, cfg_.eta_divergence, ctl_.p + 1, kap_v_.p, rho_dot_.p);
+            last_divergence_launched_ = solve<true>(dt, cfg_.max_divergence_iters, cfg_.eta_divergence, ctl_.p + 1,
+                                                    kap_v_.p, rho_dot_.p);
         // 4. gravity + damping + XSPH (dfsph.cu:188-213)
         const R decay = std::exp(-R(cfg_.damping) * dt);
-        launch(DFSPH_KERNEL_FORCES_XSPH, forces_xsph_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p, vr_[cv_ ^ 1].p,
-               cell_start_.p, g_, phys_, decay, R(cfg_.gravity[0]) * dt, R(cfg_.gravity[1]) * dt,
-               R(cfg_.gravity[2]) * dt, R(cfg_.viscosity), cfg_.viscosity > 0.0f ? 1 : 0);
+        const bool xsph = explicit_eps_ ? any_xsph_ : cfg_.viscosity > 0.0f;
+        launch(DFSPH_KERNEL_FORCES_XSPH, forces_xsph_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
+               vr_[cv_ ^ 1].p, cell_start_.p, g_, phys_, decay, R(cfg_.gravity[0]) * dt, R(cfg_.gravity[1]) * dt,
+               R(cfg_.gravity[2]) * dt, R(cfg_.viscosity), scenes_ > 1 ? (const R*)eps_scene_.p : (const R*)nullptr,
+               xsph ? 1 : 0);
         cv_ ^= 1;
         // 5. density solve (dfsph.cu:215-260)
         last_density_launched_ =
@@ -498,13 +653,14 @@ private:
         // 6. advect + max |v| (+ next step's cell counts)
         const R lo[3] = {R(cfg_.domain_min[0]), R(cfg_.domain_min[1]), R(cfg_.domain_min[2])};
         const R hi[3] = {R(cfg_.domain_max[0]), R(cfg_.domain_max[1]), R(cfg_.domain_max[2])};
+        u32* mvs = scenes_ > 1 ? maxv_scene_.p : nullptr;
         if (count_next) {
-            launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, true>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p, dt, lo[0], lo[1],
-                   lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p);
+            launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, true>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p,
+                   dt, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p, mvs);
             counts_valid_ = true;
         } else {
-            launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, false>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p, dt, lo[0], lo[1],
-                   lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p);
+            launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, false>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p,
+                   dt, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p, mvs);
         }
     }
 
@@ -512,10 +668,15 @@ private:
     int device_;
     cudaStream_t stream_;
     GridGeom geom_;
-    GridDev<R> g_;
+    GridDev<R> g_;   // fluid grid (scene-aware)
+    GridDev<R> gb_;  // wall grid
     Phys<R> phys_;
     float mass_f_ = 0;
     u32 cap_ = 0, bcap_ = 0, n_ = 0, nb_ = 0, n_tiles_ = 0;
+    u32 scenes_ = 1, cells1_ = 0;
+    size_t keys_ = 0;
+    std::vector<u32> scene_counts_;
+    bool explicit_eps_ = false, any_xsph_ = false;
     int cx_ = 0, cv_ = 0, ci_ = 0;
     bool counts_valid_ = false, have_state_ = false, stepped_ = false;
     u32 last_density_launched_ = 0, last_divergence_launched_ = 0;
@@ -523,11 +684,19 @@ private:
     u32 profile_mask_ = 0;
     std::vector<Record> records_;
     std::vector<cudaEvent_t> free_events_;
+    // CUDA graph of two steps
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t graph_exec_ = nullptr;
+    float graph_dt_ = 0.0f;
+    unsigned long long graph_kernels_ = 0;
+    bool capturing_ = false;
+    cudaStream_t capture_stream_ = nullptr;
 
     DevBuf<V4> xk_[2], vr_[2], xb_[2], bscratch_[2];
     DevBuf<u32> id_[2], bid_[2];
-    DevBuf<R> alpha_, rho_adv_, kap_, kap_v_, rho_dot_;
-    DevBuf<u32> key_, rank_, tmp_src_, tmp_id_, key_sorted_, nbr_f_, nbr_b_;
+    DevBuf<R> alpha_, rho_adv_, kap_, kap_v_, rho_dot_, eps_scene_;
+    DevBuf<u32> key_, rank_, tmp_src_, tmp_id_, key_sorted_, nbr_f_, nbr_b_, maxv_scene_;
+    DevBuf<unsigned short> slot_scene_;
     DevBuf<u32> bkey_, brank_, bkey_sorted_, btmp_src_, btmp_id_;
     DevBuf<u32> count_, cell_start_, tile_sums_, bcs_;
     DevBuf<unsigned char> bmask_;

@@ -21,6 +21,10 @@ struct SolverBase {
     virtual void set_stream(cudaStream_t s) = 0;
     virtual void set_boundary(const float* xyz, std::uint32_t n, int mem) = 0;
     virtual void set_fluid(const float* xyz, const float* vel, std::uint32_t n, int mem) = 0;
+    virtual void set_fluid_batch(std::uint32_t n_scenes, const std::uint32_t* counts, const float* xyz,
+                                 const float* vel, int mem) = 0;
+    virtual void set_scene_viscosity(const float* eps, std::uint32_t n_scenes) = 0;
+    virtual void get_scene_max_velocity(float* out, std::uint32_t n_scenes) = 0;
     virtual void step(float dt, std::uint32_t n_steps) = 0;
     virtual void step_store(float* pos, float* vel, std::uint32_t n, float dt, float* density, float* alpha,
                             float* kappa, float* density_adv) = 0;
@@ -38,5 +42,9 @@ std::unique_ptr<SolverBase> make_solver_fp64(const dfsph_config& cfg, int device
 void build_cell_grid(const float* xyz, std::uint32_t n, const float origin[3], const int dims[3],
                      float cell_length, std::uint32_t* sorted_keys, std::uint32_t* sorted_idx,
                      std::uint32_t* cell_start, cudaStream_t st);
+
+// SpatialAccel's Morton order (core/src/spatial_accel.cu:11-40,158-179).
+void morton_sort(const float* xyz, std::uint32_t n, const float smin[3], const float smax[3],
+                 std::uint32_t* sorted_codes, std::uint32_t* sorted_idx, cudaStream_t st);
 
 }  // namespace dfsph

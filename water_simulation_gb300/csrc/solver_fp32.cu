@@ -25,7 +25,7 @@ void build_cell_grid(const float* xyz, u32 n, const float origin[3], const int d
     }
     const u32 n_tiles = u32((cells + SCAN_TILE - 1) / SCAN_TILE);
     // one allocation for every temporary
-    const size_t words = cells /*count*/ + (n_tiles + 1) + 7 * size_t(n);
+    const size_t words = cells /*count*/ + (cells + 1) /*starts*/ + (n_tiles + 1) + 7 * size_t(n);
     const size_t vbytes = 4 * size_t(n) * sizeof(R4<float>);
     unsigned char* mem = nullptr;
     DFSPH_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&mem), vbytes + words * sizeof(u32), st));
@@ -35,6 +35,7 @@ void build_cell_grid(const float* xyz, u32 n, const float origin[3], const int d
     R4<float>* v_out = v_in + n;
     u32* w = reinterpret_cast<u32*>(mem + vbytes);
     u32* count = w; w += cells;
+    u32* starts = w; w += cells + 1;  // cell_start with its closing entry
     u32* tiles = w; w += n_tiles + 1;
     u32* key = w; w += n;
     u32* rank = w; w += n;
@@ -55,15 +56,16 @@ void build_cell_grid(const float* xyz, u32 n, const float origin[3], const int d
     const u32 m = geo.total + 1;
     scan_tile_sums<<<n_tiles, SCAN_BLOCK, 0, st>>>(count, m, tiles);
     DFSPH_LAUNCHED();
-    scan_tile_offsets<<<1, 1024, 0, st>>>(tiles, n_tiles, nullptr, 0);
+    scan_tile_offsets<<<1, 1024, 0, st>>>(tiles, n_tiles, starts + m, nullptr, 0, nullptr, 0);
     DFSPH_LAUNCHED();
-    scan_tiles<<<n_tiles, SCAN_BLOCK, 0, st>>>(count, m, tiles, cell_start);
+    scan_tiles<<<n_tiles, SCAN_BLOCK, 0, st>>>(count, m, tiles, starts);
     DFSPH_LAUNCHED();
-    scatter_kernel<<<blocks_for(n, 256), 256, 0, st>>>(int(n), key, rank, cell_start, id0, tsrc, tid);
+    scatter_kernel<<<blocks_for(n, 256), 256, 0, st>>>(int(n), key, rank, starts, id0, tsrc, tid);
     DFSPH_LAUNCHED();
-    reorder_kernel<float><<<blocks_for(n, 256), 256, 0, st>>>(int(n), tsrc, tid, key, cell_start, geo.total,
-                                                              ~0u, x_in, v_in, x_out, v_out, idn, ks, ctl);
+    reorder_kernel<float><<<blocks_for(n, 256), 256, 0, st>>>(int(n), tsrc, tid, key, starts, m, ~0u, x_in, v_in,
+                                                              x_out, v_out, idn, ks, ctl);
     DFSPH_LAUNCHED();
+    DFSPH_CUDA(cudaMemcpyAsync(cell_start, starts, size_t(m) * sizeof(u32), cudaMemcpyDeviceToDevice, st));
     if (sorted_keys) DFSPH_CUDA(cudaMemcpyAsync(sorted_keys, ks, size_t(n) * sizeof(u32), cudaMemcpyDeviceToDevice, st));
     if (sorted_idx) DFSPH_CUDA(cudaMemcpyAsync(sorted_idx, idn, size_t(n) * sizeof(u32), cudaMemcpyDeviceToDevice, st));
     DFSPH_CUDA(cudaFreeAsync(ctl, st));

@@ -144,19 +144,52 @@ def puddle(seed: int = 1) -> Scene:
 def dam_break(scale: int = 1, reference_mode: bool = True) -> Scene:
     """Dam break: a (40 x 80 x 40) * scale column at spacing 0.01 / scale against the
     x = 0 wall of a 1.6 x 1.0 x 0.6 m tank (scale 1: 128,000 particles, scale 2:
-    1,024,000). The first particle sits 3 spacings from the walls (boundary layers
-    occupy [0, 2s]); the column is centred in z. Fixed 4 density iterations and,
+    1,024,000). The block starts 3 spacings inside the x = 0 wall and the floor
+    (the wall layers occupy [0, 2s]), lattice points at lo + (i + 1/2) s, i.e. at
+    cell centres; the column is centred in z. Fixed 4 density iterations and,
     outside reference mode, 2 divergence iterations; dt = 5e-4 / scale."""
     r = 0.005 / scale
     s = 2 * r
     nx, ny, nz = 40 * scale, 80 * scale, 40 * scale
-    lo = (2.5 * s, 2.5 * s, 0.5 * (0.6 - nz * s))
+    lo = (3.0 * s, 3.0 * s, 0.5 * (0.6 - nz * s))
     fluid = lattice_block(lo, (nx, ny, nz), s, 0.05 * r, 2 if scale == 1 else 3)
     dlo, dhi = (0.0, 0.0, 0.0), (1.6, 1.0, 0.6)
     return Scene(f"dam_break_{nx * ny * nz}", r, dlo, dhi, fluid, np.zeros_like(fluid),
                  sample_aabb_boundary(dlo, dhi, s, 3), dt=5e-4 / scale,
                  steps=2000 if scale == 1 else 500, viscosity=0.01,
                  max_density_iters=4, max_divergence_iters=0 if reference_mode else 2)
+
+
+def batched_blocks(n_scenes: int = 64, seed_base: int = 1000, n_min: int = 2000, n_max: int = 60000):
+    """Independent falling blocks in the unit box, one per scene: scene k draws
+    (from seed seed_base + k) a particle count uniform in [n_min, n_max], block
+    aspect ratios x:y and z:y uniform in [0.5, 2] and an XSPH coefficient
+    uniform in [0.005, 0.05]; r = 0.01 m, dt = 1e-3 s. All scenes share the
+    wall particles of the box. Returns (scenes, viscosities)."""
+    r = 0.01
+    s = 2 * r
+    lo_box, hi_box = (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)
+    walls = sample_aabb_boundary(lo_box, hi_box, s, 3)
+    max_cells = int(round((1.0 - 6 * s) / s))  # lattice sites between the wall layers
+    out, eps = [], []
+    for k in range(n_scenes):
+        seed = seed_base + k
+        u = uniform01(seed, np.arange(4, dtype=np.uint64))
+        target = n_min + u[0] * (n_max - n_min)
+        ax = 0.5 + 1.5 * u[1]
+        az = 0.5 + 1.5 * u[2]
+        ny = max(1, int(round((target / (ax * az)) ** (1.0 / 3.0))))
+        nx = min(max_cells, max(1, int(round(ax * ny))))
+        nz = min(max_cells, max(1, int(round(az * ny))))
+        ny = min(max_cells, ny)
+        lo = (0.5 - 0.5 * nx * s, min(0.3, 1.0 - 3 * s - ny * s), 0.5 - 0.5 * nz * s)
+        fluid = lattice_block(lo, (nx, ny, nz), s, 0.05 * r, seed)
+        e = 0.005 + 0.045 * u[3]
+        sc = Scene(f"batch_{k}", r, lo_box, hi_box, fluid, np.zeros_like(fluid), walls, dt=1e-3, steps=300,
+                   viscosity=float(np.float32(e)), max_density_iters=4, max_divergence_iters=0)
+        out.append(sc)
+        eps.append(float(np.float32(e)))
+    return out, eps
 
 
 def falling_block(n_side=(12, 12, 12), seed: int = 7, radius: float = 0.01,

@@ -83,6 +83,30 @@ class Solver:
                                               xyz.shape[0], _lib.MEM_HOST))
         self.n = xyz.shape[0]
 
+    def set_fluid_batch(self, fluids, velocities=None) -> None:
+        """One array of positions (and velocities) per scene (n_scenes > 1)."""
+        counts = np.array([f.shape[0] for f in fluids], dtype=np.uint32)
+        xyz = np.ascontiguousarray(np.concatenate(fluids, axis=0), dtype=np.float32)
+        vp = None
+        if velocities is not None:
+            vel = np.ascontiguousarray(np.concatenate(velocities, axis=0), dtype=np.float32)
+            vp = vel.ctypes.data_as(ctypes.c_void_p)
+        self._check(self._lib.dfsph_set_fluid_batch(self._ctx, len(counts), counts.ctypes.data_as(ctypes.c_void_p),
+                                                    xyz.ctypes.data_as(ctypes.c_void_p), vp, _lib.MEM_HOST))
+        self.n = int(counts.sum())
+        self.scene_counts = counts
+
+    def set_scene_viscosity(self, eps) -> None:
+        e = np.ascontiguousarray(eps, dtype=np.float32)
+        self._check(self._lib.dfsph_set_scene_viscosity(self._ctx, e.ctypes.data_as(ctypes.POINTER(ctypes.c_float)),
+                                                        e.size))
+
+    def scene_max_velocity(self, n_scenes: int) -> np.ndarray:
+        out = np.zeros(n_scenes, np.float32)
+        self._check(self._lib.dfsph_get_scene_max_velocity(self._ctx, out.ctypes.data_as(
+            ctypes.POINTER(ctypes.c_float)), n_scenes))
+        return out
+
     def set_fluid_device(self, xyz_ptr: int, vel_ptr: int | None, n: int) -> None:
         self._check(self._lib.dfsph_set_fluid(self._ctx, ctypes.c_void_p(xyz_ptr),
                                               ctypes.c_void_p(vel_ptr) if vel_ptr else None, n,
