@@ -79,11 +79,16 @@ template <class R> __device__ __forceinline__ R kernel_w(R r, const Phys<R>& p) 
 // ---------------------------------------------------------------------------
 // Reductions: FP64 block partial sums with a deterministic last-block finish.
 // ---------------------------------------------------------------------------
+constexpr int MAXV_SLOTS = 32;
+
 struct IterCtl {
     double err_sum;       // sum of the last finished reduction
     u32 stop_iter;        // iteration after which the solver stopped (~0u: running)
     u32 blocks_done;      // last-block counter
-    u32 maxv_bits;        // max |v| as float bits (non-negative floats order as ints)
+    u32 maxv_bits;        // unused
+    u32 maxv_slot[32];    // max |v| as float bits (non-negative floats order as
+                          // ints), spread over MAXV_SLOTS words; the max of the
+                          // words is the step's max |v|
     u32 flags;            // bit0: non-finite seen; bit1: sentinel order not canonical
 };
 
@@ -223,6 +228,7 @@ static __global__ void __launch_bounds__(1024) scan_tile_offsets(u32* __restrict
             ctl[k].stop_iter = ~0u;
             ctl[k].blocks_done = 0u;
             ctl[k].maxv_bits = 0u;
+            for (int w = 0; w < MAXV_SLOTS; ++w) ctl[k].maxv_slot[w] = 0u;
             ctl[k].flags = 0u;
         }
     }
@@ -505,6 +511,7 @@ __global__ void __launch_bounds__(128) density_alpha_kernel(
     u32 cf = 0, cb = 0;
     for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
         if (DIAG) cf += e - b;
+#pragma unroll 2
         for (u32 j = b; j < e; ++j) {
             const R4<R> pj = ld(xk + j);
             const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
@@ -629,6 +636,7 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
         const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
         R rd = 0;
         for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+#pragma unroll 2
             for (u32 j = b; j < e; ++j) {
                 const R4<R> pj = ld(xk_in + j);
                 const R4<R> vj = ld(vr + j);
@@ -773,10 +781,18 @@ __global__ void __launch_bounds__(256) advect_kernel(
         const u32 m = __reduce_max_sync(peers, vbits);
         if (i < n && (threadIdx.x & 31) == __ffs(peers) - 1 && m) atomicMax(maxv_scene + scene, m);
     }
-    // max over the warp, then one atomic per warp (NaN bits dominate)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) vbits = max(vbits, __shfl_xor_sync(0xffffffffu, vbits, o));
-    if ((threadIdx.x & 31) == 0 && vbits) atomicMax(&ctl->maxv_bits, vbits);
+    // max over the block, then one atomic per block into one of MAXV_SLOTS
+    // words (one word for every block would serialise the atomics in L2);
+    // NaN bits dominate every finite magnitude
+    __shared__ u32 wmax[8];
+    const u32 m = __reduce_max_sync(0xffffffffu, vbits);
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        u32 b = 0;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) b = max(b, wmax[w]);
+        if (b) atomicMax(&ctl->maxv_slot[blockIdx.x % MAXV_SLOTS], b);
+    }
 }
 
 }  // namespace dfsph

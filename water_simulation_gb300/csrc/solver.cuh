@@ -358,8 +358,10 @@ public:
         read_ctl();
         switch (which) {
             case DFSPH_SCALAR_MAX_VELOCITY: {
+                u32 bits = 0;
+                for (int w = 0; w < MAXV_SLOTS; ++w) bits = std::max(bits, host_ctl_[0].maxv_slot[w]);
                 float f;
-                std::memcpy(&f, &host_ctl_[0].maxv_bits, sizeof(f));
+                std::memcpy(&f, &bits, sizeof(f));
                 return stepped_ ? double(f) : 0.0;
             }
             case DFSPH_SCALAR_LAST_DENSITY_ITERS:
