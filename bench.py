@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched comparison")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-drop timing")
     return ap.parse_args()
 
 
@@ -329,6 +330,60 @@ def bench_batch(steps, n_scenes=64, warmup=3):
             "batched_ms_per_step": ms_batch / steps, "sequential_ms_per_step": ms_seq / steps}
 
 
+def bench_adjoint(graph: bool):
+    """Differentiable drop: 32,768 particles (32^3 block, r = 0.01 m), 200 steps
+    at dt = 1e-3 s, fixed 2 divergence + 4 density iterations, checkpoint every
+    20 steps, loss = mean |x_T - (x_0 + (0.1, 0, 0))|^2. forward =
+    dfsph_adjoint_forward (the 200 steps + 11 checkpoints), backward =
+    dfsph_adjoint_backward (each 20-step segment replayed once with its
+    per-step records, then the reverse kernels). Device time on the solver's
+    stream; the loss gradient is formed on the device between the two."""
+    import torch
+
+    from water_simulation_gb300 import scenes
+    from water_simulation_gb300.solver import Solver
+
+    sc = scenes.adjoint_drop()
+    every = sc.extra["checkpoint_every"]
+    stream = torch.cuda.current_stream()
+    cfg = sc.config()
+    cfg.use_cuda_graph = 1 if graph else 0
+    s = Solver(cfg, stream=stream.cuda_stream)
+    s.set_boundary(sc.boundary)
+    dev = torch.device("cuda")
+    x0 = torch.tensor(sc.fluid, device=dev)
+    v0 = torch.tensor(sc.velocity, device=dev)
+    tgt = x0 + torch.tensor(sc.extra["target_shift"], dtype=torch.float32, device=dev)
+    xT, vT = torch.empty_like(x0), torch.empty_like(v0)
+    gx0, gv0 = torch.empty_like(x0), torch.empty_like(v0)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    res = None
+    for rep in range(2):  # the first pass allocates the checkpoints and records
+        s.adjoint_set_state_device(x0.data_ptr(), v0.data_ptr(), sc.n)
+        torch.cuda.synchronize()
+        l0 = s.kernel_launches()
+        ev[0].record(stream)
+        s.adjoint_forward(sc.dt, sc.steps, every)
+        ev[1].record(stream)
+        l1 = s.kernel_launches()
+        s.adjoint_state_device(xT.data_ptr(), vT.data_ptr())
+        xbar = (2.0 / sc.n) * (xT - tgt)
+        loss = ((xT - tgt) ** 2).sum(dim=1).mean()
+        ev[2].record(stream)
+        ge = s.adjoint_backward_device(xbar.data_ptr(), None, gx0.data_ptr(), gv0.data_ptr())
+        ev[3].record(stream)
+        torch.cuda.synchronize()
+        l2 = s.kernel_launches()
+        fwd, bwd = ev[0].elapsed_time(ev[1]), ev[2].elapsed_time(ev[3])
+        res = {"workload": sc.name, "particles": sc.n, "steps": sc.steps, "checkpoint_every": every,
+               "cuda_graph_forward": bool(graph), "forward_ms": fwd, "backward_ms": bwd,
+               "backward_over_forward": bwd / fwd, "forward_launches": l1 - l0,
+               "backward_launches": l2 - l1, "loss": float(loss), "grad_xsph": ge,
+               "grad_v0_norm": float(gv0.norm()), "finite": bool(torch.isfinite(gv0).all())}
+    s.close()
+    return res
+
+
 def cpu_sample(sc, steps, threads=0):
     """The FP32 restatement of the reference step on the host cores."""
     from oracle import oracle as O
@@ -464,6 +519,14 @@ def main():
             line["batched"] = bench_batch(20)
         except Exception as e:
             line["batched"] = {"unavailable": str(e)[:200]}
+    if rank == 0 and not args.no_adjoint:
+        try:
+            plain, graphed = bench_adjoint(False), bench_adjoint(True)
+            line["adjoint"] = {"plain_forward": plain, "graph_forward": graphed,
+                               "backward_over_forward": max(plain["backward_over_forward"],
+                                                            graphed["backward_over_forward"])}
+        except Exception as e:
+            line["adjoint"] = {"unavailable": str(e)[:200]}
     if rank == 0 and not args.no_ref_cuda:
         try:
             line["ref_cuda"] = bench_ref_cuda(sc, 3 if sc.n > 500000 else 10)

@@ -123,7 +123,8 @@ typedef struct dfsph_ctx dfsph_ctx;
 #define DFSPH_KERNEL_ADVECT           8   /* integrator + max |v| (+ next counts)  */
 #define DFSPH_KERNEL_IO               9   /* import / export / readback           */
 #define DFSPH_KERNEL_OTHER           10
-#define DFSPH_KERNEL_CLASSES         11
+#define DFSPH_KERNEL_ADJOINT         11   /* reverse-mode kernels of dfsph_adjoint_backward */
+#define DFSPH_KERNEL_CLASSES         12
 
 /* Reference defaults of DFSPHSolver::Config (dfsph.h:19-33). */
 int dfsph_config_init(dfsph_config* cfg);
@@ -185,6 +186,33 @@ int dfsph_get_scalar(dfsph_ctx* ctx, int which, double* out);
  * and forgets them. */
 int dfsph_profile_enable(dfsph_ctx* ctx, uint32_t mask);
 int dfsph_profile_read(dfsph_ctx* ctx, int kernel_class, double* total_ms, uint64_t* launches);
+
+/* ---- differentiable rollout (no counterpart in the reference) -------------
+ * Reverse-mode derivative of dfsph_step through every stage: density + alpha,
+ * both Jacobi solvers with their fixed iteration counts, wall terms, XSPH and
+ * the integrator (max(.,0) and clamps use the forward pass's active sets).
+ * Needs one scene and fixed iteration counts (eta_density = 0, and
+ * eta_divergence = 0 when max_divergence_iters > 0), else DFSPH_ERR_STATE.
+ * Arrays hold the working type T: float for DFSPH_PRECISION_FP32 and
+ * FP32_KAHAN, double for DFSPH_PRECISION_FP64; positions and velocities are
+ * T[3n] in the caller's original particle order. */
+/* Fluid state in the working type (dfsph_set_fluid without the float rounding
+ * of an FP64 context). vel may be NULL (zero). */
+int dfsph_adjoint_set_state(dfsph_ctx* ctx, const void* pos, const void* vel, uint32_t n, int mem);
+/* Current state in the working type. Either pointer may be NULL. */
+int dfsph_adjoint_get_state(dfsph_ctx* ctx, void* pos, void* vel, int mem);
+/* n_steps steps of dfsph_step from the current state, keeping a checkpoint of
+ * (x, v) in device memory every checkpoint_every steps (and the final state).
+ * The context then holds x_T, v_T. The XSPH coefficient in use is recorded. */
+int dfsph_adjoint_forward(dfsph_ctx* ctx, float dt, uint32_t n_steps, uint32_t checkpoint_every);
+/* Given dL/dx_T and dL/dv_T (vel_bar may be NULL = 0), writes dL/dx_0,
+ * dL/dv_0 (either output may be NULL) and *xsph_bar = dL/d(XSPH coefficient)
+ * accumulated in FP64 (may be NULL). Each segment between checkpoints is
+ * replayed once with its per-step records (neighbour structure included),
+ * then differentiated step by step in reverse. The context is left at the
+ * rollout's final state. */
+int dfsph_adjoint_backward(dfsph_ctx* ctx, const void* pos_bar, const void* vel_bar, void* pos0_bar,
+                           void* vel0_bar, double* xsph_bar, int mem);
 
 /* Wait for the context's stream; returns a pending device error if any. */
 int dfsph_synchronize(dfsph_ctx* ctx);

@@ -70,6 +70,57 @@ struct Config {
 
 template <class R> struct V3 { R x, y, z; };
 
+// Forward-mode dual number: a value and its derivative along one direction.
+// Solver<Dual> runs the FP64 step on the values (every branch, max(0, .),
+// clamp and neighbour set decided by them) and carries the exact directional
+// derivative of the step along, which is the checker of the GPU adjoint
+// (dfsph_adjoint_backward): <gradient, direction> must equal it.
+struct Dual {
+    double v = 0.0, d = 0.0;
+    Dual() = default;
+    Dual(double a) : v(a), d(0.0) {}  // NOLINT: constants promote implicitly
+    Dual(double a, double b) : v(a), d(b) {}
+    explicit operator double() const { return v; }
+    Dual operator-() const { return {-v, -d}; }
+    Dual& operator+=(const Dual& o) { v += o.v; d += o.d; return *this; }
+    Dual& operator-=(const Dual& o) { v -= o.v; d -= o.d; return *this; }
+    Dual& operator*=(const Dual& o) { d = d * o.v + v * o.d; v *= o.v; return *this; }
+};
+inline Dual operator+(const Dual& a, const Dual& b) { return {a.v + b.v, a.d + b.d}; }
+inline Dual operator-(const Dual& a, const Dual& b) { return {a.v - b.v, a.d - b.d}; }
+inline Dual operator*(const Dual& a, const Dual& b) { return {a.v * b.v, a.d * b.v + a.v * b.d}; }
+inline Dual operator/(const Dual& a, const Dual& b) { return {a.v / b.v, (a.d * b.v - a.v * b.d) / (b.v * b.v)}; }
+inline Dual operator+(const Dual& a, double b) { return {a.v + b, a.d}; }
+inline Dual operator+(double a, const Dual& b) { return {a + b.v, b.d}; }
+inline Dual operator-(const Dual& a, double b) { return {a.v - b, a.d}; }
+inline Dual operator-(double a, const Dual& b) { return {a - b.v, -b.d}; }
+inline Dual operator*(const Dual& a, double b) { return {a.v * b, a.d * b}; }
+inline Dual operator*(double a, const Dual& b) { return {a * b.v, a * b.d}; }
+inline Dual operator/(const Dual& a, double b) { return {a.v / b, a.d / b}; }
+inline Dual operator/(double a, const Dual& b) { return {a / b.v, -a * b.d / (b.v * b.v)}; }
+inline bool operator<(const Dual& a, const Dual& b) { return a.v < b.v; }
+inline bool operator>(const Dual& a, const Dual& b) { return a.v > b.v; }
+inline bool operator<=(const Dual& a, const Dual& b) { return a.v <= b.v; }
+inline bool operator>=(const Dual& a, const Dual& b) { return a.v >= b.v; }
+inline bool operator==(const Dual& a, const Dual& b) { return a.v == b.v; }
+inline bool operator!=(const Dual& a, const Dual& b) { return a.v != b.v; }
+inline bool operator<(const Dual& a, double b) { return a.v < b; }
+inline bool operator>(const Dual& a, double b) { return a.v > b; }
+// sqrt(0) carries a zero derivative: only a self pair has r^2 = 0, and its
+// r^2 is identically zero.
+inline Dual sqrt(const Dual& a) {
+    const double r = std::sqrt(a.v);
+    return {r, r > 0.0 ? a.d / (2.0 * r) : 0.0};
+}
+inline Dual exp(const Dual& a) {
+    const double e = std::exp(a.v);
+    return {e, e * a.d};
+}
+inline double floor(const Dual& a) { return std::floor(a.v); }
+using std::exp;
+using std::floor;
+using std::sqrt;
+
 // Float -> int conversion with the GPU's cvt.rzi.s32.f32 semantics
 // (NaN -> 0, saturating). The reference casts floorf(...) results to int
 // (core/src/cell_grid.cu:11-13, dfsph_kernels.cu:15-17); on the GPU that cast
@@ -113,9 +164,9 @@ static inline u32 linear_cell(long long cx, long long cy, long long cz, const Gr
 // 1.0f / cell_length computed in CellGrid::build (core/src/cell_grid.cu:81).
 template <class R>
 static inline u32 hash_cell(const V3<R>& p, const Grid& g, R inv) {
-    const long long cx = f2i_sat(std::floor((p.x - R(g.origin[0])) * inv));
-    const long long cy = f2i_sat(std::floor((p.y - R(g.origin[1])) * inv));
-    const long long cz = f2i_sat(std::floor((p.z - R(g.origin[2])) * inv));
+    const long long cx = f2i_sat(floor((p.x - R(g.origin[0])) * inv));
+    const long long cy = f2i_sat(floor((p.y - R(g.origin[1])) * inv));
+    const long long cz = f2i_sat(floor((p.z - R(g.origin[2])) * inv));
     if (cx < 0 || cx >= g.dims[0] || cy < 0 || cy >= g.dims[1] || cz < 0 || cz >= g.dims[2])
         return g.total;
     return linear_cell(cx, cy, cz, g);
@@ -166,9 +217,9 @@ static void build_grid(const V3<R>* pos, std::size_t n, const Grid& g, GridArray
 template <class R, class F>
 static inline void for_neighbors(const V3<R>& p, const Grid& g, R inv_stencil,
                                  const GridArrays& ga, F&& f) {
-    const long long cx = f2i_sat(std::floor((p.x - R(g.origin[0])) * inv_stencil));
-    const long long cy = f2i_sat(std::floor((p.y - R(g.origin[1])) * inv_stencil));
-    const long long cz = f2i_sat(std::floor((p.z - R(g.origin[2])) * inv_stencil));
+    const long long cx = f2i_sat(floor((p.x - R(g.origin[0])) * inv_stencil));
+    const long long cy = f2i_sat(floor((p.y - R(g.origin[1])) * inv_stencil));
+    const long long cz = f2i_sat(floor((p.z - R(g.origin[2])) * inv_stencil));
     for (int dz = -1; dz <= 1; ++dz)
         for (int dy = -1; dy <= 1; ++dy)
             for (int dx = -1; dx <= 1; ++dx) {
@@ -196,7 +247,7 @@ template <class R> static inline R kernel_W(R r, R l) {
 // Cubic spline gradient (core/include/water/core/sph_kernels.cuh:25-41).
 template <class R> static inline V3<R> kernel_gradW(const V3<R>& rij, R l) {
     const R r2 = rij.x * rij.x + rij.y * rij.y + rij.z * rij.z;
-    const R r = std::sqrt(r2);
+    const R r = sqrt(r2);
     if (r < R(1e-12)) return {R(0), R(0), R(0)};
     const R q = r / l;
     if (q >= R(2)) return {R(0), R(0), R(0)};
@@ -230,11 +281,13 @@ struct Solver {
     u32 last_density_iters = 0, last_divergence_iters = 0;
     R max_v = 0;
     R last_density_err = 0, last_divergence_err = 0;
+    R xsph = 0;  // XSPH coefficient (Config::viscosity; a Dual carries its seed)
 
     void init(const Config& c, const float* fx, const float* fv, std::size_t n,
               const float* bx, std::size_t nb) {
         cfg = c;
         grid = make_grid(c);
+        xsph = R(c.viscosity);
         l = R(c.smoothing_length);
         // The stencil reciprocal: the device value when given (the FP32 instance
         // must match the device's stencil centring bit for bit), else IEEE.
@@ -280,7 +333,7 @@ struct Solver {
             const V3<R> pi = xb[i];
             for_neighbors(pi, grid, inv_stencil, bg, [&](u32 j) {
                 const V3<R> r = sub(pi, xb[j]);
-                const R d = std::sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
+                const R d = sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
                 sum_w += kernel_W(d, l);
             });
             mb[i] = R(cfg.rest_density) / std::max(sum_w, R(1e-9));
@@ -298,14 +351,14 @@ struct Solver {
             u32 cf = 0, cb = 0;
             for_neighbors(pi, grid, inv_stencil, fg, [&](u32 j) {
                 const V3<R> r = sub(pi, x[j]);
-                const R d = std::sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
+                const R d = sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
                 r_acc += mass * kernel_W(d, l);
                 ++cf;
             });
             if (has_boundary()) {
                 for_neighbors(pi, grid, inv_stencil, bg, [&](u32 j) {
                     const V3<R> r = sub(pi, xb[j]);
-                    const R d = std::sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
+                    const R d = sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
                     r_acc += mb[j] * kernel_W(d, l);
                     ++cb;
                 });
@@ -346,7 +399,7 @@ struct Solver {
 
     // apply_gravity_kernel (dfsph_kernels.cu:347-355): v <- v e^{-d dt} + g dt.
     void apply_external_forces(R dt) {
-        const R decay = std::exp(-R(cfg.damping) * dt);
+        const R decay = exp(-R(cfg.damping) * dt);
         const R g[3] = {R(cfg.gravity[0]), R(cfg.gravity[1]), R(cfg.gravity[2])};
         const long long n = (long long)x.size();
 #pragma omp parallel for schedule(static)
@@ -361,7 +414,7 @@ struct Solver {
     // particle reads the velocities as they were before this pass.
     void apply_xsph() {
         if (!(cfg.viscosity > 0.0f)) return;  // dfsph.cu:198
-        const R eps = R(cfg.viscosity);
+        const R eps = xsph;
         const std::vector<V3<R>> v0 = v;
         const long long n = (long long)x.size();
 #pragma omp parallel for schedule(dynamic, 256)
@@ -373,7 +426,7 @@ struct Solver {
             for_neighbors(pi, grid, inv_stencil, fg, [&](u32 j) {
                 if ((long long)j == i) return;
                 const V3<R> r = sub(pi, x[j]);
-                const R dist = std::sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
+                const R dist = sqrt(r.x * r.x + r.y * r.y + r.z * r.z);
                 const R W = kernel_W(dist, l);
                 const R rho_avg = R(0.5) * (rho_i + rho[j]);
                 const R c = eps * (mass / std::max(rho_avg, R(1e-9))) * W;
@@ -512,7 +565,7 @@ struct Solver {
 #pragma omp parallel for schedule(static)
         for (long long i = 0; i < n; ++i) {
             V3<R> vv = v[i];
-            const R sp = std::sqrt(vv.x * vv.x + vv.y * vv.y + vv.z * vv.z);
+            const R sp = sqrt(vv.x * vv.x + vv.y * vv.y + vv.z * vv.z);
             if (sp > max_vc) {
                 const R s = max_vc / sp;
                 vv.x *= s; vv.y *= s; vv.z *= s;
@@ -530,7 +583,7 @@ struct Solver {
         R m = 0;
         bool nan = false;
         for (long long i = 0; i < n; ++i) {
-            const R s = std::sqrt(v[i].x * v[i].x + v[i].y * v[i].y + v[i].z * v[i].z);
+            const R s = sqrt(v[i].x * v[i].x + v[i].y * v[i].y + v[i].z * v[i].z);
             if (s != s) nan = true;
             m = std::max(m, s);
         }
@@ -773,6 +826,43 @@ double oracle_scalar(void* p, int which) {
     };
     return h->s32 ? f(*h->s32) : f(*h->s64);
 }
+
+// Forward-mode (dual number) instance: the same FP64 step carrying the
+// derivative along the direction (dx, dv, d_xsph) of the initial positions,
+// velocities and XSPH coefficient. Checker of the GPU adjoint only.
+void* oracle_dual_create(const Config* cfg, const float* fluid_xyz, const float* fluid_v, u32 n,
+                         const float* boundary_xyz, u32 nb, const double* dx, const double* dv, double d_xsph) {
+    auto* s = new Solver<oracle::Dual>;
+    s->init(*cfg, fluid_xyz, fluid_v, n, boundary_xyz, nb);
+    for (u32 i = 0; i < n; ++i) {
+        if (dx) { s->x[i].x.d = dx[3 * i]; s->x[i].y.d = dx[3 * i + 1]; s->x[i].z.d = dx[3 * i + 2]; }
+        if (dv) { s->v[i].x.d = dv[3 * i]; s->v[i].y.d = dv[3 * i + 1]; s->v[i].z.d = dv[3 * i + 2]; }
+    }
+    s->xsph.d = d_xsph;
+    return s;
+}
+
+int oracle_dual_step(void* p, float dt, u32 n_steps) {
+    auto* s = static_cast<Solver<oracle::Dual>*>(p);
+    for (u32 k = 0; k < n_steps; ++k) s->step(oracle::Dual(double(dt)));
+    return 0;
+}
+
+// Values and derivatives of positions and velocities (double[3n] each; any may be NULL).
+int oracle_dual_get(void* p, double* x, double* v, double* dx, double* dv) {
+    auto* s = static_cast<Solver<oracle::Dual>*>(p);
+    for (std::size_t i = 0; i < s->x.size(); ++i) {
+        const oracle::V3<oracle::Dual>& a = s->x[i];
+        const oracle::V3<oracle::Dual>& b = s->v[i];
+        if (x) { x[3 * i] = a.x.v; x[3 * i + 1] = a.y.v; x[3 * i + 2] = a.z.v; }
+        if (dx) { dx[3 * i] = a.x.d; dx[3 * i + 1] = a.y.d; dx[3 * i + 2] = a.z.d; }
+        if (v) { v[3 * i] = b.x.v; v[3 * i + 1] = b.y.v; v[3 * i + 2] = b.z.v; }
+        if (dv) { dv[3 * i] = b.x.d; dv[3 * i + 1] = b.y.d; dv[3 * i + 2] = b.z.d; }
+    }
+    return 0;
+}
+
+void oracle_dual_destroy(void* p) { delete static_cast<Solver<oracle::Dual>*>(p); }
 
 void oracle_set_threads(int n) {
 #ifdef _OPENMP

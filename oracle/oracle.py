@@ -66,6 +66,12 @@ def load():
         L.oracle_get.argtypes = [P, ctypes.c_int, P]
         L.oracle_scalar.restype = ctypes.c_double
         L.oracle_scalar.argtypes = [P, ctypes.c_int]
+        L.oracle_dual_create.restype = P
+        L.oracle_dual_create.argtypes = [ctypes.POINTER(OracleConfig), P, P, ctypes.c_uint32, P, ctypes.c_uint32,
+                                         P, P, ctypes.c_double]
+        L.oracle_dual_step.argtypes = [P, ctypes.c_float, ctypes.c_uint32]
+        L.oracle_dual_get.argtypes = [P, P, P, P, P]
+        L.oracle_dual_destroy.argtypes = [P]
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         L.oracle_max_threads.restype = ctypes.c_int
         _lib = L
@@ -205,3 +211,46 @@ class Oracle:
 
     def last_density_iters(self):
         return int(self.scalar(2))
+
+
+class DualOracle:
+    """The FP64 oracle step in forward mode: values plus the exact derivative
+    along one direction (dx, dv) of the initial state and d_xsph of the XSPH
+    coefficient, every branch and neighbour set decided by the values. The
+    checker of the GPU adjoint: <gradient, direction> = d(loss) along it."""
+
+    def __init__(self, cfg: OracleConfig, fluid, vel, boundary, dx=None, dv=None, d_xsph=0.0, threads=0):
+        L = load()
+        if threads:
+            L.oracle_set_threads(threads)
+        self._L = L
+        self.fluid = np.ascontiguousarray(fluid, np.float32).reshape(-1, 3)
+        self.n = self.fluid.shape[0]
+        vel = np.ascontiguousarray(vel, np.float32).reshape(-1, 3)
+        b = np.ascontiguousarray(boundary, np.float32).reshape(-1, 3)
+        dxa = None if dx is None else np.ascontiguousarray(dx, np.float64).reshape(-1, 3)
+        dva = None if dv is None else np.ascontiguousarray(dv, np.float64).reshape(-1, 3)
+        ptr = lambda a: None if a is None else a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        self._keep = (vel, b, dxa, dva)
+        self._h = L.oracle_dual_create(ctypes.byref(cfg), ptr(self.fluid), ptr(vel), self.n, ptr(b), b.shape[0],
+                                       ptr(dxa), ptr(dva), float(d_xsph))
+
+    def step(self, dt, n=1):
+        self._L.oracle_dual_step(self._h, ctypes.c_float(dt), n)
+
+    def state(self):
+        """(x, v, dx, dv) as (n, 3) float64 arrays."""
+        out = [np.empty((self.n, 3), np.float64) for _ in range(4)]
+        self._L.oracle_dual_get(self._h, *(a.ctypes.data_as(ctypes.c_void_p) for a in out))
+        return tuple(out)
+
+    def close(self):
+        if self._h:
+            self._L.oracle_dual_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -68,9 +68,10 @@ KERNEL_FORCES_XSPH = 7
 KERNEL_ADVECT = 8
 KERNEL_IO = 9
 KERNEL_OTHER = 10
-KERNEL_CLASSES = 11
+KERNEL_ADJOINT = 11
+KERNEL_CLASSES = 12
 KERNEL_NAMES = ["grid_count", "grid_scan", "grid_scatter", "grid_reorder", "density_alpha", "pressure_rate",
-                "pressure_apply", "forces_xsph", "advect", "io", "other"]
+                "pressure_apply", "forces_xsph", "advect", "io", "other", "adjoint"]
 
 
 class DfsphConfig(ctypes.Structure):
@@ -120,6 +121,10 @@ _SIGNATURES = [
     ("dfsph_profile_enable", ctypes.c_int, [_P, ctypes.c_uint32]),
     ("dfsph_profile_read", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_uint64)]),
+    ("dfsph_adjoint_set_state", ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, ctypes.c_int]),
+    ("dfsph_adjoint_get_state", ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
+    ("dfsph_adjoint_forward", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_uint32, ctypes.c_uint32]),
+    ("dfsph_adjoint_backward", ctypes.c_int, [_P, _P, _P, _P, _P, ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
     ("dfsph_last_error", ctypes.c_char_p, [_P]),
     ("dfsph_status_string", ctypes.c_char_p, [ctypes.c_int]),
     ("dfsph_sample_aabb_boundary", ctypes.c_int64,

@@ -263,6 +263,43 @@ int dfsph_synchronize(dfsph_ctx* ctx) {
     });
 }
 
+int dfsph_adjoint_set_state(dfsph_ctx* ctx, const void* pos, const void* vel, uint32_t n, int mem) {
+    if (!ctx || (n > 0 && !pos)) return DFSPH_ERR_INVALID_ARGUMENT;
+    if (mem != DFSPH_MEM_HOST && mem != DFSPH_MEM_DEVICE) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        ctx->solver->adjoint_set_state(pos, vel, n, mem);
+    });
+}
+
+int dfsph_adjoint_get_state(dfsph_ctx* ctx, void* pos, void* vel, int mem) {
+    if (!ctx) return DFSPH_ERR_INVALID_ARGUMENT;
+    if (mem != DFSPH_MEM_HOST && mem != DFSPH_MEM_DEVICE) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        ctx->solver->adjoint_get_state(pos, vel, mem);
+    });
+}
+
+int dfsph_adjoint_forward(dfsph_ctx* ctx, float dt, uint32_t n_steps, uint32_t checkpoint_every) {
+    if (!ctx || !(dt > 0.0f) || dt > 1.0e30f || n_steps == 0 || checkpoint_every == 0)
+        return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        ctx->solver->adjoint_forward(dt, n_steps, checkpoint_every);
+    });
+}
+
+int dfsph_adjoint_backward(dfsph_ctx* ctx, const void* pos_bar, const void* vel_bar, void* pos0_bar,
+                           void* vel0_bar, double* xsph_bar, int mem) {
+    if (!ctx) return DFSPH_ERR_INVALID_ARGUMENT;
+    if (mem != DFSPH_MEM_HOST && mem != DFSPH_MEM_DEVICE) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        ctx->solver->adjoint_backward(pos_bar, vel_bar, pos0_bar, vel0_bar, xsph_bar, mem);
+    });
+}
+
 const char* dfsph_last_error(const dfsph_ctx* ctx) {
     if (!ctx) return g_create_error.c_str();
     return ctx->last_error.c_str();

@@ -484,6 +484,15 @@ __device__ __forceinline__ bool boundary_near(const Centre& c, const GridDev<R>&
     return __ldg(mask + cell) != 0;
 }
 
+// Per-step records written by the forward kernels when the adjoint replays a
+// segment (null pointers otherwise): positions with rho, (G, den) of alpha and
+// the slot -> original index map of the step's sorted order.
+template <class R> struct Tape1 {
+    R4<R>* x;
+    R4<R>* g;
+    u32* id;
+};
+
 struct BoundaryDev {
     const void* xb;             // R4<R>*, (x, y, z, m_b), sorted
     const u32* bcs;             // boundary cell_start
@@ -501,7 +510,7 @@ template <class R, bool KAHAN, bool DIAG>
 __global__ void __launch_bounds__(128) density_alpha_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, R* __restrict__ alpha,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, u32* __restrict__ nbr_f,
-    u32* __restrict__ nbr_b) {
+    u32* __restrict__ nbr_b, const u32* __restrict__ id, Tape1<R> tp) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R4<R> pi = ld(xk + i);
@@ -569,6 +578,11 @@ __global__ void __launch_bounds__(128) density_alpha_kernel(
     vr[i] = v;
     alpha[i] = denom > R(1e-9) ? rho / denom : R(0);
     if (DIAG) { nbr_f[i] = cf; nbr_b[i] = cb; }
+    if (tp.x) {
+        tp.x[i] = {pi.x, pi.y, pi.z, rho};
+        tp.g[i] = {gx, gy, gz, denom};
+        tp.id[i] = id[i];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -581,10 +595,11 @@ template <class R>
 __global__ void __launch_bounds__(128) forces_xsph_kernel(
     int n, const R4<R>* __restrict__ xk, const R4<R>* __restrict__ vr_in, R4<R>* __restrict__ vr_out,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, R decay, R gdx, R gdy, R gdz, R eps,
-    const R* __restrict__ eps_scene, int do_xsph) {
+    const R* __restrict__ eps_scene, int do_xsph, R4<R>* __restrict__ tape_v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R4<R> vi = ld(vr_in + i);
+    if (tape_v) tape_v[i] = vi;
     R dx = 0, dy = 0, dz = 0;
     if (do_xsph) {
         const R4<R> pi = ld(xk + i);
@@ -625,7 +640,7 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
     const R4<R>* __restrict__ vr, const R* __restrict__ alpha, R* __restrict__ rho_adv,
     R* __restrict__ kap, const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd,
     R dt, double* __restrict__ partials, IterCtl* ctl, u32 iter, u32 first_check, double inv_n,
-    double threshold) {
+    double threshold, R4<R>* __restrict__ tape_v) {
     __shared__ double sh[4];
     if (stopped_before(ctl, iter)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -633,6 +648,7 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
     if (i < n) {
         const R4<R> pi = ld(xk_in + i);
         const R4<R> vi = ld(vr + i);
+        if (tape_v) tape_v[i] = vi;
         const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
         R rd = 0;
         for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
@@ -742,27 +758,34 @@ template <class R, bool COUNT>
 __global__ void __launch_bounds__(256) advect_kernel(
     int n, R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, R dt, R lox, R loy, R loz, R hix,
     R hiy, R hiz, GridDev<R> g, u32* __restrict__ key, u32* __restrict__ rank,
-    u32* __restrict__ count, IterCtl* ctl, u32* __restrict__ maxv_scene) {
+    u32* __restrict__ count, IterCtl* ctl, u32* __restrict__ maxv_scene, R4<R>* __restrict__ tape_v,
+    unsigned char* __restrict__ tape_mask) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     u32 vbits = 0;
     u32 scene = 0xffffffffu;  // lanes past the end form their own group
     if (i < n) {
         R4<R> v = vr[i];
         R4<R> x = xk[i];
+        if (tape_v) tape_v[i] = v;
+        // mask bits (recorded for the adjoint): 0-2 position clamped on x/y/z,
+        // 3-5 velocity component zeroed, 6 speed clamped
+        u32 mk = 0;
         const R maxv = R(5);
         const R sp = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
         if (sp > maxv) {
             const R s = maxv / sp;
             v.x *= s; v.y *= s; v.z *= s;
+            mk |= 64u;
         }
         R px = x.x + v.x * dt, py = x.y + v.y * dt, pz = x.z + v.z * dt;
         const R eps = R(1e-3);
-        if (px < lox + eps) { px = lox + eps; if (v.x < R(0)) v.x = R(0); }
-        if (py < loy + eps) { py = loy + eps; if (v.y < R(0)) v.y = R(0); }
-        if (pz < loz + eps) { pz = loz + eps; if (v.z < R(0)) v.z = R(0); }
-        if (px > hix - eps) { px = hix - eps; if (v.x > R(0)) v.x = R(0); }
-        if (py > hiy - eps) { py = hiy - eps; if (v.y > R(0)) v.y = R(0); }
-        if (pz > hiz - eps) { pz = hiz - eps; if (v.z > R(0)) v.z = R(0); }
+        if (px < lox + eps) { px = lox + eps; mk |= 1u; if (v.x < R(0)) { v.x = R(0); mk |= 8u; } }
+        if (py < loy + eps) { py = loy + eps; mk |= 2u; if (v.y < R(0)) { v.y = R(0); mk |= 16u; } }
+        if (pz < loz + eps) { pz = loz + eps; mk |= 4u; if (v.z < R(0)) { v.z = R(0); mk |= 32u; } }
+        if (px > hix - eps) { px = hix - eps; mk |= 1u; if (v.x > R(0)) { v.x = R(0); mk |= 8u; } }
+        if (py > hiy - eps) { py = hiy - eps; mk |= 2u; if (v.y > R(0)) { v.y = R(0); mk |= 16u; } }
+        if (pz > hiz - eps) { pz = hiz - eps; mk |= 4u; if (v.z > R(0)) { v.z = R(0); mk |= 32u; } }
+        if (tape_mask) tape_mask[i] = static_cast<unsigned char>(mk);
         vr[i] = {v.x, v.y, v.z, v.w};
         xk[i] = {px, py, pz, R(0)};
         const float mag = float(sqrt(v.x * v.x + v.y * v.y + v.z * v.z));

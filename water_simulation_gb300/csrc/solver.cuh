@@ -15,6 +15,7 @@
 #include <string>
 #include <vector>
 
+#include "adjoint.cuh"
 #include "kernels.cuh"
 #include "solver_api.h"
 
@@ -136,6 +137,7 @@ public:
         drop_graph();
         if (capture_stream_) cudaStreamDestroy(capture_stream_);
         if (host_ctl_) cudaFreeHost(host_ctl_);
+        if (eps_host_) cudaFreeHost(eps_host_);
         for (const Record& r : records_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
         for (cudaEvent_t e : free_events_) cudaEventDestroy(e);
     }
@@ -151,6 +153,7 @@ public:
         nb_ = n;
         drop_pending_counts();
         drop_graph();
+        ad_valid_ = false;  // a recorded rollout ran against the old walls
         if (n == 0) {
             DFSPH_CUDA(cudaMemsetAsync(bcs_.p, 0, (size_t(cells1_) + 1) * sizeof(u32), stream_));
             return;
@@ -401,7 +404,254 @@ public:
         *count = c;
     }
 
+    // ------------------------------------------------------------- adjoint
+    void adjoint_set_state(const void* pos, const void* vel, u32 n, int mem) override {
+        if (scenes_ != 1) throw Error(DFSPH_ERR_STATE, "the adjoint steps one scene");
+        if (n > cap_) throw Error(DFSPH_ERR_OUT_OF_RANGE, "count " + std::to_string(n) + " exceeds capacity");
+        const R* p = static_cast<const R*>(pos);
+        const R* v = static_cast<const R*>(vel);
+        if (mem == DFSPH_MEM_HOST && n) {
+            R* st = static_cast<R*>(ad_staging(size_t(n) * 6 * sizeof(R)));
+            DFSPH_CUDA(cudaMemcpyAsync(st, p, size_t(n) * 3 * sizeof(R), cudaMemcpyHostToDevice, stream_));
+            if (v)
+                DFSPH_CUDA(cudaMemcpyAsync(st + 3 * size_t(n), v, size_t(n) * 3 * sizeof(R), cudaMemcpyHostToDevice,
+                                           stream_));
+            DFSPH_CUDA(cudaStreamSynchronize(stream_));
+            p = st;
+            v = v ? st + 3 * size_t(n) : nullptr;
+        }
+        n_ = n;
+        drop_pending_counts();
+        drop_graph();
+        ad_valid_ = false;
+        if (n == 0) return;
+        ensure_adjoint_buffers();
+        const int nb = blocks_for(n, 256);
+        launch(DFSPH_KERNEL_IO, pack3_kernel<R>, nb, 256, int(n), p, xg_.p);
+        launch(DFSPH_KERNEL_IO, pack3_kernel<R>, nb, 256, int(n), v, vg_.p);
+        launch(DFSPH_KERNEL_IO, load_state_kernel<R>, nb, 256, int(n), (const V4*)xg_.p, (const V4*)vg_.p,
+               xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
+        counts_valid_ = false;
+        have_state_ = true;
+    }
+
+    void adjoint_get_state(void* pos, void* vel, int mem) override {
+        const size_t n = n_;
+        if (n == 0) return;
+        const size_t bytes = 3 * n * sizeof(R);
+        void* outs[2] = {pos, vel};
+        for (int k = 0; k < 2; ++k) {
+            if (!outs[k]) continue;
+            void* out = mem == DFSPH_MEM_DEVICE ? outs[k] : scratch_bytes(bytes);
+            launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, R>, blocks_for(n, 256), 256, int(n), id_[ci_].p,
+                   k == 0 ? (const V4*)xk_[cx_].p : (const V4*)vr_[cv_].p, -1, (R*)out);
+            if (mem != DFSPH_MEM_DEVICE) {
+                DFSPH_CUDA(cudaMemcpyAsync(outs[k], out, bytes, cudaMemcpyDeviceToHost, stream_));
+                DFSPH_CUDA(cudaStreamSynchronize(stream_));
+            }
+        }
+    }
+
+    void adjoint_forward(float dt, u32 n_steps, u32 every) override {
+        check_adjoint_config();
+        if (!have_state_ || n_ == 0) throw Error(DFSPH_ERR_STATE, "no fluid state: set one first");
+        ad_valid_ = false;
+        const u32 segs = (n_steps + every - 1) / every;
+        const size_t need = (size_t(segs) + 1) * 2 * size_t(n_);
+        if (ck_.n < need) ck_.alloc(need);
+        for (u32 s = 0; s < segs; ++s) {
+            save_checkpoint(s);
+            step(dt, std::min(every, n_steps - s * every));
+        }
+        save_checkpoint(segs);
+        ad_n_ = n_;
+        ad_steps_ = n_steps;
+        ad_every_ = every;
+        ad_dt_ = dt;
+        ad_eps_ = cfg_.viscosity;
+        ad_valid_ = true;
+    }
+
+    void adjoint_backward(const void* xbar, const void* vbar, void* x0bar, void* v0bar, double* eps_bar,
+                          int mem) override {
+        if (!ad_valid_ || n_ != ad_n_) throw Error(DFSPH_ERR_STATE, "no recorded rollout: call dfsph_adjoint_forward");
+        if (cfg_.viscosity != ad_eps_) throw Error(DFSPH_ERR_STATE, "the XSPH coefficient changed since the rollout");
+        check_adjoint_config();
+        if (!xbar) throw Error(DFSPH_ERR_INVALID_ARGUMENT, "pos_bar is required");
+        const u32 n = n_;
+        ensure_adjoint_buffers();
+        const R* xb = static_cast<const R*>(xbar);
+        const R* vb = static_cast<const R*>(vbar);
+        if (mem == DFSPH_MEM_HOST) {
+            R* st = static_cast<R*>(ad_staging(size_t(n) * 6 * sizeof(R)));
+            DFSPH_CUDA(cudaMemcpyAsync(st, xb, size_t(n) * 3 * sizeof(R), cudaMemcpyHostToDevice, stream_));
+            if (vb)
+                DFSPH_CUDA(cudaMemcpyAsync(st + 3 * size_t(n), vb, size_t(n) * 3 * sizeof(R), cudaMemcpyHostToDevice,
+                                           stream_));
+            DFSPH_CUDA(cudaStreamSynchronize(stream_));
+            xb = st;
+            vb = vb ? st + 3 * size_t(n) : nullptr;
+        }
+        const int nb = blocks_for(n, 256);
+        launch(DFSPH_KERNEL_IO, pack3_kernel<R>, nb, 256, int(n), xb, xg_.p);
+        launch(DFSPH_KERNEL_IO, pack3_kernel<R>, nb, 256, int(n), vb, vg_.p);
+        DFSPH_CUDA(cudaMemsetAsync(eps_acc_.p, 0, sizeof(double), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(eps_ctr_.p, 0, sizeof(u32), stream_));
+        const u32 segs = (ad_steps_ + ad_every_ - 1) / ad_every_;
+        ensure_tape(std::min(ad_every_, ad_steps_));
+        drop_graph();
+        for (u32 s = segs; s-- > 0;) {
+            const u32 s0 = s * ad_every_;
+            const u32 cnt = std::min(ad_every_, ad_steps_ - s0);
+            restore_checkpoint(s);
+            for (u32 k = 0; k < cnt; ++k) {
+                const StepTape<R> t = tape_at(k);
+                step_once(R(ad_dt_), true, &t);
+            }
+            for (u32 k = cnt; k-- > 0;) backward_step(tape_at(k));
+        }
+        const size_t bytes = 3 * size_t(n) * sizeof(R);
+        void* outs[2] = {x0bar, v0bar};
+        for (int k = 0; k < 2; ++k) {
+            if (!outs[k]) continue;
+            void* out = mem == DFSPH_MEM_DEVICE ? outs[k] : scratch_bytes(bytes);
+            launch(DFSPH_KERNEL_IO, unpack3_kernel<R>, nb, 256, int(n), k == 0 ? (const V4*)xg_.p : (const V4*)vg_.p,
+                   (R*)out);
+            if (mem != DFSPH_MEM_DEVICE) {
+                DFSPH_CUDA(cudaMemcpyAsync(outs[k], out, bytes, cudaMemcpyDeviceToHost, stream_));
+                DFSPH_CUDA(cudaStreamSynchronize(stream_));
+            }
+        }
+        if (eps_bar) {
+            DFSPH_CUDA(cudaMemcpyAsync(eps_host_, eps_acc_.p, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+            DFSPH_CUDA(cudaStreamSynchronize(stream_));
+            *eps_bar = *eps_host_;
+        }
+        restore_checkpoint(segs);
+    }
+
 private:
+    void check_adjoint_config() const {
+        if (scenes_ != 1) throw Error(DFSPH_ERR_STATE, "the adjoint steps one scene");
+        if ((cfg_.max_density_iters > 0 && cfg_.eta_density > 0.0f) ||
+            (cfg_.max_divergence_iters > 0 && cfg_.eta_divergence > 0.0f))
+            throw Error(DFSPH_ERR_STATE, "the adjoint needs fixed iteration counts (eta_density = eta_divergence = 0)");
+    }
+
+    void* ad_staging(size_t bytes) {
+        if (ad_staging_.n < bytes) ad_staging_.alloc(bytes);
+        return ad_staging_.p;
+    }
+
+    void ensure_adjoint_buffers() {
+        if (xg_.n >= cap_ && cap_) return;
+        const size_t c = std::max(cap_, 1u);
+        xg_.alloc(c); vg_.alloc(c); xbar_.alloc(c); vbar_[0].alloc(c); vbar_[1].alloc(c);
+        xr_.alloc(c); xq_.alloc(c); gq_.alloc(c);
+        rhobar_.alloc(c); alphabar_.alloc(c);
+        eps_part_.alloc((c + 127) / 128);
+        eps_ctr_.alloc(1);
+        eps_acc_.alloc(1);
+        if (!eps_host_) DFSPH_CUDA(cudaMallocHost(reinterpret_cast<void**>(&eps_host_), sizeof(double)));
+    }
+
+    void save_checkpoint(u32 slot) {
+        const size_t n = n_;
+        V4* base = ck_.p + size_t(slot) * 2 * n;
+        launch(DFSPH_KERNEL_IO, save_state_kernel<R>, blocks_for(n, 256), 256, int(n), id_[ci_].p, xk_[cx_].p,
+               vr_[cv_].p, base, base + n);
+    }
+
+    void restore_checkpoint(u32 slot) {
+        const size_t n = n_;
+        const V4* base = ck_.p + size_t(slot) * 2 * n;
+        drop_pending_counts();
+        launch(DFSPH_KERNEL_IO, load_state_kernel<R>, blocks_for(n, 256), 256, int(n), base, base + n, xk_[cx_].p,
+               vr_[cv_].p, id_[ci_].p);
+        counts_valid_ = false;
+    }
+
+    // Per-step record layout: 256-byte aligned arrays of stride np slots.
+    static size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+    size_t tape_stride() const { return (size_t(n_) + 63) & ~size_t(63); }
+    size_t tape_step_bytes() const {
+        const size_t np = tape_stride();
+        const size_t kd = cfg_.max_divergence_iters, kr = cfg_.max_density_iters;
+        return align256(np * sizeof(V4)) * (4 + 2 * (kd + kr)) + align256(np * sizeof(R)) * 2 * (kd + kr) +
+               align256(np * sizeof(u32)) + align256(np) + align256((keys_ + 1) * sizeof(u32));
+    }
+    void ensure_tape(u32 steps) {
+        const size_t need = tape_step_bytes() * steps;
+        if (tape_.n < need) tape_.alloc(need);
+    }
+    StepTape<R> tape_at(u32 k) {
+        const size_t np = tape_stride();
+        const size_t kd = cfg_.max_divergence_iters, kr = cfg_.max_density_iters;
+        unsigned char* q = tape_.p + tape_step_bytes() * k;
+        auto take = [&](size_t bytes) {
+            unsigned char* r = q;
+            q += align256(bytes);
+            return r;
+        };
+        StepTape<R> t;
+        t.stride = np;
+        t.x = reinterpret_cast<V4*>(take(np * sizeof(V4)));
+        t.g = reinterpret_cast<V4*>(take(np * sizeof(V4)));
+        t.vx = reinterpret_cast<V4*>(take(np * sizeof(V4)));
+        t.va = reinterpret_cast<V4*>(take(np * sizeof(V4)));
+        const size_t its[2] = {kd, kr};
+        for (int w = 0; w < 2; ++w) {
+            t.xkf[w] = reinterpret_cast<V4*>(q); for (size_t i = 0; i < its[w]; ++i) take(np * sizeof(V4));
+            t.v[w] = reinterpret_cast<V4*>(q); for (size_t i = 0; i < its[w]; ++i) take(np * sizeof(V4));
+            t.kap[w] = reinterpret_cast<R*>(q); for (size_t i = 0; i < its[w]; ++i) take(np * sizeof(R));
+            t.adv[w] = reinterpret_cast<R*>(q); for (size_t i = 0; i < its[w]; ++i) take(np * sizeof(R));
+        }
+        t.id = reinterpret_cast<u32*>(take(np * sizeof(u32)));
+        t.amask = take(np);
+        t.cs = reinterpret_cast<u32*>(take((keys_ + 1) * sizeof(u32)));
+        return t;
+    }
+
+    // Reverse of step_once for one recorded step: the adjoint of the step's
+    // output state (xg_, vg_ in original order) becomes that of its input.
+    void backward_step(const StepTape<R>& t) {
+        const int n = int(n_);
+        const int b128 = blocks_for(n, 128), b256 = blocks_for(n, 256);
+        const R dt = R(ad_dt_);
+        const BoundaryDev bd = bdev();
+        const size_t st = t.stride;
+        int cur = 0;
+        launch(DFSPH_KERNEL_ADJOINT, adjoint_advect_kernel<R>, b256, 256, n, (const u32*)t.id, (const V4*)t.va,
+               (const unsigned char*)t.amask, dt, (const V4*)xg_.p, (const V4*)vg_.p, xbar_.p, vbar_[cur].p,
+               rhobar_.p, alphabar_.p);
+        for (u32 it = cfg_.max_density_iters; it-- > 0;) {
+            launch(DFSPH_KERNEL_ADJOINT, adjoint_apply_kernel<R, false>, b128, 128, n, (const V4*)(t.xkf[1] + it * st),
+                   (const V4*)t.x, (const V4*)t.g, (const R*)(t.kap[1] + it * st), (const R*)(t.adv[1] + it * st),
+                   (const V4*)vbar_[cur].p, (const u32*)t.cs, g_, phys_, bd, dt, xbar_.p, rhobar_.p, alphabar_.p,
+                   xr_.p);
+            launch(DFSPH_KERNEL_ADJOINT, adjoint_rate_kernel<R>, b128, 128, n, (const V4*)xr_.p,
+                   (const V4*)(t.v[1] + it * st), (const u32*)t.cs, g_, phys_, bd, vbar_[cur].p, xbar_.p);
+        }
+        const R decay = std::exp(-R(cfg_.damping) * dt);
+        launch(DFSPH_KERNEL_ADJOINT, adjoint_xsph_kernel<R>, b128, 128, n, (const V4*)t.x, (const V4*)t.vx,
+               (const V4*)vbar_[cur].p, vbar_[cur ^ 1].p, (const u32*)t.cs, g_, phys_, decay, R(ad_eps_), xbar_.p,
+               rhobar_.p, eps_part_.p, eps_ctr_.p, eps_acc_.p);
+        cur ^= 1;
+        for (u32 it = cfg_.max_divergence_iters; it-- > 0;) {
+            launch(DFSPH_KERNEL_ADJOINT, adjoint_apply_kernel<R, true>, b128, 128, n, (const V4*)(t.xkf[0] + it * st),
+                   (const V4*)t.x, (const V4*)t.g, (const R*)(t.kap[0] + it * st), (const R*)(t.adv[0] + it * st),
+                   (const V4*)vbar_[cur].p, (const u32*)t.cs, g_, phys_, bd, dt, xbar_.p, rhobar_.p, alphabar_.p,
+                   xr_.p);
+            launch(DFSPH_KERNEL_ADJOINT, adjoint_rate_kernel<R>, b128, 128, n, (const V4*)xr_.p,
+                   (const V4*)(t.v[0] + it * st), (const u32*)t.cs, g_, phys_, bd, vbar_[cur].p, xbar_.p);
+        }
+        launch(DFSPH_KERNEL_ADJOINT, adjoint_density_prep_kernel<R>, b256, 256, n, (const V4*)t.x, (const V4*)t.g,
+               (const R*)rhobar_.p, (const R*)alphabar_.p, xq_.p, gq_.p);
+        launch(DFSPH_KERNEL_ADJOINT, adjoint_density_kernel<R>, b128, 128, n, (const V4*)xq_.p, (const V4*)gq_.p,
+               (const V4*)vbar_[cur].p, (const V4*)xbar_.p, (const u32*)t.id, (const u32*)t.cs, g_, phys_, bd, xg_.p,
+               vg_.p);
+    }
+
     static constexpr u32 kSentinelCap = 4096;
 
     template <class K, class... A> void launch(int kclass, K kernel, int grid, int block, A... args) {
@@ -449,7 +699,9 @@ private:
         graph_ = nullptr;
     }
     void ensure_graph(float dt) {
-        if (graph_exec_ && graph_dt_ == dt) return;
+        // a replayed adjoint segment leaves the ping-pong parity where a plain
+        // step would not, so the graph is only reused at its capture parity
+        if (graph_exec_ && graph_dt_ == dt && cx_ == graph_cx_ && cv_ == graph_cv_ && ci_ == graph_ci_) return;
         drop_graph();
         const int cx = cx_, cv = cv_, ci = ci_;
         const bool counted = counts_valid_, stepped = stepped_;
@@ -482,6 +734,7 @@ private:
         if (cx_ != cx || cv_ != cv || ci_ != ci) throw Error(DFSPH_ERR_STATE, "graph capture changed buffer parity");
         DFSPH_CUDA(cudaGraphInstantiate(&graph_exec_, graph_, 0));
         graph_dt_ = dt;
+        graph_cx_ = cx_; graph_cv_ = cv_; graph_ci_ = ci_;
     }
 
     // The integrator leaves the next step's per-cell counts in count_; any new
@@ -569,24 +822,33 @@ private:
     // the kernels stop themselves once the mean error is below eta rho0; the
     // host additionally stops launching after the device reports convergence.
     template <bool DIV>
-    u32 solve(R dt, u32 max_iters, float eta, IterCtl* ctl, R* kap_out, R* adv_out) {
+    u32 solve(R dt, u32 max_iters, float eta, IterCtl* ctl, R* kap_out, R* adv_out, const u32* cs,
+              const StepTape<R>* tp) {
         const int n = int(n_);
         const bool adaptive = eta > 0.0f;
         const double thr = double(eta) * double(cfg_.rest_density);
         const u32 first_check = DIV ? 0u : 1u;  // density: from the 2nd iteration (dfsph.cu:255)
+        const int w = DIV ? 0 : 1;
         u32 launched = 0;
         for (u32 it = 0; it < max_iters; ++it) {
+            // a replayed segment keeps every iteration's (x, kf), kappa and
+            // rate in its tape; positions do not change within the step
+            V4* xin = xk_[cx_].p;
+            V4* xout = tp ? tp->xkf[w] + it * tp->stride : xk_[cx_ ^ 1].p;
+            R* kap_it = tp ? tp->kap[w] + it * tp->stride : kap_out;
+            R* adv_it = tp ? tp->adv[w] + it * tp->stride : adv_out;
+            V4* tv = tp ? tp->v[w] + it * tp->stride : nullptr;
             if (adaptive)
                 launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true>, blocks_for(n, 128), 128, n,
-                       xk_[cx_].p, xk_[cx_ ^ 1].p, vr_[cv_].p, alpha_.p, adv_out, kap_out, cell_start_.p, g_, phys_,
-                       bdev(), dt, partials_.p, ctl, it, first_check, 1.0 / double(n), thr);
+                       xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), dt, partials_.p, ctl,
+                       it, first_check, 1.0 / double(n), thr, tv);
             else
                 launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, false>, blocks_for(n, 128), 128, n,
-                       xk_[cx_].p, xk_[cx_ ^ 1].p, vr_[cv_].p, alpha_.p, adv_out, kap_out, cell_start_.p, g_, phys_,
-                       bdev(), dt, partials_.p, ctl, it, first_check, 1.0 / double(n), thr);
-            cx_ ^= 1;
-            launch(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p,
-                   vr_[cv_].p, kap_out, cell_start_.p, g_, phys_, bdev(), dt, ctl, it);
+                       xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), dt, partials_.p, ctl,
+                       it, first_check, 1.0 / double(n), thr, tv);
+            if (!tp) cx_ ^= 1;
+            launch(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R>, blocks_for(n, 128), 128, n, xout,
+                   vr_[cv_].p, kap_it, cs, g_, phys_, bdev(), dt, ctl, it);
             launched = it + 1;
             if (adaptive && it >= first_check) {
                 // The reference reads the error back every iteration
@@ -601,68 +863,73 @@ private:
         return launched;
     }
 
-    void step_once(R dt, bool count_next) {
+    void step_once(R dt, bool count_next, const StepTape<R>* tp = nullptr) {
         if (!have_state_) throw Error(DFSPH_ERR_STATE, "no fluid state: call dfsph_set_fluid first");
         const int n = int(n_);
         if (n == 0) return;  // dfsph.cu:121-122
         stepped_ = true;
+        u32* cs = tp ? tp->cs : cell_start_.p;
+        const Tape1<R> t1{tp ? tp->x : nullptr, tp ? tp->g : nullptr, tp ? tp->id : nullptr};
         // 1. grid build (CellGrid::build, core/src/cell_grid.cu:73-138)
         if (!counts_valid_)
             launch(DFSPH_KERNEL_GRID_COUNT, count_kernel<R>, blocks_for(n, 256), 256, n, xk_[cx_].p, g_, key_.p,
                    rank_.p, count_.p);
-        scan(cell_start_.p, keys_, /*step start*/ true);
-        launch(DFSPH_KERNEL_GRID_SCATTER, scatter_kernel, blocks_for(n, 256), 256, n, key_.p, rank_.p, cell_start_.p,
+        scan(cs, keys_, /*step start*/ true);
+        launch(DFSPH_KERNEL_GRID_SCATTER, scatter_kernel, blocks_for(n, 256), 256, n, key_.p, rank_.p, cs,
                id_[ci_].p, tmp_src_.p, tmp_id_.p);
         launch(DFSPH_KERNEL_GRID_REORDER, reorder_kernel<R>, blocks_for(n, 256), 256, n, tmp_src_.p, tmp_id_.p,
-               key_.p, cell_start_.p, cells1_, kSentinelCap, xk_[cx_].p, vr_[cv_].p, xk_[cx_ ^ 1].p, vr_[cv_ ^ 1].p,
+               key_.p, cs, cells1_, kSentinelCap, xk_[cx_].p, vr_[cv_].p, xk_[cx_ ^ 1].p, vr_[cv_ ^ 1].p,
                id_[ci_ ^ 1].p, key_sorted_.p, ctl_.p);
         cx_ ^= 1; cv_ ^= 1; ci_ ^= 1;
         counts_valid_ = false;
         // 2. density + alpha (dfsph.cu:137-186)
         const BoundaryDev bd = bdev();
         const bool kahan = cfg_.precision == DFSPH_PRECISION_FP32_KAHAN;
+        const u32* idn = id_[ci_].p;
         if (cfg_.record_diagnostics) {
             if (kahan)
                 launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, true>, blocks_for(n, 128), 128, n,
-                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cell_start_.p, g_, phys_, bd, nbr_f_.p, nbr_b_.p);
+                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, nbr_f_.p, nbr_b_.p, idn, t1);
             else
                 launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, true>, blocks_for(n, 128), 128, n,
-                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cell_start_.p, g_, phys_, bd, nbr_f_.p, nbr_b_.p);
+                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, nbr_f_.p, nbr_b_.p, idn, t1);
         } else {
             if (kahan)
                 launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, false>, blocks_for(n, 128), 128, n,
-                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cell_start_.p, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr);
+                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr, idn, t1);
             else
                 launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, false>, blocks_for(n, 128), 128, n,
-                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cell_start_.p, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr);
+                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr, idn, t1);
         }
         // 3. divergence solve (the reference's plan; 0 iterations = the reference)
         last_divergence_launched_ = 0;
         if (cfg_.max_divergence_iters > 0)
             last_divergence_launched_ = solve<true>(dt, cfg_.max_divergence_iters, cfg_.eta_divergence, ctl_.p + 1,
-                                                    kap_v_.p, rho_dot_.p);
+                                                    kap_v_.p, rho_dot_.p, cs, tp);
         // 4. gravity + damping + XSPH (dfsph.cu:188-213)
         const R decay = std::exp(-R(cfg_.damping) * dt);
         const bool xsph = explicit_eps_ ? any_xsph_ : cfg_.viscosity > 0.0f;
         launch(DFSPH_KERNEL_FORCES_XSPH, forces_xsph_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
-               vr_[cv_ ^ 1].p, cell_start_.p, g_, phys_, decay, R(cfg_.gravity[0]) * dt, R(cfg_.gravity[1]) * dt,
+               vr_[cv_ ^ 1].p, cs, g_, phys_, decay, R(cfg_.gravity[0]) * dt, R(cfg_.gravity[1]) * dt,
                R(cfg_.gravity[2]) * dt, R(cfg_.viscosity), scenes_ > 1 ? (const R*)eps_scene_.p : (const R*)nullptr,
-               xsph ? 1 : 0);
+               xsph ? 1 : 0, tp ? tp->vx : nullptr);
         cv_ ^= 1;
         // 5. density solve (dfsph.cu:215-260)
         last_density_launched_ =
-            solve<false>(dt, cfg_.max_density_iters, cfg_.eta_density, ctl_.p + 2, kap_.p, rho_adv_.p);
+            solve<false>(dt, cfg_.max_density_iters, cfg_.eta_density, ctl_.p + 2, kap_.p, rho_adv_.p, cs, tp);
         // 6. advect + max |v| (+ next step's cell counts)
         const R lo[3] = {R(cfg_.domain_min[0]), R(cfg_.domain_min[1]), R(cfg_.domain_min[2])};
         const R hi[3] = {R(cfg_.domain_max[0]), R(cfg_.domain_max[1]), R(cfg_.domain_max[2])};
         u32* mvs = scenes_ > 1 ? maxv_scene_.p : nullptr;
         if (count_next) {
             launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, true>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p,
-                   dt, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p, mvs);
+                   dt, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p, mvs,
+                   tp ? tp->va : nullptr, tp ? tp->amask : nullptr);
             counts_valid_ = true;
         } else {
             launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, false>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p,
-                   dt, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p, mvs);
+                   dt, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p, mvs,
+                   tp ? tp->va : nullptr, tp ? tp->amask : nullptr);
         }
     }
 
@@ -707,6 +974,19 @@ private:
     DevBuf<float> staging_;
     DevBuf<unsigned char> readback_;
     IterCtl* host_ctl_ = nullptr;
+    // differentiable rollout: checkpoints (x, v per slot, original order),
+    // per-step records of one segment, adjoint accumulators
+    bool ad_valid_ = false;
+    u32 ad_n_ = 0, ad_steps_ = 0, ad_every_ = 1;
+    float ad_dt_ = 0.0f, ad_eps_ = 0.0f;
+    DevBuf<V4> ck_;
+    DevBuf<unsigned char> tape_, ad_staging_;
+    DevBuf<V4> xg_, vg_, xbar_, vbar_[2], xr_, xq_, gq_;
+    DevBuf<R> rhobar_, alphabar_;
+    DevBuf<double> eps_part_, eps_acc_;
+    DevBuf<u32> eps_ctr_;
+    double* eps_host_ = nullptr;
+    int graph_cx_ = 0, graph_cv_ = 0, graph_ci_ = 0;
 };
 
 }  // namespace dfsph

@@ -33,6 +33,12 @@ struct SolverBase {
     virtual void synchronize() = 0;
     virtual void profile_enable(std::uint32_t mask) = 0;
     virtual void profile_read(int kclass, double* total_ms, unsigned long long* count) = 0;
+    // differentiable rollout; arrays hold the working type (float or double)
+    virtual void adjoint_set_state(const void* pos, const void* vel, std::uint32_t n, int mem) = 0;
+    virtual void adjoint_get_state(void* pos, void* vel, int mem) = 0;
+    virtual void adjoint_forward(float dt, std::uint32_t n_steps, std::uint32_t checkpoint_every) = 0;
+    virtual void adjoint_backward(const void* pos_bar, const void* vel_bar, void* pos0_bar, void* vel0_bar,
+                                  double* xsph_bar, int mem) = 0;
 };
 
 std::unique_ptr<SolverBase> make_solver_fp32(const dfsph_config& cfg, int device, cudaStream_t s);

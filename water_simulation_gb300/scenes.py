@@ -204,3 +204,35 @@ def falling_block(n_side=(12, 12, 12), seed: int = 7, radius: float = 0.01,
     b = sample_aabb_boundary(lo, hi, s, 3) if boundary else np.zeros((0, 3), np.float32)
     return Scene(f"block_{fluid.shape[0]}", r, lo, hi, fluid, vel, b, dt=1e-3, steps=50, viscosity=0.01,
                  max_density_iters=4, max_divergence_iters=0)
+
+
+def adjoint_drop(n_side: int = 32, seed: int = 11, velocity_sigma: float = 0.1) -> Scene:
+    """Differentiable drop: an n_side^3 block (32^3 = 32,768 particles, r = 0.01 m)
+    centred in x and z with its lower corner at y = 0.3 in the unit box, initial
+    velocities N(0, sigma^2) per component (seeded), dt = 1e-3 s, 200 steps,
+    fixed 2 divergence and 4 density iterations, XSPH 0.01. The loss target is
+    the initial block translated by (0.1, 0, 0) m (extra["target_shift"]);
+    checkpoints every 20 steps (extra["checkpoint_every"])."""
+    r = 0.01
+    s = 2 * r
+    lo = (0.5 - 0.5 * n_side * s, 0.3, 0.5 - 0.5 * n_side * s)
+    fluid = lattice_block(lo, (n_side, n_side, n_side), s, 0.05 * r, seed)
+    vel = normal(seed + 100, fluid.shape[0], velocity_sigma)
+    dlo, dhi = (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)
+    return Scene(f"adjoint_drop_{fluid.shape[0]}", r, dlo, dhi, fluid, vel, sample_aabb_boundary(dlo, dhi, s, 3),
+                 dt=1e-3, steps=200, viscosity=0.01, max_density_iters=4, max_divergence_iters=2,
+                 extra={"target_shift": (0.1, 0.0, 0.0), "checkpoint_every": 20})
+
+
+def adjoint_puddle(seed: int = 1, velocity_sigma: float = 0.1, steps: int = 40) -> Scene:
+    """The settled-puddle block (17^3 = 4913 particles at corner (0.3, 0.5, 0.3))
+    with N(0, sigma^2) initial velocities and the adjoint's fixed 2 divergence
+    and 4 density iterations: the finite-difference gradient check case."""
+    sc = puddle(seed)
+    sc.name = "adjoint_puddle_4913"
+    sc.velocity = normal(seed + 100, sc.n, velocity_sigma)
+    sc.steps = steps
+    sc.max_density_iters, sc.max_divergence_iters = 4, 2
+    sc.eta_density, sc.eta_divergence = 0.0, 0.0
+    sc.extra = {"target_shift": (0.1, 0.0, 0.0), "checkpoint_every": 20}
+    return sc

@@ -200,6 +200,69 @@ class Solver:
     def velocities(self) -> np.ndarray:
         return self.field(_lib.FIELD_VELOCITY)
 
+    # -- differentiable rollout (arrays of the working type) -----------------
+    @property
+    def real_dtype(self):
+        return np.float64 if self.config.precision == _lib.PRECISION_FP64 else np.float32
+
+    def adjoint_set_state(self, pos, vel=None) -> None:
+        """Host arrays (n, 3) of the working type, or device pointers (int) with n given by pos.shape."""
+        pos = np.ascontiguousarray(pos, dtype=self.real_dtype).reshape(-1, 3)
+        vp = None
+        if vel is not None:
+            vel = np.ascontiguousarray(vel, dtype=self.real_dtype).reshape(-1, 3)
+            vp = vel.ctypes.data_as(ctypes.c_void_p)
+        self._check(self._lib.dfsph_adjoint_set_state(self._ctx, pos.ctypes.data_as(ctypes.c_void_p), vp,
+                                                      pos.shape[0], _lib.MEM_HOST))
+        self.n = pos.shape[0]
+
+    def adjoint_set_state_device(self, pos_ptr: int, vel_ptr: int | None, n: int) -> None:
+        self._check(self._lib.dfsph_adjoint_set_state(self._ctx, ctypes.c_void_p(pos_ptr),
+                                                      ctypes.c_void_p(vel_ptr) if vel_ptr else None, n,
+                                                      _lib.MEM_DEVICE))
+        self.n = n
+
+    def adjoint_state(self):
+        """(positions, velocities) as (n, 3) host arrays of the working type."""
+        x = np.empty((self.n, 3), self.real_dtype)
+        v = np.empty((self.n, 3), self.real_dtype)
+        if self.n:
+            self._check(self._lib.dfsph_adjoint_get_state(self._ctx, x.ctypes.data_as(ctypes.c_void_p),
+                                                          v.ctypes.data_as(ctypes.c_void_p), _lib.MEM_HOST))
+        return x, v
+
+    def adjoint_state_device(self, pos_ptr: int, vel_ptr: int) -> None:
+        vp = lambda p: ctypes.c_void_p(p) if p else None  # noqa: E731
+        self._check(self._lib.dfsph_adjoint_get_state(self._ctx, vp(pos_ptr), vp(vel_ptr), _lib.MEM_DEVICE))
+
+    def adjoint_forward(self, dt: float, n_steps: int, checkpoint_every: int = 20) -> None:
+        self._check(self._lib.dfsph_adjoint_forward(self._ctx, ctypes.c_float(dt), n_steps, checkpoint_every))
+
+    def adjoint_backward(self, pos_bar, vel_bar=None):
+        """Host arrays in, (dL/dx0, dL/dv0, dL/d xsph) out."""
+        xb = np.ascontiguousarray(pos_bar, dtype=self.real_dtype).reshape(-1, 3)
+        vb = None if vel_bar is None else np.ascontiguousarray(vel_bar, dtype=self.real_dtype).reshape(-1, 3)
+        gx = np.empty_like(xb)
+        gv = np.empty_like(xb)
+        ge = ctypes.c_double()
+        self._check(self._lib.dfsph_adjoint_backward(
+            self._ctx, xb.ctypes.data_as(ctypes.c_void_p), None if vb is None else vb.ctypes.data_as(ctypes.c_void_p),
+            gx.ctypes.data_as(ctypes.c_void_p), gv.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ge),
+            _lib.MEM_HOST))
+        return gx, gv, ge.value
+
+    def adjoint_backward_device(self, pos_bar_ptr: int, vel_bar_ptr: int | None, pos0_bar_ptr: int,
+                                vel0_bar_ptr: int) -> float:
+        vp = lambda p: ctypes.c_void_p(p) if p else None  # noqa: E731
+        ge = ctypes.c_double()
+        self._check(self._lib.dfsph_adjoint_backward(self._ctx, vp(pos_bar_ptr), vp(vel_bar_ptr), vp(pos0_bar_ptr),
+                                                     vp(vel0_bar_ptr), ctypes.byref(ge), _lib.MEM_DEVICE))
+        return ge.value
+
+    def set_xsph(self, eps: float) -> None:
+        """XSPH coefficient of a one-scene context (DFSPHSolver::Config::viscosity)."""
+        self.set_scene_viscosity([eps])
+
 
 def solver_for(scene, precision: int = _lib.PRECISION_FP32, diagnostics: bool = False, device: int = 0,
                stream: int | None = None) -> Solver:
