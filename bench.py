@@ -21,6 +21,12 @@ roofline   the dominant kernel class, timed live with CUDA events during the
            wall particle), against the measured HBM copy bandwidth.
 cpu_baseline  the FP32 C++/OpenMP restatement of the reference step (oracle/)
            on all host cores, on a bounded sample of the same workload.
+batched    64 independent scenes in one context (one CUDA graph of two steps)
+           against 64 single-scene contexts stepped one after another.
+precision  FP32 and FP32 + Kahan density sums against the FP64 build of the
+           same kernels after 50 steps of the workload.
+adjoint    the differentiable drop (32,768 particles, 200 steps, checkpoint
+           every 20): backward time over forward time.
 ref_cuda   the reference's own CUDA kernels (compiled from its sources for
            sm_103a, oracle/_ref) under its restated host orchestration, timed on
            the same GPU in the same run.
@@ -44,10 +50,14 @@ sys.path.insert(0, ROOT)
 
 FALLBACK_HBM_GBS = 6800.0
 
-# DRAM bytes (read + write) per particle of one launch of each kernel class,
-# from `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum` on the 1M dam
-# break (profiles/dfsph_kernels_dam1m.md). None until captured.
-NCU_TRAFFIC_PER_PARTICLE: dict = {}
+# DRAM bytes (read + write) per fluid particle of one launch of each kernel
+# class, from `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum` on the
+# 1M dam break (profiles/dfsph_kernels_dam1m.md, one launch per kernel). The
+# traffic of a launch on another workload is scaled by its particle count.
+NCU_TRAFFIC_PER_PARTICLE: dict = {
+    "pressure_rate": 46.1, "pressure_apply": 40.2, "density_alpha": 25.0, "forces_xsph": 38.2,
+    "advect": 37.3, "grid_reorder": 52.7, "grid_scatter": 17.6, "grid_count": 20.7,
+}
 
 
 def parse():
@@ -62,6 +72,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched comparison")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-drop timing")
+    ap.add_argument("--no-precision", action="store_true", help="skip the FP32 vs FP64 field errors")
     return ap.parse_args()
 
 
@@ -330,6 +341,41 @@ def bench_batch(steps, n_scenes=64, warmup=3):
             "batched_ms_per_step": ms_batch / steps, "sequential_ms_per_step": ms_seq / steps}
 
 
+def bench_precision(sc, steps=50):
+    """Field error of the FP32 step (plain and with Kahan density sums; both
+    with FP64 convergence reductions) against the FP64 build of the same
+    kernels after `steps` steps from the same input."""
+    from water_simulation_gb300 import _lib
+    from water_simulation_gb300.solver import solver_for
+
+    out = {}
+    ref = None
+    for name, prec in (("fp64", _lib.PRECISION_FP64), ("fp32", _lib.PRECISION_FP32),
+                       ("fp32_kahan", _lib.PRECISION_FP32_KAHAN)):
+        s = solver_for(sc, precision=prec)
+        s.step(sc.dt, steps)
+        f = {"x": s.field(_lib.FIELD_POSITION).astype(np.float64), "v": s.field(_lib.FIELD_VELOCITY).astype(np.float64),
+             "rho": s.field(_lib.FIELD_DENSITY).astype(np.float64)}
+        s.close()
+        if ref is None:
+            ref = f
+            continue
+        vs = np.linalg.norm(ref["v"], axis=1).max()
+        rel = np.abs(f["rho"] - ref["rho"]) / np.abs(ref["rho"])
+        out[name] = {
+            "density_max_rel": float(rel.max()),
+            "density_rel_p50": float(np.percentile(rel, 50)),
+            "density_rel_p99": float(np.percentile(rel, 99)),
+            "density_frac_over_1e-4": float(np.mean(rel > 1e-4)),
+            "density_rms_rel": float(np.sqrt(np.mean(((f["rho"] - ref["rho"]) / ref["rho"]) ** 2))),
+            "position_max_abs_m": float(np.abs(f["x"] - ref["x"]).max()),
+            "velocity_max_abs_rel_to_max_speed": float(np.abs(f["v"] - ref["v"]).max() / max(vs, 1e-30)),
+        }
+    out["steps"] = steps
+    out["reference"] = "FP64 build of the same kernels"
+    return out
+
+
 def bench_adjoint(graph: bool):
     """Differentiable drop: 32,768 particles (32^3 block, r = 0.01 m), 200 steps
     at dt = 1e-3 s, fixed 2 divergence + 4 density iterations, checkpoint every
@@ -504,6 +550,8 @@ def main():
                      "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else "fallback",
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_ms,
                      "traffic": (traffic * sc.n) if traffic else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch on the 1M dam "
+                                       "break, scaled by particle count (profiles/dfsph_kernels_dam1m.md)",
                      "active_boundary_particles": res["nb_active"]},
         "kernel_share_warmup": res["warmup_share"],
     }
@@ -519,6 +567,11 @@ def main():
             line["batched"] = bench_batch(20)
         except Exception as e:
             line["batched"] = {"unavailable": str(e)[:200]}
+    if rank == 0 and not args.no_precision:
+        try:
+            line["precision"] = bench_precision(sc, 50)
+        except Exception as e:
+            line["precision"] = {"unavailable": str(e)[:200]}
     if rank == 0 and not args.no_adjoint:
         try:
             plain, graphed = bench_adjoint(False), bench_adjoint(True)
