@@ -25,6 +25,8 @@ batched    64 independent scenes in one context (one CUDA graph of two steps)
            against 64 single-scene contexts stepped one after another.
 precision  FP32 and FP32 + Kahan density sums against the FP64 build of the
            same kernels after 50 steps of the workload.
+frames     sim_cli's frame loop on the puddle block: substeps chosen on the
+           device inside one graph launch per frame, against the host loop.
 adjoint    the differentiable drop (32,768 particles, 200 steps, checkpoint
            every 20): backward time over forward time.
 ref_cuda   the reference's own CUDA kernels (compiled from its sources for
@@ -73,6 +75,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-scene batched comparison")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-drop timing")
     ap.add_argument("--no-precision", action="store_true", help="skip the FP32 vs FP64 field errors")
+    ap.add_argument("--no-frames", action="store_true", help="skip the device-stepped frame timing")
     return ap.parse_args()
 
 
@@ -341,6 +344,37 @@ def bench_batch(steps, n_scenes=64, warmup=3):
             "batched_ms_per_step": ms_batch / steps, "sequential_ms_per_step": ms_seq / steps}
 
 
+def bench_frames(n_frames=24):
+    """sim_cli's frame loop on the settled-puddle block (4,913 particles, fixed
+    4 density iterations): frames with the substep size chosen on the device
+    (one graph launch per frame) against the reference's host loop (max |v|
+    read back before every substep). Wall time of n_frames frames."""
+    from water_simulation_gb300 import scenes
+    from water_simulation_gb300.solver import Solver
+
+    sc = scenes.puddle()
+    sc.max_density_iters, sc.max_divergence_iters, sc.eta_density, sc.eta_divergence = 4, 0, 0.0, 0.0
+    out = {"workload": "puddle_4913 frames at 24 fps", "frames": n_frames}
+    for name, graph in (("device", True), ("host_loop", False)):
+        cfg = sc.config()
+        cfg.use_cuda_graph = 1 if graph else 0
+        s = Solver(cfg)
+        s.set_boundary(sc.boundary)
+        s.set_fluid(sc.fluid, sc.velocity)
+        s.step_frames(2)  # warm-up (and graph capture)
+        s.synchronize()
+        t0 = time.perf_counter()
+        subs = s.step_frames(n_frames)
+        s.synchronize()
+        t1 = time.perf_counter()
+        out[name] = {"ms_per_frame": 1e3 * (t1 - t0) / n_frames, "substeps": int(subs.sum()),
+                     "ms_per_substep": 1e3 * (t1 - t0) / max(int(subs.sum()), 1),
+                     "on_device": s.frames_on_device()}
+        s.close()
+    out["speedup"] = out["host_loop"]["ms_per_frame"] / out["device"]["ms_per_frame"]
+    return out
+
+
 def bench_precision(sc, steps=50):
     """Field error of the FP32 step (plain and with Kahan density sums; both
     with FP64 convergence reductions) against the FP64 build of the same
@@ -567,6 +601,11 @@ def main():
             line["batched"] = bench_batch(20)
         except Exception as e:
             line["batched"] = {"unavailable": str(e)[:200]}
+    if rank == 0 and not args.no_frames:
+        try:
+            line["frames"] = bench_frames()
+        except Exception as e:
+            line["frames"] = {"unavailable": str(e)[:200]}
     if rank == 0 and not args.no_precision:
         try:
             line["precision"] = bench_precision(sc, 50)

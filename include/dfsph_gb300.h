@@ -110,6 +110,8 @@ typedef struct dfsph_ctx dfsph_ctx;
 
 #define DFSPH_SCALAR_ACTIVE_BOUNDARY      12  /* boundary particles with a fluid particle within
                                                  2h of them (counted on demand, last grid) */
+#define DFSPH_SCALAR_FRAME_GRAPH          13  /* 1: the last dfsph_step_frames ran as device-stepped
+                                                 graphs; 0: as the host loop */
 
 /* Kernel classes for dfsph_profile_* (bit k of the mask selects class k). */
 #define DFSPH_KERNEL_GRID_COUNT       0   /* cell keys + per-cell counts          */
@@ -173,6 +175,32 @@ int dfsph_step(dfsph_ctx* ctx, float dt, uint32_t n_steps);
  * This is the entry the C++ façade's DFSPHSolver::step uses. */
 int dfsph_step_store(dfsph_ctx* ctx, float* pos, float* vel, uint32_t n, float dt,
                      float* density, float* alpha, float* kappa, float* density_adv);
+
+/* ---- CFL frames (no counterpart in the reference's library: sim_cli's loop,
+ * apps/sim_cli/main.cpp:171-181, with TimeStepper::next_dt,
+ * core/include/water/core/timestep.h:23-28) ------------------------------- */
+typedef struct dfsph_frame_config {
+    float    frame_dt;                /* length of one frame: sim_cli's 1 / scene fps      */
+    float    stepper_frame_dt;        /* TimeStepper::Config::frame_dt (1/24 s); the dt
+                                         floor is stepper_frame_dt / max_substeps        */
+    float    dt_max;                  /* TimeStepper::Config::dt_max (1/24 s)              */
+    float    cfl_lambda;              /* TimeStepper::Config::cfl_lambda (0.4)             */
+    uint32_t max_substeps;            /* TimeStepper::Config::max_substeps (16)            */
+    float    min_velocity;            /* sim_cli's floor on max |v| before next_dt (0.5)   */
+    uint32_t max_substeps_per_frame;  /* sim_cli's substep cap per frame (64)              */
+} dfsph_frame_config;
+
+/* sim_cli's values (above; frame_dt = 1/24 s). */
+int dfsph_frame_config_init(dfsph_frame_config* fc);
+
+/* n_frames frames: per frame, substeps of dt = next_dt(max(max|v|, min_velocity),
+ * particle_radius, remaining) until remaining <= 1e-6 or the cap, exactly
+ * sim_cli's loop. With use_cuda_graph = 1 and fixed iteration counts each frame
+ * is one graph launch whose substep size is chosen on the device after every
+ * substep (no host synchronisation inside a frame); otherwise the host runs
+ * the loop. substeps (host, n_frames entries, may be NULL) receives the
+ * substep count of each frame. Returns after the last frame. */
+int dfsph_step_frames(dfsph_ctx* ctx, const dfsph_frame_config* fc, uint32_t n_frames, uint32_t* substeps);
 
 /* Field readback (density_at/alpha_at/boundary_mass_at, dfsph.cu:330-353, as
  * whole arrays). dst_bytes is checked against the field's size. */

@@ -16,6 +16,7 @@
 #include "dfsph_gb300.h"
 #include "water/core/cell_grid.h"
 #include "water/core/particle_store.h"
+#include "water/core/timestep.h"
 #include "water/core/types.h"
 
 namespace water::solvers {
@@ -52,6 +53,10 @@ public:
         // never runs a divergence solve; it runs here only when enabled.
         bool enable_divergence_solver = false;
         u32 precision = DFSPH_PRECISION_FP32;
+        // step_frame runs a whole frame as one CUDA graph launch, with the
+        // substep size chosen on the device, when the iteration counts are
+        // fixed (eta = 0); otherwise it runs the host loop.
+        bool device_frames = true;
     };
 
     DFSPHSolver(ParticleStore& fluid, ParticleStore* boundary, Config cfg, cudaStream_t stream = 0)
@@ -72,6 +77,7 @@ public:
         c.domain_min[0] = cfg.domain_min.x; c.domain_min[1] = cfg.domain_min.y; c.domain_min[2] = cfg.domain_min.z;
         c.domain_max[0] = cfg.domain_max.x; c.domain_max[1] = cfg.domain_max.y; c.domain_max[2] = cfg.domain_max.z;
         c.precision = cfg.precision;
+        c.use_cuda_graph = cfg.device_frames ? 1u : 0u;
         c.capacity = static_cast<uint32_t>(fluid.capacity());
         c.boundary_capacity = boundary ? static_cast<uint32_t>(boundary->capacity()) : 0u;
         int dev = 0;
@@ -133,6 +139,47 @@ public:
                       ctx_.get(), "DFSPHSolver::step");
         grid_dirty_ = true;
         stats_dirty_ = true;
+    }
+
+    // One frame of CFL substeps on the caller's store: sim_cli's loop
+    // (apps/sim_cli/main.cpp:171-181) with TimeStepper::next_dt, each dt from
+    // max(max |v|, min_velocity); no counterpart in the reference's library.
+    // Returns the number of substeps taken.
+    u32 step_frame(const TimeStepper& ts, f32 frame_dt, f32 min_velocity = 0.5f, u32 max_substeps_per_frame = 64) {
+        const std::size_t n = fluid_.count();
+        const TimeStepper::Config tc = ts.config();
+        dfsph_frame_config fc;
+        dfsph_frame_config_init(&fc);
+        fc.frame_dt = frame_dt;
+        fc.stepper_frame_dt = tc.frame_dt;
+        fc.dt_max = tc.dt_max;
+        fc.cfl_lambda = tc.cfl_lambda;
+        fc.max_substeps = tc.max_substeps;
+        fc.min_velocity = min_velocity;
+        fc.max_substeps_per_frame = max_substeps_per_frame;
+        detail::check(dfsph_set_fluid(ctx_.get(), reinterpret_cast<const float*>(fluid_.positions()),
+                                      reinterpret_cast<const float*>(fluid_.velocities()), static_cast<uint32_t>(n),
+                                      DFSPH_MEM_DEVICE),
+                      ctx_.get(), "DFSPHSolver::step_frame");
+        uint32_t sub = 0;
+        detail::check(dfsph_step_frames(ctx_.get(), &fc, 1, &sub), ctx_.get(), "DFSPHSolver::step_frame");
+        if (n) {
+            const std::size_t v3 = n * sizeof(Vec3f), s1 = n * sizeof(f32);
+            const struct { int field; void* dst; std::size_t bytes; } outs[] = {
+                {DFSPH_FIELD_POSITION, fluid_.positions(), v3},
+                {DFSPH_FIELD_VELOCITY, fluid_.velocities(), v3},
+                {DFSPH_FIELD_DENSITY, fluid_.attribute_data(density_), s1},
+                {DFSPH_FIELD_ALPHA, fluid_.attribute_data(alpha_), s1},
+                {DFSPH_FIELD_KAPPA, fluid_.attribute_data(kappa_), s1},
+                {DFSPH_FIELD_DENSITY_ADV, fluid_.attribute_data(density_adv_), s1},
+            };
+            for (const auto& o : outs)
+                detail::check(dfsph_get_field(ctx_.get(), o.field, o.dst, o.bytes, DFSPH_MEM_DEVICE), ctx_.get(),
+                              "DFSPHSolver::step_frame");
+        }
+        grid_dirty_ = true;
+        stats_dirty_ = true;
+        return sub;
     }
 
     // Largest particle speed after the last step (0 before the first step).

@@ -49,6 +49,20 @@ def test_config_defaults_match_reference_config():
     assert list(c.domain_min) == [0, 0, 0] and list(c.domain_max) == [1, 1, 1]
 
 
+def test_frame_config_defaults_match_sim_cli():
+    # TimeStepper::Config (core/include/water/core/timestep.h:10-15) and
+    # sim_cli's 0.5 m/s floor and 64-substep cap (apps/sim_cli/main.cpp:172,175)
+    fc = _lib.DfsphFrameConfig()
+    assert _lib.load().dfsph_frame_config_init(ctypes.byref(fc)) == 0
+    assert fc.frame_dt == np.float32(1 / 24) and fc.stepper_frame_dt == np.float32(1 / 24)
+    assert fc.dt_max == np.float32(1 / 24) and fc.cfl_lambda == np.float32(0.4)
+    assert fc.max_substeps == 16 and fc.min_velocity == np.float32(0.5) and fc.max_substeps_per_frame == 64
+    lib = _lib.load()
+    assert lib.dfsph_step_frames(None, ctypes.byref(fc), 1, None) == _lib.ERR_INVALID_ARGUMENT
+    assert lib.dfsph_adjoint_forward(None, ctypes.c_float(1e-3), 1, 1) == _lib.ERR_INVALID_ARGUMENT
+    assert lib.dfsph_adjoint_backward(None, None, None, None, None, None, 0) == _lib.ERR_INVALID_ARGUMENT
+
+
 @pytest.mark.parametrize("r,dmax", [(0.01, (1, 1, 1)), (0.005, (1.6, 1.0, 0.6)), (0.0025, (1.6, 1.0, 0.6)),
                                     (0.0015, (1, 1, 1)), (0.012, (1, 1, 1))])
 def test_grid_geometry_matches_oracle(r, dmax):

@@ -56,6 +56,7 @@ SCALAR_BOUNDARY_COUNT = 9
 SCALAR_KERNEL_LAUNCHES = 10
 SCALAR_FLAGS = 11
 SCALAR_ACTIVE_BOUNDARY = 12
+SCALAR_FRAME_GRAPH = 13
 
 KERNEL_GRID_COUNT = 0
 KERNEL_GRID_SCAN = 1
@@ -100,6 +101,20 @@ class DfsphConfig(ctypes.Structure):
     ]
 
 
+class DfsphFrameConfig(ctypes.Structure):
+    """struct dfsph_frame_config (include/dfsph_gb300.h)."""
+
+    _fields_ = [
+        ("frame_dt", ctypes.c_float),
+        ("stepper_frame_dt", ctypes.c_float),
+        ("dt_max", ctypes.c_float),
+        ("cfl_lambda", ctypes.c_float),
+        ("max_substeps", ctypes.c_uint32),
+        ("min_velocity", ctypes.c_float),
+        ("max_substeps_per_frame", ctypes.c_uint32),
+    ]
+
+
 # (name, restype, argtypes) of every exported entry point
 _P = ctypes.c_void_p
 _F = ctypes.POINTER(ctypes.c_float)
@@ -121,6 +136,9 @@ _SIGNATURES = [
     ("dfsph_profile_enable", ctypes.c_int, [_P, ctypes.c_uint32]),
     ("dfsph_profile_read", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_uint64)]),
+    ("dfsph_frame_config_init", ctypes.c_int, [ctypes.POINTER(DfsphFrameConfig)]),
+    ("dfsph_step_frames", ctypes.c_int, [_P, ctypes.POINTER(DfsphFrameConfig), ctypes.c_uint32,
+                                         ctypes.POINTER(ctypes.c_uint32)]),
     ("dfsph_adjoint_set_state", ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, ctypes.c_int]),
     ("dfsph_adjoint_get_state", ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
     ("dfsph_adjoint_forward", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_uint32, ctypes.c_uint32]),

@@ -3,7 +3,13 @@
 // per frame (CFL TimeStepper) -> optional binary frame files.
 //
 //   sim_cli --scene PATH [--frames START:END] [--record] [--out DIR]
-//           [--no-vulkan] [--damping F] [--viscosity F]
+//           [--no-vulkan] [--damping F] [--viscosity F] [--fixed-iters N]
+//           [--host-substeps]
+//
+// By default each frame is one DFSPHSolver::step_frame: with fixed iteration
+// counts (--fixed-iters N: N density iterations, eta = 0) the whole frame is
+// one CUDA graph launch whose substep size is chosen on the device;
+// --host-substeps runs the reference's host loop of next_dt + step instead.
 //
 // Frame file format (read by the reference's tools/*.py): little-endian u32 N
 // followed by N x 3 float32 positions. --no-vulkan is accepted for
@@ -39,11 +45,13 @@ struct Args {
     std::string out_dir = "out";
     float damping = -1.0f;
     float viscosity = -1.0f;
+    int fixed_iters = -1;
+    bool host_substeps = false;
 };
 
 [[noreturn]] void usage_exit(int code) {
     std::puts("Usage: sim_cli --scene PATH [--frames START:END] [--record] "
-              "[--out DIR] [--no-vulkan] [--damping F] [--viscosity F]");
+              "[--out DIR] [--no-vulkan] [--damping F] [--viscosity F] [--fixed-iters N] [--host-substeps]");
     std::exit(code);
 }
 
@@ -72,6 +80,10 @@ Args parse(int argc, char** argv) {
             a.damping = std::stof(argv[++i]);
         } else if (s == "--viscosity" && i + 1 < argc) {
             a.viscosity = std::stof(argv[++i]);
+        } else if (s == "--fixed-iters" && i + 1 < argc) {
+            a.fixed_iters = std::stoi(argv[++i]);
+        } else if (s == "--host-substeps") {
+            a.host_substeps = true;
         } else if (s == "-h" || s == "--help") {
             usage_exit(0);
         } else {
@@ -154,6 +166,10 @@ int main(int argc, char** argv) try {
     cfg.domain_min = {0.0f, 0.0f, 0.0f};
     cfg.domain_max = {1.0f, 1.0f, 1.0f};
     if (args.damping >= 0.0f) cfg.damping = args.damping;
+    if (args.fixed_iters >= 0) {
+        cfg.max_density_iters = static_cast<water::u32>(args.fixed_iters);
+        cfg.eta_density = 0.0f;
+    }
     std::printf("solver cfg:   damping=%.3f viscosity=%.4f\n", cfg.damping, cfg.viscosity);
 
     const float spacing = 2.0f * cfg.particle_radius;
@@ -178,13 +194,17 @@ int main(int argc, char** argv) try {
     const float frame_dt = 1.0f / scene.output.fps;
     std::vector<water::Vec3f> host(store.count());
     for (int f = args.frames_start; f < args.frames_end; ++f) {
-        float remaining = frame_dt;
         int sub = 0;
-        while (remaining > 1e-6f && sub < 64) {
-            const float dt = ts.next_dt(std::max(solver.max_velocity(), 0.5f), cfg.particle_radius, remaining);
-            solver.step(dt);
-            remaining -= dt;
-            ++sub;
+        if (args.host_substeps) {
+            float remaining = frame_dt;
+            while (remaining > 1e-6f && sub < 64) {
+                const float dt = ts.next_dt(std::max(solver.max_velocity(), 0.5f), cfg.particle_radius, remaining);
+                solver.step(dt);
+                remaining -= dt;
+                ++sub;
+            }
+        } else {
+            sub = static_cast<int>(solver.step_frame(ts, frame_dt));
         }
         WATER_CUDA_CHECK(cudaDeviceSynchronize());
         std::printf("frame %4d: substeps=%2d, max_v=%.4f m/s\n", f + 1, sub, solver.max_velocity());

@@ -263,6 +263,32 @@ int dfsph_synchronize(dfsph_ctx* ctx) {
     });
 }
 
+int dfsph_frame_config_init(dfsph_frame_config* fc) {
+    if (!fc) return DFSPH_ERR_INVALID_ARGUMENT;
+    // TimeStepper::Config (core/include/water/core/timestep.h:10-15) and
+    // sim_cli's floor and cap (apps/sim_cli/main.cpp:172,175)
+    fc->frame_dt = 1.0f / 24.0f;
+    fc->stepper_frame_dt = 1.0f / 24.0f;
+    fc->dt_max = 1.0f / 24.0f;
+    fc->cfl_lambda = 0.4f;
+    fc->max_substeps = 16;
+    fc->min_velocity = 0.5f;
+    fc->max_substeps_per_frame = 64;
+    return DFSPH_OK;
+}
+
+int dfsph_step_frames(dfsph_ctx* ctx, const dfsph_frame_config* fc, uint32_t n_frames, uint32_t* substeps) {
+    if (!ctx || !fc) return DFSPH_ERR_INVALID_ARGUMENT;
+    if (!(fc->frame_dt > 0.0f) || fc->frame_dt > 1.0e30f || !(fc->stepper_frame_dt > 0.0f) ||
+        !(fc->dt_max > 0.0f) || !(fc->cfl_lambda > 0.0f) ||
+        fc->max_substeps == 0 || fc->max_substeps_per_frame == 0 || !(fc->min_velocity >= 0.0f))
+        return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        ctx->solver->step_frames(*fc, n_frames, substeps);
+    });
+}
+
 int dfsph_adjoint_set_state(dfsph_ctx* ctx, const void* pos, const void* vel, uint32_t n, int mem) {
     if (!ctx || (n > 0 && !pos)) return DFSPH_ERR_INVALID_ARGUMENT;
     if (mem != DFSPH_MEM_HOST && mem != DFSPH_MEM_DEVICE) return DFSPH_ERR_INVALID_ARGUMENT;

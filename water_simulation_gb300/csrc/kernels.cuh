@@ -128,6 +128,46 @@ static __device__ __forceinline__ void finish_reduction(double partial, double* 
     }
 }
 
+// A CFL frame stepped on the device: the substep size is chosen after every
+// substep from the in-kernel max |v| (the reference's TimeStepper::next_dt,
+// core/include/water/core/timestep.h:23-28, with sim_cli's 0.5 m/s floor and
+// 64-substep cap, apps/sim_cli/main.cpp:171-181), so no host round trip is
+// needed between substeps.
+struct FrameCtl {
+    float dt;            // substep size in use
+    float remaining;     // time left in the frame
+    u32 substeps;        // substeps taken in this frame
+    u32 frames_done;
+    u32 fresh;           // 1: no step taken yet (max |v| reads as 0)
+    u32 max_frames;      // length of substeps_out
+    float decay_f;       // e^{-damping dt} of the substep
+    double decay_d;
+    float frame_dt, dt_max, cfl_lambda, radius, dt_min, v_floor, damping;
+    u32 max_per_frame;
+    u32 more;            // 1: the frame continues (read by the host-driven loop)
+    u32* substeps_out;   // substeps per frame (device), or null
+};
+
+// Step size and the quantities derived from it, either fixed by the host
+// (dev == null) or read from the device frame control at kernel start.
+template <class R> struct StepDt {
+    R dt, decay, gx, gy, gz;   // gravity
+    const FrameCtl* dev;
+};
+
+template <class R> __device__ __forceinline__ R mul_rn(R a, R b);
+template <> __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+template <> __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
+template <class R> __device__ __forceinline__ void resolve_dt(StepDt<R>& s) {
+    if (s.dev) {
+        const FrameCtl* f = s.dev;
+        s.dt = R(*((volatile const float*)&f->dt));
+        s.decay = sizeof(R) == sizeof(float) ? R(*((volatile const float*)&f->decay_f))
+                                             : R(*((volatile const double*)&f->decay_d));
+    }
+}
+
 __device__ __forceinline__ bool stopped_before(const IterCtl* ctl, u32 iter) {
     // Iteration `iter` runs only while no earlier iteration decided to stop.
     return *((volatile const u32*)&ctl->stop_iter) < iter;
@@ -594,10 +634,14 @@ __global__ void __launch_bounds__(128) density_alpha_kernel(
 template <class R>
 __global__ void __launch_bounds__(128) forces_xsph_kernel(
     int n, const R4<R>* __restrict__ xk, const R4<R>* __restrict__ vr_in, R4<R>* __restrict__ vr_out,
-    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, R decay, R gdx, R gdy, R gdz, R eps,
+    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, StepDt<R> sd, R eps,
     const R* __restrict__ eps_scene, int do_xsph, R4<R>* __restrict__ tape_v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    resolve_dt(sd);
+    const R decay = sd.decay;
+    // g dt rounded on its own, as the host computes it
+    const R gdx = mul_rn(sd.gx, sd.dt), gdy = mul_rn(sd.gy, sd.dt), gdz = mul_rn(sd.gz, sd.dt);
     const R4<R> vi = ld(vr_in + i);
     if (tape_v) tape_v[i] = vi;
     R dx = 0, dy = 0, dz = 0;
@@ -639,10 +683,12 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
     int n, const R4<R>* __restrict__ xk_in, R4<R>* __restrict__ xk_out,
     const R4<R>* __restrict__ vr, const R* __restrict__ alpha, R* __restrict__ rho_adv,
     R* __restrict__ kap, const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd,
-    R dt, double* __restrict__ partials, IterCtl* ctl, u32 iter, u32 first_check, double inv_n,
+    StepDt<R> sd, double* __restrict__ partials, IterCtl* ctl, u32 iter, u32 first_check, double inv_n,
     double threshold, R4<R>* __restrict__ tape_v) {
     __shared__ double sh[4];
     if (stopped_before(ctl, iter)) return;
+    resolve_dt(sd);
+    const R dt = sd.dt;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double err = 0;
     if (i < n) {
@@ -707,9 +753,11 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
 template <class R>
 __global__ void __launch_bounds__(128) pressure_apply_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, const R* __restrict__ kap,
-    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, R dt, const IterCtl* ctl,
+    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, const IterCtl* ctl,
     u32 iter) {
     if (stopped_before(ctl, iter)) return;
+    resolve_dt(sd);
+    const R dt = sd.dt;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R4<R> pi = ld(xk + i);
@@ -752,20 +800,24 @@ __global__ void __launch_bounds__(128) pressure_apply_kernel(
 // ---------------------------------------------------------------------------
 // Integrator (advect_kernel dfsph_kernels.cu:363-386, MAX_VELOCITY_CLAMP = 5,
 // dfsph.cu:268) fused with the max-|v| reduction (dfsph.cu:303-326) and, when
-// COUNT, the next step's cell keys and per-cell counts.
+// COUNT, the next step's cell keys and per-cell counts. Positions are read
+// from xk and written to xk_out (the same buffer, or the other one when that
+// returns the position buffers to where the step found them).
 // ---------------------------------------------------------------------------
 template <class R, bool COUNT>
 __global__ void __launch_bounds__(256) advect_kernel(
-    int n, R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, R dt, R lox, R loy, R loz, R hix,
+    int n, const R4<R>* xk, R4<R>* xk_out, R4<R>* __restrict__ vr, StepDt<R> sd, R lox, R loy, R loz, R hix,
     R hiy, R hiz, GridDev<R> g, u32* __restrict__ key, u32* __restrict__ rank,
     u32* __restrict__ count, IterCtl* ctl, u32* __restrict__ maxv_scene, R4<R>* __restrict__ tape_v,
     unsigned char* __restrict__ tape_mask) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    resolve_dt(sd);
+    const R dt = sd.dt;
     u32 vbits = 0;
     u32 scene = 0xffffffffu;  // lanes past the end form their own group
     if (i < n) {
         R4<R> v = vr[i];
-        R4<R> x = xk[i];
+        const R4<R> x = xk[i];
         if (tape_v) tape_v[i] = v;
         // mask bits (recorded for the adjoint): 0-2 position clamped on x/y/z,
         // 3-5 velocity component zeroed, 6 speed clamped
@@ -787,7 +839,7 @@ __global__ void __launch_bounds__(256) advect_kernel(
         if (pz > hiz - eps) { pz = hiz - eps; mk |= 4u; if (v.z > R(0)) { v.z = R(0); mk |= 32u; } }
         if (tape_mask) tape_mask[i] = static_cast<unsigned char>(mk);
         vr[i] = {v.x, v.y, v.z, v.w};
-        xk[i] = {px, py, pz, R(0)};
+        xk_out[i] = {px, py, pz, R(0)};
         const float mag = float(sqrt(v.x * v.x + v.y * v.y + v.z * v.z));
         vbits = __float_as_uint(mag);
         scene = scene_of(g, i);

@@ -9,6 +9,7 @@
 // all of them, scene after scene, and one launch per kernel steps all of them.
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -16,6 +17,7 @@
 #include <vector>
 
 #include "adjoint.cuh"
+#include "frames.cuh"
 #include "kernels.cuh"
 #include "solver_api.h"
 
@@ -138,6 +140,7 @@ public:
         if (capture_stream_) cudaStreamDestroy(capture_stream_);
         if (host_ctl_) cudaFreeHost(host_ctl_);
         if (eps_host_) cudaFreeHost(eps_host_);
+        if (host_fctl_) cudaFreeHost(host_fctl_);
         for (const Record& r : records_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
         for (cudaEvent_t e : free_events_) cudaEventDestroy(e);
     }
@@ -195,9 +198,13 @@ public:
         const float* pos = upload(xyz, vel, n, mem);
         const float* v = vel ? pos + 3 * size_t(n) : nullptr;
         if (mem == DFSPH_MEM_DEVICE) { pos = xyz; v = vel; }
+        // captured graphs bake the particle counts in; new values of the same
+        // counts keep them valid
+        const bool same = n == n_ && scene_counts_.size() == n_scenes &&
+                          std::equal(counts, counts + n_scenes, scene_counts_.begin());
         n_ = n;
         drop_pending_counts();
-        drop_graph();
+        if (!same) drop_graph();
         scene_counts_.assign(counts, counts + n_scenes);
         if (scenes_ > 1 && n) {
             // sorted order is scene-major, so slot -> scene never changes
@@ -356,6 +363,7 @@ public:
             case DFSPH_SCALAR_BOUNDARY_COUNT: return double(nb_);
             case DFSPH_SCALAR_KERNEL_LAUNCHES: return double(launches_);
             case DFSPH_SCALAR_ACTIVE_BOUNDARY: return double(active_boundary());
+            case DFSPH_SCALAR_FRAME_GRAPH: return double(last_frame_graph_);
             default: break;
         }
         read_ctl();
@@ -402,6 +410,69 @@ public:
         records_.swap(keep);
         *total_ms = t;
         *count = c;
+    }
+
+    // ------------------------------------------------------------ frames
+    // n_frames frames of CFL substeps (sim_cli's loop, apps/sim_cli/main.cpp
+    // :171-181). With graphs enabled and fixed iteration counts each frame is
+    // one launch of a graph whose WHILE node repeats a captured substep and
+    // whose dt is chosen on the device; otherwise the host runs the
+    // reference's loop, reading max |v| back before every substep.
+    void step_frames(const dfsph_frame_config& fc, u32 n_frames, u32* substeps) override {
+        if (!have_state_) throw Error(DFSPH_ERR_STATE, "no fluid state: call dfsph_set_fluid first");
+        if (n_frames == 0) return;
+        std::vector<u32> subs(n_frames, 0u);
+        if (graph_ok()) {
+            if (!fctl_.p) {
+                fctl_.alloc(1);
+                DFSPH_CUDA(cudaMallocHost(reinterpret_cast<void**>(&host_fctl_), sizeof(FrameCtl)));
+            }
+            if (frame_sub_.n < n_frames) frame_sub_.alloc(n_frames);
+            FrameCtl& h = *host_fctl_;
+            std::memset(&h, 0, sizeof(h));
+            h.frame_dt = fc.frame_dt;
+            h.dt_max = fc.dt_max;
+            h.cfl_lambda = fc.cfl_lambda;
+            h.radius = cfg_.particle_radius;
+            h.dt_min = fc.stepper_frame_dt / static_cast<float>(fc.max_substeps);
+            h.v_floor = fc.min_velocity;
+            h.damping = cfg_.damping;
+            h.max_per_frame = fc.max_substeps_per_frame;
+            h.fresh = stepped_ ? 0u : 1u;
+            h.max_frames = n_frames;
+            h.substeps_out = frame_sub_.p;
+            DFSPH_CUDA(cudaMemcpyAsync(fctl_.p, &h, sizeof(FrameCtl), cudaMemcpyHostToDevice, stream_));
+            if (!counts_valid_) {
+                launch(DFSPH_KERNEL_GRID_COUNT, count_kernel<R>, blocks_for(n_, 256), 256, int(n_), xk_[cx_].p, g_,
+                       key_.p, rank_.p, count_.p);
+                counts_valid_ = true;
+            }
+            ensure_frame_graph();
+            for (u32 f = 0; f < n_frames; ++f) DFSPH_CUDA(cudaGraphLaunch(frame_exec_, stream_));
+            DFSPH_CUDA(cudaMemcpyAsync(subs.data(), frame_sub_.p, n_frames * sizeof(u32), cudaMemcpyDeviceToHost,
+                                       stream_));
+            DFSPH_CUDA(cudaStreamSynchronize(stream_));
+            unsigned long long total = 0;
+            for (u32 v : subs) total += v;
+            launches_ += total * frame_body_kernels_ + 2ull * n_frames;
+            stepped_ = true;
+            last_frame_graph_ = 1;
+        } else {
+            for (u32 f = 0; f < n_frames; ++f) {
+                float remaining = fc.frame_dt;
+                u32 sub = 0;
+                while (remaining > 1e-6f && sub < fc.max_substeps_per_frame) {
+                    const float maxv = float(get_scalar(DFSPH_SCALAR_MAX_VELOCITY));
+                    const float dt = host_next_dt(fc, std::max(maxv, fc.min_velocity), remaining);
+                    step(dt, 1);
+                    remaining -= dt;
+                    ++sub;
+                }
+                subs[f] = sub;
+            }
+            last_frame_graph_ = 0;
+        }
+        if (substeps) std::memcpy(substeps, subs.data(), n_frames * sizeof(u32));
     }
 
     // ------------------------------------------------------------- adjoint
@@ -685,9 +756,9 @@ private:
         return e;
     }
 
-    // ---- CUDA graphs: two steps return every ping-pong buffer to where it
-    // started (each step flips x 1 + iterations times, v twice, id once), so a
-    // captured pair of steps replays with the same pointers.
+    // ---- CUDA graphs: every step returns the ping-pong buffers to where it
+    // found them (step_once), so a captured pair of steps replays with the
+    // same pointers.
     bool graph_ok() const {
         const bool adaptive = cfg_.eta_density > 0.0f || (cfg_.max_divergence_iters > 0 && cfg_.eta_divergence > 0.0f);
         return cfg_.use_cuda_graph && !adaptive && profile_mask_ == 0 && have_state_ && n_ > 0;
@@ -697,6 +768,95 @@ private:
         if (graph_) cudaGraphDestroy(graph_);
         graph_exec_ = nullptr;
         graph_ = nullptr;
+        if (frame_exec_) cudaGraphExecDestroy(frame_exec_);
+        if (frame_graph_) cudaGraphDestroy(frame_graph_);
+        frame_exec_ = nullptr;
+        frame_graph_ = nullptr;
+    }
+
+    // TimeStepper::next_dt (core/include/water/core/timestep.h:23-28) on the host.
+    float host_next_dt(const dfsph_frame_config& fc, float max_velocity, float remaining) const {
+        const float v = std::max(max_velocity, 1e-6f);
+        const float dt_cfl = fc.cfl_lambda * cfg_.particle_radius / v;
+        const float dt_min = fc.stepper_frame_dt / static_cast<float>(fc.max_substeps);
+        return std::min({fc.dt_max, dt_cfl, remaining, std::max(dt_cfl, dt_min)});
+    }
+
+    // Graph of one frame: frame_begin -> WHILE(cond) { one substep with the
+    // device dt; frame_control } -> frame_end. The substep is captured once;
+    // steps leave the buffer parity unchanged, so every iteration replays the
+    // same pointers. Rebuilt when the stream, the state or the parity changes.
+    void ensure_frame_graph() {
+        if (frame_exec_ && cx_ == fg_cx_ && cv_ == fg_cv_ && ci_ == fg_ci_) return;
+        if (frame_exec_) cudaGraphExecDestroy(frame_exec_);
+        if (frame_graph_) cudaGraphDestroy(frame_graph_);
+        frame_exec_ = nullptr;
+        frame_graph_ = nullptr;
+        if (!capture_stream_) DFSPH_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
+        const int cx = cx_, cv = cv_, ci = ci_;
+        const cudaStream_t caller = stream_;
+        const unsigned long long k0 = graph_kernels_;
+        cudaGraph_t g = nullptr;
+        DFSPH_CUDA(cudaGraphCreate(&g, 0));
+        bool in_capture = false;
+        try {
+            FrameCtl* f = fctl_.p;
+            const IterCtl* c = ctl_.p;
+            void* begin_args[] = {&f, &c};
+            cudaKernelNodeParams kp = {};
+            kp.func = reinterpret_cast<void*>(frame_begin_kernel);
+            kp.gridDim = dim3(1);
+            kp.blockDim = dim3(32);
+            kp.kernelParams = begin_args;
+            cudaGraphNode_t nb = nullptr;
+            DFSPH_CUDA(cudaGraphAddKernelNode(&nb, g, nullptr, 0, &kp));
+            cudaGraphConditionalHandle h = 0;
+            DFSPH_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault));
+            cudaGraphNodeParams cp = {};
+            cp.type = cudaGraphNodeTypeConditional;
+            cp.conditional.handle = h;
+            cp.conditional.type = cudaGraphCondTypeWhile;
+            cp.conditional.size = 1;
+            cudaGraphNode_t nc = nullptr;
+            DFSPH_CUDA(cudaGraphAddNode(&nc, g, &nb, nullptr, 1, &cp));
+            cudaGraph_t body = cp.conditional.phGraph_out[0];
+            DFSPH_CUDA(cudaStreamBeginCaptureToGraph(capture_stream_, body, nullptr, nullptr, 0,
+                                                     cudaStreamCaptureModeThreadLocal));
+            in_capture = true;
+            stream_ = capture_stream_;
+            capturing_ = true;
+            step_once(R(0), true, nullptr, f);
+            launch(DFSPH_KERNEL_OTHER, frame_control_kernel, 1, 32, f, c, h, 1);
+            capturing_ = false;
+            stream_ = caller;
+            in_capture = false;
+            cudaGraph_t captured = nullptr;
+            DFSPH_CUDA(cudaStreamEndCapture(capture_stream_, &captured));
+            void* end_args[] = {&f};
+            kp.func = reinterpret_cast<void*>(frame_end_kernel);
+            kp.kernelParams = end_args;
+            cudaGraphNode_t ne = nullptr;
+            DFSPH_CUDA(cudaGraphAddKernelNode(&ne, g, &nc, 1, &kp));
+            if (cx_ != cx || cv_ != cv || ci_ != ci) throw Error(DFSPH_ERR_STATE, "a step changed buffer parity");
+            DFSPH_CUDA(cudaGraphInstantiate(&frame_exec_, g, 0));
+        } catch (...) {
+            if (in_capture) {
+                cudaGraph_t x = nullptr;
+                cudaStreamEndCapture(capture_stream_, &x);
+            }
+            cudaGraphDestroy(g);
+            cudaGetLastError();
+            capturing_ = false;
+            stream_ = caller;
+            cx_ = cx; cv_ = cv; ci_ = ci;
+            graph_kernels_ = k0;
+            frame_exec_ = nullptr;
+            throw;
+        }
+        frame_graph_ = g;
+        frame_body_kernels_ = graph_kernels_ - k0;
+        graph_kernels_ = k0;
+        fg_cx_ = cx_; fg_cv_ = cv_; fg_ci_ = ci_;
     }
     void ensure_graph(float dt) {
         // a replayed adjoint segment leaves the ping-pong parity where a plain
@@ -822,7 +982,7 @@ private:
     // the kernels stop themselves once the mean error is below eta rho0; the
     // host additionally stops launching after the device reports convergence.
     template <bool DIV>
-    u32 solve(R dt, u32 max_iters, float eta, IterCtl* ctl, R* kap_out, R* adv_out, const u32* cs,
+    u32 solve(const StepDt<R>& sd, u32 max_iters, float eta, IterCtl* ctl, R* kap_out, R* adv_out, const u32* cs,
               const StepTape<R>* tp) {
         const int n = int(n_);
         const bool adaptive = eta > 0.0f;
@@ -840,15 +1000,15 @@ private:
             V4* tv = tp ? tp->v[w] + it * tp->stride : nullptr;
             if (adaptive)
                 launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true>, blocks_for(n, 128), 128, n,
-                       xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), dt, partials_.p, ctl,
+                       xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl,
                        it, first_check, 1.0 / double(n), thr, tv);
             else
                 launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, false>, blocks_for(n, 128), 128, n,
-                       xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), dt, partials_.p, ctl,
+                       xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl,
                        it, first_check, 1.0 / double(n), thr, tv);
             if (!tp) cx_ ^= 1;
             launch(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R>, blocks_for(n, 128), 128, n, xout,
-                   vr_[cv_].p, kap_it, cs, g_, phys_, bdev(), dt, ctl, it);
+                   vr_[cv_].p, kap_it, cs, g_, phys_, bdev(), sd, ctl, it);
             launched = it + 1;
             if (adaptive && it >= first_check) {
                 // The reference reads the error back every iteration
@@ -863,12 +1023,25 @@ private:
         return launched;
     }
 
-    void step_once(R dt, bool count_next, const StepTape<R>* tp = nullptr) {
+    // One step. Every step leaves the ping-pong buffers where it found them
+    // (the sorted index is rebuilt in place, and the integrator writes the
+    // other position buffer when the step flipped it an odd number of times),
+    // so any captured sequence of steps replays with the same pointers.
+    // With fdev the kernels read dt from the device frame control.
+    void step_once(R dt, bool count_next, const StepTape<R>* tp = nullptr, const FrameCtl* fdev = nullptr) {
         if (!have_state_) throw Error(DFSPH_ERR_STATE, "no fluid state: call dfsph_set_fluid first");
         const int n = int(n_);
         if (n == 0) return;  // dfsph.cu:121-122
         stepped_ = true;
         u32* cs = tp ? tp->cs : cell_start_.p;
+        const int cx0 = cx_;
+        StepDt<R> sd;
+        sd.dt = dt;
+        sd.decay = std::exp(-R(cfg_.damping) * dt);
+        sd.gx = R(cfg_.gravity[0]);
+        sd.gy = R(cfg_.gravity[1]);
+        sd.gz = R(cfg_.gravity[2]);
+        sd.dev = fdev;
         const Tape1<R> t1{tp ? tp->x : nullptr, tp ? tp->g : nullptr, tp ? tp->id : nullptr};
         // 1. grid build (CellGrid::build, core/src/cell_grid.cu:73-138)
         if (!counts_valid_)
@@ -879,8 +1052,8 @@ private:
                id_[ci_].p, tmp_src_.p, tmp_id_.p);
         launch(DFSPH_KERNEL_GRID_REORDER, reorder_kernel<R>, blocks_for(n, 256), 256, n, tmp_src_.p, tmp_id_.p,
                key_.p, cs, cells1_, kSentinelCap, xk_[cx_].p, vr_[cv_].p, xk_[cx_ ^ 1].p, vr_[cv_ ^ 1].p,
-               id_[ci_ ^ 1].p, key_sorted_.p, ctl_.p);
-        cx_ ^= 1; cv_ ^= 1; ci_ ^= 1;
+               id_[ci_].p, key_sorted_.p, ctl_.p);
+        cx_ ^= 1; cv_ ^= 1;
         counts_valid_ = false;
         // 2. density + alpha (dfsph.cu:137-186)
         const BoundaryDev bd = bdev();
@@ -904,31 +1077,32 @@ private:
         // 3. divergence solve (the reference's plan; 0 iterations = the reference)
         last_divergence_launched_ = 0;
         if (cfg_.max_divergence_iters > 0)
-            last_divergence_launched_ = solve<true>(dt, cfg_.max_divergence_iters, cfg_.eta_divergence, ctl_.p + 1,
+            last_divergence_launched_ = solve<true>(sd, cfg_.max_divergence_iters, cfg_.eta_divergence, ctl_.p + 1,
                                                     kap_v_.p, rho_dot_.p, cs, tp);
         // 4. gravity + damping + XSPH (dfsph.cu:188-213)
-        const R decay = std::exp(-R(cfg_.damping) * dt);
         const bool xsph = explicit_eps_ ? any_xsph_ : cfg_.viscosity > 0.0f;
         launch(DFSPH_KERNEL_FORCES_XSPH, forces_xsph_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
-               vr_[cv_ ^ 1].p, cs, g_, phys_, decay, R(cfg_.gravity[0]) * dt, R(cfg_.gravity[1]) * dt,
-               R(cfg_.gravity[2]) * dt, R(cfg_.viscosity), scenes_ > 1 ? (const R*)eps_scene_.p : (const R*)nullptr,
-               xsph ? 1 : 0, tp ? tp->vx : nullptr);
+               vr_[cv_ ^ 1].p, cs, g_, phys_, sd, R(cfg_.viscosity),
+               scenes_ > 1 ? (const R*)eps_scene_.p : (const R*)nullptr, xsph ? 1 : 0, tp ? tp->vx : nullptr);
         cv_ ^= 1;
         // 5. density solve (dfsph.cu:215-260)
         last_density_launched_ =
-            solve<false>(dt, cfg_.max_density_iters, cfg_.eta_density, ctl_.p + 2, kap_.p, rho_adv_.p, cs, tp);
+            solve<false>(sd, cfg_.max_density_iters, cfg_.eta_density, ctl_.p + 2, kap_.p, rho_adv_.p, cs, tp);
         // 6. advect + max |v| (+ next step's cell counts)
         const R lo[3] = {R(cfg_.domain_min[0]), R(cfg_.domain_min[1]), R(cfg_.domain_min[2])};
         const R hi[3] = {R(cfg_.domain_max[0]), R(cfg_.domain_max[1]), R(cfg_.domain_max[2])};
         u32* mvs = scenes_ > 1 ? maxv_scene_.p : nullptr;
+        const V4* xin = xk_[cx_].p;
+        V4* xout = cx_ != cx0 ? xk_[cx_ ^ 1].p : xk_[cx_].p;
+        cx_ = cx0;
         if (count_next) {
-            launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, true>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p,
-                   dt, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p, mvs,
+            launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, true>, blocks_for(n, 256), 256, n, xin, xout, vr_[cv_].p,
+                   sd, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p, mvs,
                    tp ? tp->va : nullptr, tp ? tp->amask : nullptr);
             counts_valid_ = true;
         } else {
-            launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, false>, blocks_for(n, 256), 256, n, xk_[cx_].p, vr_[cv_].p,
-                   dt, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p, mvs,
+            launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, false>, blocks_for(n, 256), 256, n, xin, xout, vr_[cv_].p,
+                   sd, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p, mvs,
                    tp ? tp->va : nullptr, tp ? tp->amask : nullptr);
         }
     }
@@ -987,6 +1161,15 @@ private:
     DevBuf<u32> eps_ctr_;
     double* eps_host_ = nullptr;
     int graph_cx_ = 0, graph_cv_ = 0, graph_ci_ = 0;
+    // device-stepped frames
+    DevBuf<FrameCtl> fctl_;
+    DevBuf<u32> frame_sub_;
+    FrameCtl* host_fctl_ = nullptr;
+    cudaGraph_t frame_graph_ = nullptr;
+    cudaGraphExec_t frame_exec_ = nullptr;
+    int fg_cx_ = 0, fg_cv_ = 0, fg_ci_ = 0;
+    unsigned long long frame_body_kernels_ = 0;
+    int last_frame_graph_ = 0;
 };
 
 }  // namespace dfsph

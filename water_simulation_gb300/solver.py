@@ -124,6 +124,22 @@ class Solver:
                                                vp(density_ptr), vp(alpha_ptr), vp(kappa_ptr),
                                                vp(density_adv_ptr)))
 
+    def step_frames(self, n_frames: int = 1, frame_config: _lib.DfsphFrameConfig | None = None) -> np.ndarray:
+        """n_frames CFL frames (sim_cli's substep loop); returns the substeps of each frame."""
+        fc = frame_config or self.frame_config()
+        out = np.zeros(max(n_frames, 1), dtype=np.uint32)
+        self._check(self._lib.dfsph_step_frames(self._ctx, ctypes.byref(fc), n_frames,
+                                                out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
+        return out[:n_frames]
+
+    def frame_config(self) -> _lib.DfsphFrameConfig:
+        fc = _lib.DfsphFrameConfig()
+        self._lib.dfsph_frame_config_init(ctypes.byref(fc))
+        return fc
+
+    def frames_on_device(self) -> bool:
+        return bool(self.scalar(_lib.SCALAR_FRAME_GRAPH))
+
     def synchronize(self) -> None:
         self._check(self._lib.dfsph_synchronize(self._ctx))
 
