@@ -84,3 +84,41 @@ def test_frames_reject_bad_configs(block):
     fc.cfl_lambda = 0.0
     with pytest.raises(_lib.DfsphError):
         s.step_frames(1, fc)
+
+
+def _adaptive(graph: bool, damping: float = 0.5):
+    # the settled-puddle configuration: density eta 1e-4, divergence eta 1e-3,
+    # at most 100 iterations each (adaptive, the reference's solver loop)
+    sc = scenes.puddle()
+    sc.velocity = scenes.normal(5, sc.n, 0.3)
+    cfg = sc.config()
+    cfg.use_cuda_graph = 1 if graph else 0
+    cfg.damping = damping
+    s = Solver(cfg)
+    s.set_boundary(sc.boundary)
+    s.set_fluid(sc.fluid, sc.velocity)
+    return s
+
+
+def test_adaptive_solves_in_graphs_match_the_host_loop():
+    # dfsph_step with graphs runs both adaptive solves as device-resident
+    # WHILE loops; the iterations, their stopping points and the state must be
+    # those of the host-driven loop, bit for bit
+    dev, host = _adaptive(True), _adaptive(False)
+    for _ in range(3):
+        dev.step(1e-3, 4)
+        host.step(1e-3, 4)
+        assert dev.last_density_iters() == host.last_density_iters()
+        assert dev.last_divergence_iters() == host.last_divergence_iters()
+    assert dev.last_density_iters() >= 2
+    assert np.array_equal(dev.positions(), host.positions())
+    assert np.array_equal(dev.velocities(), host.velocities())
+
+
+def test_adaptive_device_frames_match_the_host_loop():
+    dev, host = _adaptive(True, 0.0), _adaptive(False, 0.0)
+    sd = dev.step_frames(3)
+    sh = host.step_frames(3)
+    assert dev.frames_on_device() and not host.frames_on_device()
+    assert list(sd) == list(sh)
+    assert np.array_equal(dev.positions(), host.positions())

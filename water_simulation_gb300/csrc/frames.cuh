@@ -1,9 +1,13 @@
-// CFL frames stepped on the device. The reference's sim_cli picks every
+// Device-resident loops: CFL frames and adaptive Jacobi solves stepped on the
+// device. The reference's sim_cli picks every
 // substep on the host after reading max |v| back (apps/sim_cli/main.cpp
 // :171-181, TimeStepper::next_dt in core/include/water/core/timestep.h:23-28);
 // here the same float arithmetic runs in a one-thread kernel after each
 // substep, against the max |v| the integrator left in IterCtl, and a CUDA
-// graph WHILE node repeats the substep until the frame is done.
+// graph WHILE node repeats the substep until the frame is done. The
+// reference's solvers read the mean error back after every iteration
+// (dfsph.cu:296-299); inside a graph a WHILE node repeats rate + apply until
+// the device-side convergence test stops it.
 #pragma once
 
 #include "kernels.cuh"
@@ -61,6 +65,26 @@ static __global__ void frame_control_kernel(FrameCtl* f, const IterCtl* ctl, cud
     if (more) choose_substep(f, read_max_velocity(ctl));
     if (use_handle) cudaGraphSetConditional(h, more ? 1u : 0u);
     f->more = more ? 1u : 0u;
+}
+
+// End of one iteration of a device-resident Jacobi loop (a WHILE node around
+// rate + apply): counts it and keeps the loop going while fewer than
+// max_iters ran and no iteration decided to stop (finish_reduction's
+// convergence test, dfsph.cu:254-258).
+static __global__ void iteration_control_kernel(IterCtl* ctl, u32 max_iters, cudaGraphConditionalHandle h) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const u32 it = ctl->iters + 1u;
+    ctl->iters = it;
+    const bool more = it < max_iters && *((volatile const u32*)&ctl->stop_iter) == ~0u;
+    cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+// Sets a WHILE node's condition before the node runs. A condition's default
+// value is applied once per launch of the whole graph, so a loop nested in
+// another loop's body (a solve inside a frame's substep) must be re-armed
+// every time its parent body runs.
+static __global__ void loop_arm_kernel(cudaGraphConditionalHandle h) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(h, 1u);
 }
 
 static __global__ void frame_end_kernel(FrameCtl* f) {

@@ -85,7 +85,7 @@ struct IterCtl {
     double err_sum;       // sum of the last finished reduction
     u32 stop_iter;        // iteration after which the solver stopped (~0u: running)
     u32 blocks_done;      // last-block counter
-    u32 maxv_bits;        // unused
+    u32 iters;            // iterations run by a device-resident solve loop
     u32 maxv_slot[32];    // max |v| as float bits (non-negative floats order as
                           // ints), spread over MAXV_SLOTS words; the max of the
                           // words is the step's max |v|
@@ -267,7 +267,7 @@ static __global__ void __launch_bounds__(1024) scan_tile_offsets(u32* __restrict
             ctl[k].err_sum = 0.0;
             ctl[k].stop_iter = ~0u;
             ctl[k].blocks_done = 0u;
-            ctl[k].maxv_bits = 0u;
+            ctl[k].iters = 0u;
             for (int w = 0; w < MAXV_SLOTS; ++w) ctl[k].maxv_slot[w] = 0u;
             ctl[k].flags = 0u;
         }
@@ -684,8 +684,18 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
     const R4<R>* __restrict__ vr, const R* __restrict__ alpha, R* __restrict__ rho_adv,
     R* __restrict__ kap, const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd,
     StepDt<R> sd, double* __restrict__ partials, IterCtl* ctl, u32 iter, u32 first_check, double inv_n,
-    double threshold, R4<R>* __restrict__ tape_v) {
+    double threshold, R4<R>* __restrict__ tape_v, const u32* dev_iter) {
     __shared__ double sh[4];
+    // Inside a device-resident loop the iteration comes from the device and
+    // even iterations read xk_in / write xk_out, odd ones the other way round.
+    if (dev_iter) {
+        iter = *((volatile const u32*)dev_iter);
+        if (iter & 1u) {
+            R4<R>* t = xk_out;
+            xk_out = const_cast<R4<R>*>(xk_in);
+            xk_in = t;
+        }
+    }
     if (stopped_before(ctl, iter)) return;
     resolve_dt(sd);
     const R dt = sd.dt;
@@ -754,7 +764,11 @@ template <class R>
 __global__ void __launch_bounds__(128) pressure_apply_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, const R* __restrict__ kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, const IterCtl* ctl,
-    u32 iter) {
+    u32 iter, const R4<R>* xk_odd, const u32* dev_iter) {
+    if (dev_iter) {
+        iter = *((volatile const u32*)dev_iter);
+        if (iter & 1u) xk = xk_odd;
+    }
     if (stopped_before(ctl, iter)) return;
     resolve_dt(sd);
     const R dt = sd.dt;

@@ -138,6 +138,7 @@ public:
     ~Solver() override {
         drop_graph();
         if (capture_stream_) cudaStreamDestroy(capture_stream_);
+        if (loop_stream_) cudaStreamDestroy(loop_stream_);
         if (host_ctl_) cudaFreeHost(host_ctl_);
         if (eps_host_) cudaFreeHost(eps_host_);
         if (host_fctl_) cudaFreeHost(host_fctl_);
@@ -266,6 +267,7 @@ public:
                     DFSPH_CUDA(cudaGraphLaunch(graph_exec_, stream_));
                     launches_ += graph_kernels_;
                 }
+                iters_on_device_ = adaptive();
             }
         }
         for (; k < n_steps; ++k) step_once(R(dt), /*count_next=*/true);
@@ -376,8 +378,10 @@ public:
                 return stepped_ ? double(f) : 0.0;
             }
             case DFSPH_SCALAR_LAST_DENSITY_ITERS:
+                if (iters_on_device_) return double(host_ctl_[2].iters);
                 return double(iters_done(host_ctl_[2], last_density_launched_));
             case DFSPH_SCALAR_LAST_DIVERGENCE_ITERS:
+                if (iters_on_device_) return double(host_ctl_[1].iters);
                 return double(iters_done(host_ctl_[1], last_divergence_launched_));
             case DFSPH_SCALAR_DENSITY_ERROR: return n_ ? host_ctl_[2].err_sum / double(n_) : 0.0;
             case DFSPH_SCALAR_DIVERGENCE_ERROR: return n_ ? host_ctl_[1].err_sum / double(n_) : 0.0;
@@ -456,6 +460,7 @@ public:
             for (u32 v : subs) total += v;
             launches_ += total * frame_body_kernels_ + 2ull * n_frames;
             stepped_ = true;
+            iters_on_device_ = adaptive();
             last_frame_graph_ = 1;
         } else {
             for (u32 f = 0; f < n_frames; ++f) {
@@ -759,9 +764,13 @@ private:
     // ---- CUDA graphs: every step returns the ping-pong buffers to where it
     // found them (step_once), so a captured pair of steps replays with the
     // same pointers.
+    bool adaptive() const {
+        return (cfg_.max_density_iters > 0 && cfg_.eta_density > 0.0f) ||
+               (cfg_.max_divergence_iters > 0 && cfg_.eta_divergence > 0.0f);
+    }
     bool graph_ok() const {
-        const bool adaptive = cfg_.eta_density > 0.0f || (cfg_.max_divergence_iters > 0 && cfg_.eta_divergence > 0.0f);
-        return cfg_.use_cuda_graph && !adaptive && profile_mask_ == 0 && have_state_ && n_ > 0;
+        // adaptive solves run as device-resident loops inside the graph
+        return cfg_.use_cuda_graph && profile_mask_ == 0 && have_state_ && n_ > 0;
     }
     void drop_graph() {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
@@ -988,6 +997,8 @@ private:
         const bool adaptive = eta > 0.0f;
         const double thr = double(eta) * double(cfg_.rest_density);
         const u32 first_check = DIV ? 0u : 1u;  // density: from the 2nd iteration (dfsph.cu:255)
+        if (capturing_ && adaptive && !tp) return solve_on_device<DIV>(sd, max_iters, thr, first_check, ctl, kap_out,
+                                                                       adv_out, cs);
         const int w = DIV ? 0 : 1;
         u32 launched = 0;
         for (u32 it = 0; it < max_iters; ++it) {
@@ -1001,14 +1012,14 @@ private:
             if (adaptive)
                 launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true>, blocks_for(n, 128), 128, n,
                        xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl,
-                       it, first_check, 1.0 / double(n), thr, tv);
+                       it, first_check, 1.0 / double(n), thr, tv, (const u32*)nullptr);
             else
                 launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, false>, blocks_for(n, 128), 128, n,
                        xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl,
-                       it, first_check, 1.0 / double(n), thr, tv);
+                       it, first_check, 1.0 / double(n), thr, tv, (const u32*)nullptr);
             if (!tp) cx_ ^= 1;
             launch(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R>, blocks_for(n, 128), 128, n, xout,
-                   vr_[cv_].p, kap_it, cs, g_, phys_, bdev(), sd, ctl, it);
+                   vr_[cv_].p, kap_it, cs, g_, phys_, bdev(), sd, ctl, it, (const V4*)nullptr, (const u32*)nullptr);
             launched = it + 1;
             if (adaptive && it >= first_check) {
                 // The reference reads the error back every iteration
@@ -1028,11 +1039,68 @@ private:
     // other position buffer when the step flipped it an odd number of times),
     // so any captured sequence of steps replays with the same pointers.
     // With fdev the kernels read dt from the device frame control.
+    // An adaptive solve inside a graph capture: a WHILE node whose body is one
+    // iteration (rate, apply, iteration_control_kernel); the kernels take the
+    // iteration number from the device and alternate the two position buffers
+    // by its parity, so the body replays with fixed pointers. Both buffers hold
+    // the step's positions afterwards (every rate pass copies them), so the
+    // host-side parity does not depend on the iteration count.
+    template <bool DIV>
+    u32 solve_on_device(const StepDt<R>& sd, u32 max_iters, double thr, u32 first_check, IterCtl* ctl, R* kap_out,
+                        R* adv_out, const u32* cs) {
+        if (max_iters == 0) return 0;
+        const int n = int(n_);
+        cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+        cudaGraph_t g = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        DFSPH_CUDA(cudaStreamGetCaptureInfo(stream_, &st, nullptr, &g, &deps, nullptr, &nd));
+        if (st != cudaStreamCaptureStatusActive) throw Error(DFSPH_ERR_STATE, "device-resident solve outside a capture");
+        cudaGraphConditionalHandle h = 0;
+        DFSPH_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault));
+        launch(DFSPH_KERNEL_OTHER, loop_arm_kernel, 1, 32, h);
+        DFSPH_CUDA(cudaStreamGetCaptureInfo(stream_, &st, nullptr, &g, &deps, nullptr, &nd));
+        cudaGraphNodeParams cp = {};
+        cp.type = cudaGraphNodeTypeConditional;
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        DFSPH_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &cp));
+        DFSPH_CUDA(cudaStreamUpdateCaptureDependencies(stream_, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        if (!loop_stream_) DFSPH_CUDA(cudaStreamCreateWithFlags(&loop_stream_, cudaStreamNonBlocking));
+        const cudaStream_t outer = stream_;
+        DFSPH_CUDA(cudaStreamBeginCaptureToGraph(loop_stream_, cp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                                 cudaStreamCaptureModeThreadLocal));
+        stream_ = loop_stream_;
+        try {
+            V4* xa = xk_[cx_].p;
+            V4* xb = xk_[cx_ ^ 1].p;
+            const u32* dit = &ctl->iters;
+            launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true>, blocks_for(n, 128), 128, n,
+                   (const V4*)xa, xb, vr_[cv_].p, alpha_.p, adv_out, kap_out, cs, g_, phys_, bdev(), sd, partials_.p,
+                   ctl, 0u, first_check, 1.0 / double(n), thr, (V4*)nullptr, dit);
+            launch(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R>, blocks_for(n, 128), 128, n, (const V4*)xb,
+                   vr_[cv_].p, kap_out, cs, g_, phys_, bdev(), sd, (const IterCtl*)ctl, 0u, (const V4*)xa, dit);
+            launch(DFSPH_KERNEL_OTHER, iteration_control_kernel, 1, 32, ctl, max_iters, h);
+        } catch (...) {
+            stream_ = outer;
+            cudaGraph_t x = nullptr;
+            cudaStreamEndCapture(loop_stream_, &x);
+            throw;
+        }
+        stream_ = outer;
+        cudaGraph_t body = nullptr;
+        DFSPH_CUDA(cudaStreamEndCapture(loop_stream_, &body));
+        return max_iters;  // at most; the device counts the iterations run
+    }
+
     void step_once(R dt, bool count_next, const StepTape<R>* tp = nullptr, const FrameCtl* fdev = nullptr) {
         if (!have_state_) throw Error(DFSPH_ERR_STATE, "no fluid state: call dfsph_set_fluid first");
         const int n = int(n_);
         if (n == 0) return;  // dfsph.cu:121-122
         stepped_ = true;
+        if (!capturing_) iters_on_device_ = false;
         u32* cs = tp ? tp->cs : cell_start_.p;
         const int cx0 = cx_;
         StepDt<R> sd;
@@ -1170,6 +1238,8 @@ private:
     int fg_cx_ = 0, fg_cv_ = 0, fg_ci_ = 0;
     unsigned long long frame_body_kernels_ = 0;
     int last_frame_graph_ = 0;
+    cudaStream_t loop_stream_ = nullptr;
+    bool iters_on_device_ = false;  // the last step's iteration counts live in IterCtl::iters
 };
 
 }  // namespace dfsph
