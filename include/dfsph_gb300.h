@@ -280,6 +280,30 @@ int dfsph_morton_sort(const float* xyz_dev, uint32_t n, const float scene_min[3]
                       const float scene_max[3], uint32_t* sorted_codes_dev,
                       uint32_t* sorted_indices_dev, void* stream);
 
+/* SpatialAccel::build (core/src/spatial_accel.cu:110-179; the class in
+ * core/include/water/core/spatial_accel.h:19-54): Morton order as
+ * dfsph_morton_sort, internal nodes by Karras' construction with equal codes
+ * ordered by sorted slot, leaf boxes position +- leaf_radius, plus the
+ * bottom-up internal-box pass the reference leaves for later. Node ids as in
+ * the reference: internal 0..n-2 (root 0), leaf of sorted slot k = n-1+k.
+ * Device arrays: codes[n], sorted_indices[n], left[n-1], right[n-1],
+ * parent[2n-1] (root: 0xFFFFFFFF), boxes[6(2n-1)] (min xyz, max xyz per node),
+ * scratch[n-1]. n < 2^30. Stream-ordered on `stream`. */
+int dfsph_lbvh_build(const float* xyz_dev, uint32_t n, const float scene_min[3], const float scene_max[3],
+                     float leaf_radius, uint32_t* codes_dev, uint32_t* sorted_indices_dev, uint32_t* left_dev,
+                     uint32_t* right_dev, uint32_t* parent_dev, float* boxes_dev, uint32_t* scratch_dev,
+                     void* stream);
+/* Refit after the particles moved: leaf boxes from xyz_dev (original order),
+ * internal boxes bottom-up on the topology of the last build. */
+int dfsph_lbvh_refit(const float* xyz_dev, uint32_t n, float leaf_radius, const uint32_t* sorted_indices_dev,
+                     const uint32_t* left_dev, const uint32_t* right_dev, const uint32_t* parent_dev,
+                     float* boxes_dev, uint32_t* scratch_dev, void* stream);
+
+/* The Akinci 2013 cohesion kernel C(r, l) of core/include/water/core/sph_kernels.cuh
+ * :43-51 (declared there, called by nothing), evaluated for n distances
+ * (device arrays). */
+int dfsph_cohesion_kernel(const float* r_dev, uint32_t n, float support, float* out_dev, void* stream);
+
 /* No counterpart in the reference. The same cell-grid build as
  * dfsph_build_cell_grid for callers that cannot allocate device memory (a
  * host callback or graph node that must not enter the allocator, a plugin

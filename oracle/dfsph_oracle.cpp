@@ -734,6 +734,99 @@ int oracle_morton_sort(const float* xyz, u32 n, const float smin[3], const float
     return 0;
 }
 
+// SpatialAccel's internal nodes (core/src/spatial_accel.cu:42-97): for each
+// internal node, the reference's delta with the index tie-break, its range
+// direction, doubling + bisection for the range end and its split search,
+// restated loop for loop; leaf boxes p +- radius (init_leaf_aabbs,
+// spatial_accel.cu:99-107); internal boxes as the union of their subtree's
+// leaf boxes (the pass the reference leaves for later). Inputs: the sorted
+// codes and permutation of oracle_morton_sort. Outputs as dfsph_lbvh_build.
+static int clz32(u32 v) {
+    int c = 0;
+    for (u32 m = 0x80000000u; m && !(v & m); m >>= 1) ++c;
+    return c;
+}
+
+static int lbvh_delta(int i, int j, const u32* codes, int n) {
+    if (j < 0 || j >= n) return -1;
+    const u32 ci = codes[i], cj = codes[j];
+    if (ci == cj) return 32 + clz32(static_cast<u32>(i ^ j));
+    return clz32(ci ^ cj);
+}
+
+int oracle_lbvh_build(const float* xyz, u32 n, const u32* codes, const u32* sorted, float radius, u32* left,
+                      u32* right, u32* parent, float* boxes) {
+    if (n == 0) return 0;
+    const int nl = static_cast<int>(n);
+    const int n_internal = nl - 1;
+    parent[0] = 0xFFFFFFFFu;
+    for (int i = 0; i < n_internal; ++i) {
+        const int d = (lbvh_delta(i, i + 1, codes, nl) - lbvh_delta(i, i - 1, codes, nl)) > 0 ? 1 : -1;
+        const int delta_min = lbvh_delta(i, i - d, codes, nl);
+        int l_max = 2;
+        while (lbvh_delta(i, i + l_max * d, codes, nl) > delta_min) l_max *= 2;
+        int l = 0;
+        for (int t = l_max / 2; t > 0; t /= 2)
+            if (lbvh_delta(i, i + (l + t) * d, codes, nl) > delta_min) l += t;
+        const int j = i + l * d;
+        const int delta_node = lbvh_delta(i, j, codes, nl);
+        int s = 0;
+        int t = (l + 1) / 2;
+        while (t > 0) {
+            if (lbvh_delta(i, i + (s + t) * d, codes, nl) > delta_node) s += t;
+            t = (t == 1) ? 0 : (t + 1) / 2;
+        }
+        const int gamma = i + s * d + std::min(d, 0);
+        const int lc = (std::min(i, j) == gamma) ? (n_internal + gamma) : gamma;
+        const int rc = (std::max(i, j) == gamma + 1) ? (n_internal + gamma + 1) : (gamma + 1);
+        left[i] = static_cast<u32>(lc);
+        right[i] = static_cast<u32>(rc);
+        parent[lc] = static_cast<u32>(i);
+        parent[rc] = static_cast<u32>(i);
+    }
+    for (int k = 0; k < nl; ++k) {
+        const float* p = xyz + 3 * std::size_t(sorted[k]);
+        float* b = boxes + 6 * std::size_t(n_internal + k);
+        for (int a = 0; a < 3; ++a) {
+            b[a] = p[a] - radius;
+            b[3 + a] = p[a] + radius;
+        }
+    }
+    // children before parents: post-order over an explicit stack
+    if (n_internal > 0) {
+        std::vector<std::pair<u32, bool>> stack{{0u, false}};
+        while (!stack.empty()) {
+            const auto [node, expanded] = stack.back();
+            stack.pop_back();
+            if (node >= static_cast<u32>(n_internal)) continue;
+            if (!expanded) {
+                stack.push_back({node, true});
+                stack.push_back({left[node], false});
+                stack.push_back({right[node], false});
+                continue;
+            }
+            const float* a = boxes + 6 * std::size_t(left[node]);
+            const float* c = boxes + 6 * std::size_t(right[node]);
+            float* o = boxes + 6 * std::size_t(node);
+            for (int k = 0; k < 3; ++k) {
+                o[k] = std::min(a[k], c[k]);
+                o[3 + k] = std::max(a[3 + k], c[3 + k]);
+            }
+        }
+    }
+    return 0;
+}
+
+// cohesion_C (core/include/water/core/sph_kernels.cuh:44-51), in double.
+double oracle_cohesion_C(double r, double l) {
+    if (r <= 0.0 || r > l) return 0.0;
+    const double sigma = 32.0 / (3.14159265358979323846 * std::pow(l, 9.0));
+    const double lm = l - r;
+    const double t = lm * lm * lm * r * r * r;
+    if (2.0 * r > l) return sigma * t;
+    return sigma * (2.0 * t - std::pow(l, 6.0) / 64.0);
+}
+
 // make_grid geometry (dfsph.cu:55-65).
 void oracle_grid_geometry(const Config* cfg, float origin[3], int dims[3]) {
     const oracle::Grid g = oracle::make_grid(*cfg);

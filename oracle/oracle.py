@@ -72,6 +72,9 @@ def load():
         L.oracle_dual_step.argtypes = [P, ctypes.c_float, ctypes.c_uint32]
         L.oracle_dual_get.argtypes = [P, P, P, P, P]
         L.oracle_dual_destroy.argtypes = [P]
+        L.oracle_lbvh_build.argtypes = [P, ctypes.c_uint32, P, P, ctypes.c_float, P, P, P, P]
+        L.oracle_cohesion_C.restype = ctypes.c_double
+        L.oracle_cohesion_C.argtypes = [ctypes.c_double, ctypes.c_double]
         L.oracle_set_threads.argtypes = [ctypes.c_int]
         L.oracle_max_threads.restype = ctypes.c_int
         _lib = L
@@ -137,6 +140,34 @@ def morton_sort(xyz, smin, smax):
     L.oracle_morton_sort(xyz.ctypes.data_as(ctypes.c_void_p), n, f3(smin), f3(smax),
                          codes.ctypes.data_as(ctypes.c_void_p), idx.ctypes.data_as(ctypes.c_void_p))
     return codes, idx
+
+
+def lbvh_build(xyz, smin, smax, radius=0.0, codes=None, sorted_idx=None):
+    """SpatialAccel build restated: (codes, sorted, left, right, parent, boxes).
+    Given codes and sorted_idx (of an earlier build), the topology is theirs and
+    only the boxes follow xyz (a refit)."""
+    L = load()
+    xyz = np.ascontiguousarray(xyz, np.float32).reshape(-1, 3)
+    n = xyz.shape[0]
+    if codes is None:
+        codes, sorted_idx = morton_sort(xyz, smin, smax)
+    codes = np.ascontiguousarray(codes, np.uint32)
+    sorted_idx = np.ascontiguousarray(sorted_idx, np.uint32)
+    m = max(n - 1, 1)
+    left = np.zeros(m, np.uint32)
+    right = np.zeros(m, np.uint32)
+    parent = np.zeros(max(2 * n - 1, 1), np.uint32)
+    boxes = np.zeros((max(2 * n - 1, 1), 6), np.float32)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    if n:
+        L.oracle_lbvh_build(p(xyz), n, p(codes), p(sorted_idx), ctypes.c_float(radius), p(left), p(right),
+                            p(parent), p(boxes))
+    return codes, sorted_idx, left[: max(n - 1, 0)], right[: max(n - 1, 0)], parent[: max(2 * n - 1, 0)], \
+        boxes[: max(2 * n - 1, 0)]
+
+
+def cohesion_C(r, l):
+    return load().oracle_cohesion_C(float(r), float(l))
 
 
 def W(r, l, precision=32):

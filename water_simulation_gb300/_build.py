@@ -33,6 +33,7 @@ CUDA_UNITS = [
     ("stencil_recip.cu", ["-use_fast_math"]),
     ("static_grid.cu", []),
     ("morton.cu", []),
+    ("lbvh.cu", []),
 ]
 CXX_UNITS = ["geometry.cpp"]
 

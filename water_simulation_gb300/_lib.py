@@ -152,6 +152,9 @@ _SIGNATURES = [
     ("dfsph_build_cell_grid", ctypes.c_int,
      [_P, ctypes.c_uint32, _F, ctypes.POINTER(ctypes.c_int), ctypes.c_float, _P, _P, _P, _P]),
     ("dfsph_morton_sort", ctypes.c_int, [_P, ctypes.c_uint32, _F, _F, _P, _P, _P]),
+    ("dfsph_lbvh_build", ctypes.c_int, [_P, ctypes.c_uint32, _F, _F, ctypes.c_float, _P, _P, _P, _P, _P, _P, _P, _P]),
+    ("dfsph_lbvh_refit", ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_float, _P, _P, _P, _P, _P, _P, _P]),
+    ("dfsph_cohesion_kernel", ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_float, _P, _P]),
     ("dfsph_build_cell_grid_static", ctypes.c_int,
      [_P, ctypes.c_uint32, _F, ctypes.POINTER(ctypes.c_int), ctypes.c_float, _P, _P, _P, _P]),
 ]

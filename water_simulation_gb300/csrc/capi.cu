@@ -354,6 +354,39 @@ int dfsph_morton_sort(const float* xyz_dev, uint32_t n, const float scene_min[3]
     });
 }
 
+int dfsph_lbvh_build(const float* xyz_dev, uint32_t n, const float scene_min[3], const float scene_max[3],
+                     float leaf_radius, uint32_t* codes_dev, uint32_t* sorted_indices_dev, uint32_t* left_dev,
+                     uint32_t* right_dev, uint32_t* parent_dev, float* boxes_dev, uint32_t* scratch_dev,
+                     void* stream) {
+    if (!scene_min || !scene_max || n >= (1u << 30)) return DFSPH_ERR_INVALID_ARGUMENT;
+    if (n > 0 && (!xyz_dev || !codes_dev || !sorted_indices_dev || !parent_dev || !boxes_dev))
+        return DFSPH_ERR_INVALID_ARGUMENT;
+    if (n > 1 && (!left_dev || !right_dev || !scratch_dev)) return DFSPH_ERR_INVALID_ARGUMENT;
+    if (!(leaf_radius >= 0.0f) || leaf_radius > 1.0e30f) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(nullptr, [&] {
+        dfsph::lbvh_build(xyz_dev, n, scene_min, scene_max, leaf_radius, codes_dev, sorted_indices_dev, left_dev,
+                          right_dev, parent_dev, boxes_dev, scratch_dev, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int dfsph_lbvh_refit(const float* xyz_dev, uint32_t n, float leaf_radius, const uint32_t* sorted_indices_dev,
+                     const uint32_t* left_dev, const uint32_t* right_dev, const uint32_t* parent_dev,
+                     float* boxes_dev, uint32_t* scratch_dev, void* stream) {
+    if (n >= (1u << 30)) return DFSPH_ERR_INVALID_ARGUMENT;
+    if (n > 0 && (!xyz_dev || !sorted_indices_dev || !parent_dev || !boxes_dev)) return DFSPH_ERR_INVALID_ARGUMENT;
+    if (n > 1 && (!left_dev || !right_dev || !scratch_dev)) return DFSPH_ERR_INVALID_ARGUMENT;
+    if (!(leaf_radius >= 0.0f) || leaf_radius > 1.0e30f) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(nullptr, [&] {
+        dfsph::lbvh_refit(xyz_dev, n, leaf_radius, sorted_indices_dev, left_dev, right_dev, parent_dev, boxes_dev,
+                          scratch_dev, static_cast<cudaStream_t>(stream));
+    });
+}
+
+int dfsph_cohesion_kernel(const float* r_dev, uint32_t n, float support, float* out_dev, void* stream) {
+    if ((n > 0 && (!r_dev || !out_dev)) || !(support > 0.0f)) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(nullptr, [&] { dfsph::cohesion(r_dev, n, support, out_dev, static_cast<cudaStream_t>(stream)); });
+}
+
 int dfsph_build_cell_grid(const float* xyz_dev, uint32_t n, const float origin[3], const int dims[3],
                           float cell_length, uint32_t* sorted_keys_dev, uint32_t* sorted_indices_dev,
                           uint32_t* cell_start_dev, void* stream) {

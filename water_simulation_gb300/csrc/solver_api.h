@@ -54,4 +54,16 @@ void build_cell_grid(const float* xyz, std::uint32_t n, const float origin[3], c
 void morton_sort(const float* xyz, std::uint32_t n, const float smin[3], const float smax[3],
                  std::uint32_t* sorted_codes, std::uint32_t* sorted_idx, cudaStream_t st);
 
+// SpatialAccel::build (core/src/spatial_accel.cu:110-179) with the bottom-up
+// box pass, and its refit on moved positions.
+void lbvh_build(const float* xyz, std::uint32_t n, const float smin[3], const float smax[3], float radius,
+                std::uint32_t* codes, std::uint32_t* sorted, std::uint32_t* left, std::uint32_t* right,
+                std::uint32_t* parent, float* boxes, std::uint32_t* scratch, cudaStream_t st);
+void lbvh_refit(const float* xyz, std::uint32_t n, float radius, const std::uint32_t* sorted,
+                const std::uint32_t* left, const std::uint32_t* right, const std::uint32_t* parent, float* boxes,
+                std::uint32_t* scratch, cudaStream_t st);
+
+// Akinci cohesion kernel C(r, l) (core/include/water/core/sph_kernels.cuh:43-51).
+void cohesion(const float* r, std::uint32_t n, float l, float* out, cudaStream_t st);
+
 }  // namespace dfsph
