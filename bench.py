@@ -76,6 +76,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-drop timing")
     ap.add_argument("--no-precision", action="store_true", help="skip the FP32 vs FP64 field errors")
     ap.add_argument("--no-frames", action="store_true", help="skip the device-stepped frame timing")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default 128-thread neighbour passes")
     return ap.parse_args()
 
 
@@ -210,6 +211,9 @@ def bench_ours(args, rank, world):
     stream = torch.cuda.current_stream()
     s = solver_for(sc, stream=stream.cuda_stream, device=local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    # launch shapes of the neighbour passes, measured on this workload (the
+    # state is restored afterwards)
+    tuned = s.autotune(sc.dt, 3) if not args.no_autotune else s.block_sizes()
     # warm-up, with every kernel class profiled to find the dominant one
     s.profile_enable((1 << _lib.KERNEL_CLASSES) - 1)
     for _ in range(args.warmup):
@@ -247,6 +251,7 @@ def bench_ours(args, rank, world):
     res = {"ms_total": ms_max, "work": work, "wall_s": wall, "launches": launches, "clocks": clk.summary(),
            "dominant": dominant, "dominant_ms": dom_ms, "dominant_launches": dom_launches,
            "nb_active": nb_active,
+           "block_sizes": {k: tuned[k] for k in ("density_alpha", "pressure_rate", "pressure_apply", "forces_xsph")},
            "warmup_share": {k: round(v[0] / max(sum(x[0] for x in share.values()), 1e-9), 4)
                             for k, v in share.items() if v[1]}}
     if not args.no_e2e:
@@ -579,7 +584,8 @@ def main():
         "config": {"workload": sc.name, "particles": sc.n, "boundary_particles": sc.nb,
                    "density_iters": sc.max_density_iters, "divergence_iters": sc.max_divergence_iters,
                    "dt": sc.dt, "parallelism": f"replicas x{world}",
-                   "l2": "flushed before every timed step (256 MB write)"},
+                   "l2": "flushed before every timed step (256 MB write)",
+                   "threads_per_block": res["block_sizes"]},
         "gpu_launches": res["launches"],
         "clocks": res["clocks"],
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",

@@ -242,6 +242,15 @@ int dfsph_adjoint_forward(dfsph_ctx* ctx, float dt, uint32_t n_steps, uint32_t c
 int dfsph_adjoint_backward(dfsph_ctx* ctx, const void* pos_bar, const void* vel_bar, void* pos0_bar,
                            void* vel0_bar, double* xsph_bar, int mem);
 
+/* Launch-shape tuning (no counterpart in the reference). Times the four
+ * neighbour passes (density + alpha, both Jacobi halves, XSPH) at 64, 128 and
+ * 256 threads per block on `steps` steps of the context's own state, each
+ * candidate from the same snapshot, keeps the fastest per pass and restores
+ * the state. block_sizes (may be NULL) receives the threads per block of every
+ * kernel class (DFSPH_KERNEL_CLASSES entries). */
+int dfsph_autotune(dfsph_ctx* ctx, float dt, uint32_t steps, int32_t* block_sizes);
+int dfsph_get_block_sizes(dfsph_ctx* ctx, int32_t* block_sizes);
+
 /* Wait for the context's stream; returns a pending device error if any. */
 int dfsph_synchronize(dfsph_ctx* ctx);
 

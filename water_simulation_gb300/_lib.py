@@ -136,6 +136,8 @@ _SIGNATURES = [
     ("dfsph_profile_enable", ctypes.c_int, [_P, ctypes.c_uint32]),
     ("dfsph_profile_read", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_uint64)]),
+    ("dfsph_autotune", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_uint32, ctypes.POINTER(ctypes.c_int32)]),
+    ("dfsph_get_block_sizes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
     ("dfsph_frame_config_init", ctypes.c_int, [ctypes.POINTER(DfsphFrameConfig)]),
     ("dfsph_step_frames", ctypes.c_int, [_P, ctypes.POINTER(DfsphFrameConfig), ctypes.c_uint32,
                                          ctypes.POINTER(ctypes.c_uint32)]),

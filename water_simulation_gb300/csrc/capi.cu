@@ -263,6 +263,26 @@ int dfsph_synchronize(dfsph_ctx* ctx) {
     });
 }
 
+int dfsph_autotune(dfsph_ctx* ctx, float dt, uint32_t steps, int32_t* block_sizes) {
+    if (!ctx || !(dt > 0.0f) || dt > 1.0e30f || steps == 0 || steps > 1000) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        int b[DFSPH_KERNEL_CLASSES];
+        ctx->solver->autotune(dt, steps, b);
+        if (block_sizes)
+            for (int k = 0; k < DFSPH_KERNEL_CLASSES; ++k) block_sizes[k] = b[k];
+    });
+}
+
+int dfsph_get_block_sizes(dfsph_ctx* ctx, int32_t* block_sizes) {
+    if (!ctx || !block_sizes) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        int b[DFSPH_KERNEL_CLASSES];
+        ctx->solver->block_sizes(b);
+        for (int k = 0; k < DFSPH_KERNEL_CLASSES; ++k) block_sizes[k] = b[k];
+    });
+}
+
 int dfsph_frame_config_init(dfsph_frame_config* fc) {
     if (!fc) return DFSPH_ERR_INVALID_ARGUMENT;
     // TimeStepper::Config (core/include/water/core/timestep.h:10-15) and

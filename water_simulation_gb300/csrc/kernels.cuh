@@ -107,6 +107,24 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
     return t;  // valid in thread 0
 }
 
+// Neighbour passes are instantiated for at most 128 and at most 256 threads
+// per block (LB) and launch with 64, 128 or 256 threads, whichever the
+// autotuner measured fastest for the workload.
+constexpr int MAX_PASS_BLOCK = 256;
+
+// block_sum for any block of whole warps up to MAX_PASS_BLOCK threads.
+__device__ __forceinline__ double block_sum_dyn(double v, double* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) t += sh[w];
+    return t;  // valid in thread 0
+}
+
 // Thread 0 of every block calls this with the block's partial; the last block
 // to arrive sums all partials in block order, so the result does not depend on
 // block scheduling. Decides convergence: stop when (iter >= first_check) and
@@ -159,13 +177,13 @@ template <class R> __device__ __forceinline__ R mul_rn(R a, R b);
 template <> __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 template <> __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 
-template <class R> __device__ __forceinline__ void resolve_dt(StepDt<R>& s) {
-    if (s.dev) {
-        const FrameCtl* f = s.dev;
-        s.dt = R(*((volatile const float*)&f->dt));
-        s.decay = sizeof(R) == sizeof(float) ? R(*((volatile const float*)&f->decay_f))
-                                             : R(*((volatile const double*)&f->decay_d));
-    }
+template <class R> __device__ __forceinline__ R step_dt(const StepDt<R>& s) {
+    return s.dev ? R(*((volatile const float*)&s.dev->dt)) : s.dt;
+}
+template <class R> __device__ __forceinline__ R step_decay(const StepDt<R>& s) {
+    if (!s.dev) return s.decay;
+    return sizeof(R) == sizeof(float) ? R(*((volatile const float*)&s.dev->decay_f))
+                                      : R(*((volatile const double*)&s.dev->decay_d));
 }
 
 __device__ __forceinline__ bool stopped_before(const IterCtl* ctl, u32 iter) {
@@ -546,8 +564,8 @@ struct BoundaryDev {
 // alpha = rho / (|sum m gradW|^2 + sum |m gradW|^2). KAHAN compensates the
 // density sums.
 // ---------------------------------------------------------------------------
-template <class R, bool KAHAN, bool DIAG>
-__global__ void __launch_bounds__(128) density_alpha_kernel(
+template <class R, bool KAHAN, bool DIAG, int LB>
+__global__ void __launch_bounds__(LB) density_alpha_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, R* __restrict__ alpha,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, u32* __restrict__ nbr_f,
     u32* __restrict__ nbr_b, const u32* __restrict__ id, Tape1<R> tp) {
@@ -631,17 +649,17 @@ __global__ void __launch_bounds__(128) density_alpha_kernel(
 // and, because g dt cancels in v'_j - v'_i, the XSPH term of v' equals
 // e^{-d dt} times the XSPH term of v. Reads vr_in, writes vr_out.
 // ---------------------------------------------------------------------------
-template <class R>
-__global__ void __launch_bounds__(128) forces_xsph_kernel(
+template <class R, int LB>
+__global__ void __launch_bounds__(LB) forces_xsph_kernel(
     int n, const R4<R>* __restrict__ xk, const R4<R>* __restrict__ vr_in, R4<R>* __restrict__ vr_out,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, StepDt<R> sd, R eps,
     const R* __restrict__ eps_scene, int do_xsph, R4<R>* __restrict__ tape_v) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    resolve_dt(sd);
-    const R decay = sd.decay;
+    const R dt = step_dt(sd);
+    const R decay = step_decay(sd);
     // g dt rounded on its own, as the host computes it
-    const R gdx = mul_rn(sd.gx, sd.dt), gdy = mul_rn(sd.gy, sd.dt), gdz = mul_rn(sd.gz, sd.dt);
+    const R gdx = mul_rn(sd.gx, dt), gdy = mul_rn(sd.gy, dt), gdz = mul_rn(sd.gz, dt);
     const R4<R> vi = ld(vr_in + i);
     if (tape_v) tape_v[i] = vi;
     R dx = 0, dy = 0, dz = 0;
@@ -678,17 +696,18 @@ __global__ void __launch_bounds__(128) forces_xsph_kernel(
 // max(0, rho_dot). Writes xk_out = (x, kappa / max(rho^2, 1e-9)); xk_in is
 // not written.
 // ---------------------------------------------------------------------------
-template <class R, bool DIVERGENCE, bool REDUCE>
-__global__ void __launch_bounds__(128) pressure_rate_kernel(
+template <class R, bool DIVERGENCE, bool REDUCE, bool DEVLOOP, int LB>
+__global__ void __launch_bounds__(LB) pressure_rate_kernel(
     int n, const R4<R>* __restrict__ xk_in, R4<R>* __restrict__ xk_out,
     const R4<R>* __restrict__ vr, const R* __restrict__ alpha, R* __restrict__ rho_adv,
     R* __restrict__ kap, const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd,
     StepDt<R> sd, double* __restrict__ partials, IterCtl* ctl, u32 iter, u32 first_check, double inv_n,
     double threshold, R4<R>* __restrict__ tape_v, const u32* dev_iter) {
-    __shared__ double sh[4];
-    // Inside a device-resident loop the iteration comes from the device and
-    // even iterations read xk_in / write xk_out, odd ones the other way round.
-    if (dev_iter) {
+    __shared__ double sh[LB / 32];
+    // Inside a device-resident loop (DEVLOOP) the iteration comes from the
+    // device and even iterations read xk_in / write xk_out, odd ones the other
+    // way round.
+    if (DEVLOOP) {
         iter = *((volatile const u32*)dev_iter);
         if (iter & 1u) {
             R4<R>* t = xk_out;
@@ -697,8 +716,7 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
         }
     }
     if (stopped_before(ctl, iter)) return;
-    resolve_dt(sd);
-    const R dt = sd.dt;
+    const R dt = step_dt(sd);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double err = 0;
     if (i < n) {
@@ -752,7 +770,7 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
         xk_out[i] = {pi.x, pi.y, pi.z, k / rmax(rho * rho, R(1e-9))};
     }
     if (REDUCE) {
-        const double t = block_sum<128>(err, sh);
+        const double t = block_sum_dyn(err, sh);
         if (threadIdx.x == 0) finish_reduction(t, partials, ctl, iter, first_check, inv_n, threshold);
     }
 }
@@ -760,18 +778,17 @@ __global__ void __launch_bounds__(128) pressure_rate_kernel(
 // Second half (apply_kappa_kernel dfsph_kernels.cu:237-301):
 // v_i -= dt sum_j m (kfac_i + kfac_j) gradW over fluid and
 // dt sum_b m_b (kfac_i + kappa_i / max(rho0^2, 1e-9)) gradW over the boundary.
-template <class R>
-__global__ void __launch_bounds__(128) pressure_apply_kernel(
+template <class R, bool DEVLOOP, int LB>
+__global__ void __launch_bounds__(LB) pressure_apply_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, const R* __restrict__ kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, const IterCtl* ctl,
     u32 iter, const R4<R>* xk_odd, const u32* dev_iter) {
-    if (dev_iter) {
+    if (DEVLOOP) {
         iter = *((volatile const u32*)dev_iter);
         if (iter & 1u) xk = xk_odd;
     }
     if (stopped_before(ctl, iter)) return;
-    resolve_dt(sd);
-    const R dt = sd.dt;
+    const R dt = step_dt(sd);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R4<R> pi = ld(xk + i);
@@ -825,8 +842,7 @@ __global__ void __launch_bounds__(256) advect_kernel(
     u32* __restrict__ count, IterCtl* ctl, u32* __restrict__ maxv_scene, R4<R>* __restrict__ tape_v,
     unsigned char* __restrict__ tape_mask) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    resolve_dt(sd);
-    const R dt = sd.dt;
+    const R dt = step_dt(sd);
     u32 vbits = 0;
     u32 scene = 0xffffffffu;  // lanes past the end form their own group
     if (i < n) {

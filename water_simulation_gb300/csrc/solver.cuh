@@ -99,7 +99,7 @@ public:
         cell_start_.alloc(keys_ + 1);  // closing entry = n
         n_tiles_ = static_cast<u32>((keys_ + SCAN_TILE - 1) / SCAN_TILE);
         tile_sums_.alloc(n_tiles_ + 1);
-        partials_.alloc(std::max<size_t>(1, (std::max(cap_, 1u) + 127) / 128));
+        partials_.alloc(std::max<size_t>(1, (std::max(cap_, 1u) + 63) / 64));  // blocks of >= 64 threads
         ctl_.alloc(3);
         staging_.alloc(std::max<size_t>(size_t(std::max(cap_, bcap_)) * 6, 6));
         if (bcap_) {
@@ -416,6 +416,60 @@ public:
         *count = c;
     }
 
+    // ------------------------------------------------------------ tuning
+    // Threads per block of the four neighbour passes, measured on the
+    // context's own state: each candidate runs `steps` steps from the same
+    // snapshot with per-class CUDA-event timing, every class keeps its fastest
+    // candidate, and the state (and the iteration controls) are put back.
+    void autotune(float dt, u32 steps, int* chosen) override {
+        if (!have_state_ || n_ == 0) throw Error(DFSPH_ERR_STATE, "no fluid state: call dfsph_set_fluid first");
+        static const int kClasses[4] = {DFSPH_KERNEL_DENSITY_ALPHA, DFSPH_KERNEL_PRESSURE_RATE,
+                                        DFSPH_KERNEL_PRESSURE_APPLY, DFSPH_KERNEL_FORCES_XSPH};
+        static const int kCandidates[3] = {64, 128, 256};
+        const size_t n = n_;
+        if (tune_ck_.n < 2 * n) tune_ck_.alloc(2 * n);
+        if (tune_ctl_.n < 3) tune_ctl_.alloc(3);
+        drop_pending_counts();
+        launch(DFSPH_KERNEL_IO, save_state_kernel<R>, blocks_for(n, 256), 256, int(n), id_[ci_].p, xk_[cx_].p,
+               vr_[cv_].p, tune_ck_.p, tune_ck_.p + n);
+        DFSPH_CUDA(cudaMemcpyAsync(tune_ctl_.p, ctl_.p, 3 * sizeof(IterCtl), cudaMemcpyDeviceToDevice, stream_));
+        const u32 saved_mask = profile_mask_;
+        const bool saved_stepped = stepped_;
+        double best[4] = {1e300, 1e300, 1e300, 1e300};
+        int pick[4] = {bs_[kClasses[0]], bs_[kClasses[1]], bs_[kClasses[2]], bs_[kClasses[3]]};
+        for (const Record& r : records_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+        records_.clear();
+        for (int c = 0; c < 3; ++c) {
+            for (int k = 0; k < 4; ++k) bs_[kClasses[k]] = kCandidates[c];
+            restore_tuning_state();
+            step_once(R(dt), true);  // untimed: first touch of this configuration
+            profile_mask_ = 0;
+            for (int k = 0; k < 4; ++k) profile_mask_ |= 1u << kClasses[k];
+            for (u32 s = 0; s < steps; ++s) step_once(R(dt), true);
+            profile_mask_ = 0;
+            for (int k = 0; k < 4; ++k) {
+                double ms = 0.0;
+                unsigned long long cnt = 0;
+                profile_read(kClasses[k], &ms, &cnt);
+                const double per = cnt ? ms / double(cnt) : 1e300;
+                if (per < best[k]) { best[k] = per; pick[k] = kCandidates[c]; }
+            }
+        }
+        for (int k = 0; k < 4; ++k) bs_[kClasses[k]] = pick[k];
+        restore_tuning_state();
+        DFSPH_CUDA(cudaMemcpyAsync(ctl_.p, tune_ctl_.p, 3 * sizeof(IterCtl), cudaMemcpyDeviceToDevice, stream_));
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        profile_mask_ = saved_mask;
+        stepped_ = saved_stepped;
+        drop_graph();  // captured launches carry the old block sizes
+        if (chosen)
+            for (int k = 0; k < DFSPH_KERNEL_CLASSES; ++k) chosen[k] = bs_[k];
+    }
+
+    void block_sizes(int* out) const override {
+        for (int k = 0; k < DFSPH_KERNEL_CLASSES; ++k) out[k] = bs_[k];
+    }
+
     // ------------------------------------------------------------ frames
     // n_frames frames of CFL substeps (sim_cli's loop, apps/sim_cli/main.cpp
     // :171-181). With graphs enabled and fixed iteration counts each frame is
@@ -607,6 +661,14 @@ public:
     }
 
 private:
+    void restore_tuning_state() {
+        const size_t n = n_;
+        drop_pending_counts();
+        launch(DFSPH_KERNEL_IO, load_state_kernel<R>, blocks_for(n, 256), 256, int(n), (const V4*)tune_ck_.p,
+               (const V4*)(tune_ck_.p + n), xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
+        counts_valid_ = false;
+    }
+
     void check_adjoint_config() const {
         if (scenes_ != 1) throw Error(DFSPH_ERR_STATE, "the adjoint steps one scene");
         if ((cfg_.max_density_iters > 0 && cfg_.eta_density > 0.0f) ||
@@ -747,6 +809,15 @@ private:
             DFSPH_CUDA(cudaEventRecord(b, stream_));
             records_.push_back({kclass, a, b});
         }
+    }
+
+    // A neighbour pass at the tuned block size: the instantiation bounded by
+    // 256 threads for 256-thread blocks, the one bounded by 128 otherwise
+    // (a tighter bound leaves the compiler more registers per thread).
+    template <class K1, class K2, class... A> void launch_pass(int kclass, K1 k128, K2 k256, A... args) {
+        const int b = bs_[kclass];
+        if (b > 128) launch(kclass, k256, blocks_for(n_, b), b, args...);
+        else launch(kclass, k128, blocks_for(n_, b), b, args...);
     }
 
     struct Record { int kclass; cudaEvent_t a, b; };
@@ -1010,15 +1081,15 @@ private:
             R* adv_it = tp ? tp->adv[w] + it * tp->stride : adv_out;
             V4* tv = tp ? tp->v[w] + it * tp->stride : nullptr;
             if (adaptive)
-                launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true>, blocks_for(n, 128), 128, n,
+                launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true, false, 128>, pressure_rate_kernel<R, DIV, true, false, 256>, n,
                        xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl,
                        it, first_check, 1.0 / double(n), thr, tv, (const u32*)nullptr);
             else
-                launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, false>, blocks_for(n, 128), 128, n,
+                launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, false, false, 128>, pressure_rate_kernel<R, DIV, false, false, 256>, n,
                        xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl,
                        it, first_check, 1.0 / double(n), thr, tv, (const u32*)nullptr);
             if (!tp) cx_ ^= 1;
-            launch(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R>, blocks_for(n, 128), 128, n, xout,
+            launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R, false, 128>, pressure_apply_kernel<R, false, 256>, n, xout,
                    vr_[cv_].p, kap_it, cs, g_, phys_, bdev(), sd, ctl, it, (const V4*)nullptr, (const u32*)nullptr);
             launched = it + 1;
             if (adaptive && it >= first_check) {
@@ -1077,10 +1148,10 @@ private:
             V4* xa = xk_[cx_].p;
             V4* xb = xk_[cx_ ^ 1].p;
             const u32* dit = &ctl->iters;
-            launch(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true>, blocks_for(n, 128), 128, n,
+            launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true, true, 128>, pressure_rate_kernel<R, DIV, true, true, 256>, n,
                    (const V4*)xa, xb, vr_[cv_].p, alpha_.p, adv_out, kap_out, cs, g_, phys_, bdev(), sd, partials_.p,
                    ctl, 0u, first_check, 1.0 / double(n), thr, (V4*)nullptr, dit);
-            launch(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R>, blocks_for(n, 128), 128, n, (const V4*)xb,
+            launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R, true, 128>, pressure_apply_kernel<R, true, 256>, n, (const V4*)xb,
                    vr_[cv_].p, kap_out, cs, g_, phys_, bdev(), sd, (const IterCtl*)ctl, 0u, (const V4*)xa, dit);
             launch(DFSPH_KERNEL_OTHER, iteration_control_kernel, 1, 32, ctl, max_iters, h);
         } catch (...) {
@@ -1129,17 +1200,17 @@ private:
         const u32* idn = id_[ci_].p;
         if (cfg_.record_diagnostics) {
             if (kahan)
-                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, true>, blocks_for(n, 128), 128, n,
+                launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, true, 128>, density_alpha_kernel<R, true, true, 256>, n,
                        xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, nbr_f_.p, nbr_b_.p, idn, t1);
             else
-                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, true>, blocks_for(n, 128), 128, n,
+                launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, true, 128>, density_alpha_kernel<R, false, true, 256>, n,
                        xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, nbr_f_.p, nbr_b_.p, idn, t1);
         } else {
             if (kahan)
-                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, false>, blocks_for(n, 128), 128, n,
+                launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, false, 128>, density_alpha_kernel<R, true, false, 256>, n,
                        xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr, idn, t1);
             else
-                launch(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, false>, blocks_for(n, 128), 128, n,
+                launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, false, 128>, density_alpha_kernel<R, false, false, 256>, n,
                        xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr, idn, t1);
         }
         // 3. divergence solve (the reference's plan; 0 iterations = the reference)
@@ -1149,7 +1220,7 @@ private:
                                                     kap_v_.p, rho_dot_.p, cs, tp);
         // 4. gravity + damping + XSPH (dfsph.cu:188-213)
         const bool xsph = explicit_eps_ ? any_xsph_ : cfg_.viscosity > 0.0f;
-        launch(DFSPH_KERNEL_FORCES_XSPH, forces_xsph_kernel<R>, blocks_for(n, 128), 128, n, xk_[cx_].p, vr_[cv_].p,
+        launch_pass(DFSPH_KERNEL_FORCES_XSPH, forces_xsph_kernel<R, 128>, forces_xsph_kernel<R, 256>, n, xk_[cx_].p, vr_[cv_].p,
                vr_[cv_ ^ 1].p, cs, g_, phys_, sd, R(cfg_.viscosity),
                scenes_ > 1 ? (const R*)eps_scene_.p : (const R*)nullptr, xsph ? 1 : 0, tp ? tp->vx : nullptr);
         cv_ ^= 1;
@@ -1240,6 +1311,11 @@ private:
     int last_frame_graph_ = 0;
     cudaStream_t loop_stream_ = nullptr;
     bool iters_on_device_ = false;  // the last step's iteration counts live in IterCtl::iters
+    DevBuf<V4> tune_ck_;
+    DevBuf<IterCtl> tune_ctl_;
+    // threads per block of each kernel class (the neighbour passes are tuned;
+    // the defaults are the choice measured on the 1M-particle dam break)
+    int bs_[DFSPH_KERNEL_CLASSES] = {256, 256, 256, 256, 256, 256, 128, 128, 256, 256, 256, 128};
 };
 
 }  // namespace dfsph

@@ -132,6 +132,17 @@ class Solver:
                                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
         return out[:n_frames]
 
+    def autotune(self, dt: float, steps: int = 3) -> dict:
+        """Pick threads per block of the neighbour passes; returns {kernel class: threads}."""
+        out = (ctypes.c_int32 * _lib.KERNEL_CLASSES)()
+        self._check(self._lib.dfsph_autotune(self._ctx, ctypes.c_float(dt), steps, out))
+        return {_lib.KERNEL_NAMES[k]: int(out[k]) for k in range(_lib.KERNEL_CLASSES)}
+
+    def block_sizes(self) -> dict:
+        out = (ctypes.c_int32 * _lib.KERNEL_CLASSES)()
+        self._check(self._lib.dfsph_get_block_sizes(self._ctx, out))
+        return {_lib.KERNEL_NAMES[k]: int(out[k]) for k in range(_lib.KERNEL_CLASSES)}
+
     def frame_config(self) -> _lib.DfsphFrameConfig:
         fc = _lib.DfsphFrameConfig()
         self._lib.dfsph_frame_config_init(ctypes.byref(fc))
