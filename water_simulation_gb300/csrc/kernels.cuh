@@ -778,19 +778,11 @@ __global__ void __launch_bounds__(LB) pressure_rate_kernel(
 // Second half (apply_kappa_kernel dfsph_kernels.cu:237-301):
 // v_i -= dt sum_j m (kfac_i + kfac_j) gradW over fluid and
 // dt sum_b m_b (kfac_i + kappa_i / max(rho0^2, 1e-9)) gradW over the boundary.
-template <class R, bool DEVLOOP, int LB>
-__global__ void __launch_bounds__(LB) pressure_apply_kernel(
-    int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, const R* __restrict__ kap,
-    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, const IterCtl* ctl,
-    u32 iter, const R4<R>* xk_odd, const u32* dev_iter) {
-    if (DEVLOOP) {
-        iter = *((volatile const u32*)dev_iter);
-        if (iter & 1u) xk = xk_odd;
-    }
-    if (stopped_before(ctl, iter)) return;
-    const R dt = step_dt(sd);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// One particle of the apply pass.
+template <class R>
+__device__ __forceinline__ void apply_particle(int i, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr,
+                                               const R* __restrict__ kap, const u32* __restrict__ cs,
+                                               const GridDev<R>& g, const Phys<R>& p, const BoundaryDev& bd, R dt) {
     const R4<R> pi = ld(xk + i);
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
     R ax = 0, ay = 0, az = 0;
@@ -826,6 +818,22 @@ __global__ void __launch_bounds__(LB) pressure_apply_kernel(
     R4<R> v = vr[i];
     v.x += ax; v.y += ay; v.z += az;
     vr[i] = v;
+}
+
+template <class R, bool DEVLOOP, int LB>
+__global__ void __launch_bounds__(LB) pressure_apply_kernel(
+    int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, const R* __restrict__ kap,
+    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, const IterCtl* ctl,
+    u32 iter, const R4<R>* xk_odd, const u32* dev_iter) {
+    if (DEVLOOP) {
+        iter = *((volatile const u32*)dev_iter);
+        if (iter & 1u) xk = xk_odd;
+    }
+    if (stopped_before(ctl, iter)) return;
+    const R dt = step_dt(sd);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    apply_particle(i, xk, vr, kap, cs, g, p, bd, dt);
 }
 
 // ---------------------------------------------------------------------------
