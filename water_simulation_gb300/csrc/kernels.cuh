@@ -778,11 +778,11 @@ __global__ void __launch_bounds__(LB) pressure_rate_kernel(
 // Second half (apply_kappa_kernel dfsph_kernels.cu:237-301):
 // v_i -= dt sum_j m (kfac_i + kfac_j) gradW over fluid and
 // dt sum_b m_b (kfac_i + kappa_i / max(rho0^2, 1e-9)) gradW over the boundary.
-// One particle of the apply pass.
+// One particle of the apply pass: its velocity after the pressure update.
 template <class R>
-__device__ __forceinline__ void apply_particle(int i, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr,
-                                               const R* __restrict__ kap, const u32* __restrict__ cs,
-                                               const GridDev<R>& g, const Phys<R>& p, const BoundaryDev& bd, R dt) {
+__device__ __forceinline__ R4<R> apply_velocity(int i, const R4<R>* __restrict__ xk, const R4<R>* __restrict__ vr,
+                                                const R* __restrict__ kap, const u32* __restrict__ cs,
+                                                const GridDev<R>& g, const Phys<R>& p, const BoundaryDev& bd, R dt) {
     const R4<R> pi = ld(xk + i);
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
     R ax = 0, ay = 0, az = 0;
@@ -817,7 +817,7 @@ __device__ __forceinline__ void apply_particle(int i, const R4<R>* __restrict__ 
     }
     R4<R> v = vr[i];
     v.x += ax; v.y += ay; v.z += az;
-    vr[i] = v;
+    return v;
 }
 
 template <class R, bool DEVLOOP, int LB>
@@ -833,7 +833,7 @@ __global__ void __launch_bounds__(LB) pressure_apply_kernel(
     const R dt = step_dt(sd);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    apply_particle(i, xk, vr, kap, cs, g, p, bd, dt);
+    vr[i] = apply_velocity(i, xk, vr, kap, cs, g, p, bd, dt);
 }
 
 // ---------------------------------------------------------------------------
@@ -843,61 +843,61 @@ __global__ void __launch_bounds__(LB) pressure_apply_kernel(
 // from xk and written to xk_out (the same buffer, or the other one when that
 // returns the position buffers to where the step found them).
 // ---------------------------------------------------------------------------
+template <class R> struct Domain {
+    R lox, loy, loz, hix, hiy, hiz;
+};
+
+// One particle of the integrator: writes v and x (to xk_out), the next
+// step's cell key and rank when COUNT, the clamp mask when recording; returns
+// the bits of |v| (non-negative floats order as integers).
 template <class R, bool COUNT>
-__global__ void __launch_bounds__(256) advect_kernel(
-    int n, const R4<R>* xk, R4<R>* xk_out, R4<R>* __restrict__ vr, StepDt<R> sd, R lox, R loy, R loz, R hix,
-    R hiy, R hiz, GridDev<R> g, u32* __restrict__ key, u32* __restrict__ rank,
-    u32* __restrict__ count, IterCtl* ctl, u32* __restrict__ maxv_scene, R4<R>* __restrict__ tape_v,
-    unsigned char* __restrict__ tape_mask) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const R dt = step_dt(sd);
-    u32 vbits = 0;
-    u32 scene = 0xffffffffu;  // lanes past the end form their own group
-    if (i < n) {
-        R4<R> v = vr[i];
-        const R4<R> x = xk[i];
-        if (tape_v) tape_v[i] = v;
-        // mask bits (recorded for the adjoint): 0-2 position clamped on x/y/z,
-        // 3-5 velocity component zeroed, 6 speed clamped
-        u32 mk = 0;
-        const R maxv = R(5);
-        const R sp = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
-        if (sp > maxv) {
-            const R s = maxv / sp;
-            v.x *= s; v.y *= s; v.z *= s;
-            mk |= 64u;
-        }
-        R px = x.x + v.x * dt, py = x.y + v.y * dt, pz = x.z + v.z * dt;
-        const R eps = R(1e-3);
-        if (px < lox + eps) { px = lox + eps; mk |= 1u; if (v.x < R(0)) { v.x = R(0); mk |= 8u; } }
-        if (py < loy + eps) { py = loy + eps; mk |= 2u; if (v.y < R(0)) { v.y = R(0); mk |= 16u; } }
-        if (pz < loz + eps) { pz = loz + eps; mk |= 4u; if (v.z < R(0)) { v.z = R(0); mk |= 32u; } }
-        if (px > hix - eps) { px = hix - eps; mk |= 1u; if (v.x > R(0)) { v.x = R(0); mk |= 8u; } }
-        if (py > hiy - eps) { py = hiy - eps; mk |= 2u; if (v.y > R(0)) { v.y = R(0); mk |= 16u; } }
-        if (pz > hiz - eps) { pz = hiz - eps; mk |= 4u; if (v.z > R(0)) { v.z = R(0); mk |= 32u; } }
-        if (tape_mask) tape_mask[i] = static_cast<unsigned char>(mk);
-        vr[i] = {v.x, v.y, v.z, v.w};
-        xk_out[i] = {px, py, pz, R(0)};
-        const float mag = float(sqrt(v.x * v.x + v.y * v.y + v.z * v.z));
-        vbits = __float_as_uint(mag);
-        scene = scene_of(g, i);
-        if (COUNT) {
-            const u32 k = cell_key(px, py, pz, g) + scene * g.cells1;
-            key[i] = k;
-            rank[i] = atomicAdd(count + k, 1u);
-        }
+__device__ __forceinline__ u32 integrate_particle(int i, R4<R> v, const R4<R>& x, R dt, const Domain<R>& d,
+                                                  const GridDev<R>& g, R4<R>* __restrict__ vr, R4<R>* xk_out,
+                                                  u32* __restrict__ key, u32* __restrict__ rank,
+                                                  u32* __restrict__ count, unsigned char* __restrict__ tape_mask) {
+    // mask bits (recorded for the adjoint): 0-2 position clamped on x/y/z,
+    // 3-5 velocity component zeroed, 6 speed clamped
+    u32 mk = 0;
+    const R maxv = R(5);
+    const R sp = sqrt(v.x * v.x + v.y * v.y + v.z * v.z);
+    if (sp > maxv) {
+        const R s = maxv / sp;
+        v.x *= s; v.y *= s; v.z *= s;
+        mk |= 64u;
     }
+    R px = x.x + v.x * dt, py = x.y + v.y * dt, pz = x.z + v.z * dt;
+    const R eps = R(1e-3);
+    if (px < d.lox + eps) { px = d.lox + eps; mk |= 1u; if (v.x < R(0)) { v.x = R(0); mk |= 8u; } }
+    if (py < d.loy + eps) { py = d.loy + eps; mk |= 2u; if (v.y < R(0)) { v.y = R(0); mk |= 16u; } }
+    if (pz < d.loz + eps) { pz = d.loz + eps; mk |= 4u; if (v.z < R(0)) { v.z = R(0); mk |= 32u; } }
+    if (px > d.hix - eps) { px = d.hix - eps; mk |= 1u; if (v.x > R(0)) { v.x = R(0); mk |= 8u; } }
+    if (py > d.hiy - eps) { py = d.hiy - eps; mk |= 2u; if (v.y > R(0)) { v.y = R(0); mk |= 16u; } }
+    if (pz > d.hiz - eps) { pz = d.hiz - eps; mk |= 4u; if (v.z > R(0)) { v.z = R(0); mk |= 32u; } }
+    if (tape_mask) tape_mask[i] = static_cast<unsigned char>(mk);
+    vr[i] = {v.x, v.y, v.z, v.w};
+    xk_out[i] = {px, py, pz, R(0)};
+    if (COUNT) {
+        const u32 k = cell_key(px, py, pz, g) + scene_of(g, i) * g.cells1;
+        key[i] = k;
+        rank[i] = atomicAdd(count + k, 1u);
+    }
+    return __float_as_uint(float(sqrt(v.x * v.x + v.y * v.y + v.z * v.z)));
+}
+
+// Max |v| of the block's particles: per scene (lanes of one scene are
+// contiguous slots; their lowest lane does the one atomic) and overall (one
+// atomic per block into one of MAXV_SLOTS words, since one word for every
+// block serialises the atomics in L2). NaN bits dominate every finite
+// magnitude. Every thread of the block calls it.
+template <int BLOCK>
+__device__ __forceinline__ void max_velocity_epilogue(bool valid, u32 vbits, u32 scene, IterCtl* ctl,
+                                                      u32* __restrict__ maxv_scene) {
+    __shared__ u32 wmax[BLOCK / 32];
     if (maxv_scene) {
-        // per-scene maxima: lanes of one scene (contiguous slots) reduce
-        // together and their lowest lane does the one atomic
         const u32 peers = __match_any_sync(0xffffffffu, scene);
         const u32 m = __reduce_max_sync(peers, vbits);
-        if (i < n && (threadIdx.x & 31) == __ffs(peers) - 1 && m) atomicMax(maxv_scene + scene, m);
+        if (valid && (threadIdx.x & 31) == __ffs(peers) - 1 && m) atomicMax(maxv_scene + scene, m);
     }
-    // max over the block, then one atomic per block into one of MAXV_SLOTS
-    // words (one word for every block would serialise the atomics in L2);
-    // NaN bits dominate every finite magnitude
-    __shared__ u32 wmax[8];
     const u32 m = __reduce_max_sync(0xffffffffu, vbits);
     if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
     __syncthreads();
@@ -906,6 +906,47 @@ __global__ void __launch_bounds__(256) advect_kernel(
         for (int w = 0; w < int(blockDim.x >> 5); ++w) b = max(b, wmax[w]);
         if (b) atomicMax(&ctl->maxv_slot[blockIdx.x % MAXV_SLOTS], b);
     }
+}
+
+template <class R, bool COUNT>
+__global__ void __launch_bounds__(256) advect_kernel(
+    int n, const R4<R>* xk, R4<R>* xk_out, R4<R>* __restrict__ vr, StepDt<R> sd, Domain<R> d, GridDev<R> g,
+    u32* __restrict__ key, u32* __restrict__ rank, u32* __restrict__ count, IterCtl* ctl,
+    u32* __restrict__ maxv_scene, R4<R>* __restrict__ tape_v, unsigned char* __restrict__ tape_mask) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const R dt = step_dt(sd);
+    u32 vbits = 0;
+    u32 scene = 0xffffffffu;  // lanes past the end form their own group
+    if (i < n) {
+        const R4<R> v = vr[i];
+        if (tape_v) tape_v[i] = v;
+        vbits = integrate_particle<R, COUNT>(i, v, xk[i], dt, d, g, vr, xk_out, key, rank, count, tape_mask);
+        scene = scene_of(g, i);
+    }
+    max_velocity_epilogue<256>(i < n, vbits, scene, ctl, maxv_scene);
+}
+
+// The last apply pass of a fixed-iteration density solve fused with the
+// integrator: the particle's new velocity goes straight into the integrator
+// (same values as the two passes: the apply pass's velocity, positions from
+// the same buffer). xk_out is the other position buffer, which nothing in
+// this pass reads.
+template <class R, bool COUNT, int LB>
+__global__ void __launch_bounds__(LB) apply_advect_kernel(
+    int n, const R4<R>* __restrict__ xk, R4<R>* xk_out, R4<R>* __restrict__ vr, const R* __restrict__ kap,
+    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, Domain<R> d,
+    u32* __restrict__ key, u32* __restrict__ rank, u32* __restrict__ count, IterCtl* ctl,
+    u32* __restrict__ maxv_scene) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const R dt = step_dt(sd);
+    u32 vbits = 0;
+    u32 scene = 0xffffffffu;
+    if (i < n) {
+        const R4<R> v = apply_velocity(i, xk, vr, kap, cs, g, p, bd, dt);
+        vbits = integrate_particle<R, COUNT>(i, v, ld(xk + i), dt, d, g, vr, xk_out, key, rank, count, nullptr);
+        scene = scene_of(g, i);
+    }
+    max_velocity_epilogue<LB>(i < n, vbits, scene, ctl, maxv_scene);
 }
 
 }  // namespace dfsph

@@ -811,6 +811,16 @@ private:
         }
     }
 
+    // The integrator's arguments, for a solve that may carry it in its last
+    // iteration (done is set when it did).
+    struct FusedAdvect {
+        Domain<R> d;
+        u32* mvs;
+        int cx0;
+        bool count;
+        bool done;
+    };
+
     // A neighbour pass at the tuned block size: the instantiation bounded by
     // 256 threads for 256-thread blocks, the one bounded by 128 otherwise
     // (a tighter bound leaves the compiler more registers per thread).
@@ -1063,7 +1073,7 @@ private:
     // host additionally stops launching after the device reports convergence.
     template <bool DIV>
     u32 solve(const StepDt<R>& sd, u32 max_iters, float eta, IterCtl* ctl, R* kap_out, R* adv_out, const u32* cs,
-              const StepTape<R>* tp) {
+              const StepTape<R>* tp, FusedAdvect* fa = nullptr) {
         const int n = int(n_);
         const bool adaptive = eta > 0.0f;
         const double thr = double(eta) * double(cfg_.rest_density);
@@ -1089,6 +1099,25 @@ private:
                        xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl,
                        it, first_check, 1.0 / double(n), thr, tv, (const u32*)nullptr);
             if (!tp) cx_ ^= 1;
+            // the last iteration of a fixed-count solve may carry the
+            // integrator, when the other position buffer is the one the step
+            // must end in
+            if (fa && !adaptive && it + 1 == max_iters && cx_ != fa->cx0) {
+                if (fa->count)
+                    launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, apply_advect_kernel<R, true, 128>,
+                                apply_advect_kernel<R, true, 256>, n, (const V4*)xout, xk_[cx_ ^ 1].p, vr_[cv_].p,
+                                (const R*)kap_it, cs, g_, phys_, bdev(), sd, fa->d, key_.p, rank_.p, count_.p, ctl_.p,
+                                fa->mvs);
+                else
+                    launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, apply_advect_kernel<R, false, 128>,
+                                apply_advect_kernel<R, false, 256>, n, (const V4*)xout, xk_[cx_ ^ 1].p, vr_[cv_].p,
+                                (const R*)kap_it, cs, g_, phys_, bdev(), sd, fa->d, key_.p, rank_.p, count_.p, ctl_.p,
+                                fa->mvs);
+                cx_ ^= 1;
+                fa->done = true;
+                launched = it + 1;
+                break;
+            }
             launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R, false, 128>, pressure_apply_kernel<R, false, 256>, n, xout,
                    vr_[cv_].p, kap_it, cs, g_, phys_, bdev(), sd, ctl, it, (const V4*)nullptr, (const u32*)nullptr);
             launched = it + 1;
@@ -1224,25 +1253,31 @@ private:
                vr_[cv_ ^ 1].p, cs, g_, phys_, sd, R(cfg_.viscosity),
                scenes_ > 1 ? (const R*)eps_scene_.p : (const R*)nullptr, xsph ? 1 : 0, tp ? tp->vx : nullptr);
         cv_ ^= 1;
-        // 5. density solve (dfsph.cu:215-260)
-        last_density_launched_ =
-            solve<false>(sd, cfg_.max_density_iters, cfg_.eta_density, ctl_.p + 2, kap_.p, rho_adv_.p, cs, tp);
-        // 6. advect + max |v| (+ next step's cell counts)
-        const R lo[3] = {R(cfg_.domain_min[0]), R(cfg_.domain_min[1]), R(cfg_.domain_min[2])};
-        const R hi[3] = {R(cfg_.domain_max[0]), R(cfg_.domain_max[1]), R(cfg_.domain_max[2])};
+        // 5. density solve (dfsph.cu:215-260), its last iteration fused with
+        // the integrator where possible
+        const Domain<R> dom{R(cfg_.domain_min[0]), R(cfg_.domain_min[1]), R(cfg_.domain_min[2]),
+                            R(cfg_.domain_max[0]), R(cfg_.domain_max[1]), R(cfg_.domain_max[2])};
         u32* mvs = scenes_ > 1 ? maxv_scene_.p : nullptr;
+        FusedAdvect fa{dom, mvs, cx0, count_next, false};
+        last_density_launched_ = solve<false>(sd, cfg_.max_density_iters, cfg_.eta_density, ctl_.p + 2, kap_.p,
+                                              rho_adv_.p, cs, tp, (tp || !fuse_advect_) ? nullptr : &fa);
+        if (fa.done) {
+            counts_valid_ = count_next;
+            return;
+        }
+        // 6. advect + max |v| (+ next step's cell counts)
         const V4* xin = xk_[cx_].p;
         V4* xout = cx_ != cx0 ? xk_[cx_ ^ 1].p : xk_[cx_].p;
         cx_ = cx0;
         if (count_next) {
             launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, true>, blocks_for(n, 256), 256, n, xin, xout, vr_[cv_].p,
-                   sd, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p, mvs,
-                   tp ? tp->va : nullptr, tp ? tp->amask : nullptr);
+                   sd, dom, g_, key_.p, rank_.p, count_.p, ctl_.p, mvs, tp ? tp->va : nullptr,
+                   tp ? tp->amask : nullptr);
             counts_valid_ = true;
         } else {
             launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, false>, blocks_for(n, 256), 256, n, xin, xout, vr_[cv_].p,
-                   sd, lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], g_, key_.p, rank_.p, count_.p, ctl_.p, mvs,
-                   tp ? tp->va : nullptr, tp ? tp->amask : nullptr);
+                   sd, dom, g_, key_.p, rank_.p, count_.p, ctl_.p, mvs, tp ? tp->va : nullptr,
+                   tp ? tp->amask : nullptr);
         }
     }
 
@@ -1311,6 +1346,7 @@ private:
     int last_frame_graph_ = 0;
     cudaStream_t loop_stream_ = nullptr;
     bool iters_on_device_ = false;  // the last step's iteration counts live in IterCtl::iters
+    bool fuse_advect_ = true;  // last density iteration carries the integrator when it can
     DevBuf<V4> tune_ck_;
     DevBuf<IterCtl> tune_ctl_;
     // threads per block of each kernel class (the neighbour passes are tuned;
