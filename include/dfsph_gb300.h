@@ -34,6 +34,7 @@ extern "C" {
 #define DFSPH_ERR_DEVICE_TIMEOUT    5  /* a bounded device wait gave up       */
 #define DFSPH_ERR_NONFINITE         6  /* NaN/Inf detected in the state       */
 #define DFSPH_ERR_NO_DEVICE         7  /* no CUDA device / driver             */
+#define DFSPH_ERR_IO                8  /* a state file could not be read or written */
 
 #define DFSPH_MEM_HOST   0
 #define DFSPH_MEM_DEVICE 1
@@ -241,6 +242,16 @@ int dfsph_adjoint_forward(dfsph_ctx* ctx, float dt, uint32_t n_steps, uint32_t c
  * rollout's final state. */
 int dfsph_adjoint_backward(dfsph_ctx* ctx, const void* pos_bar, const void* vel_bar, void* pos0_bar,
                            void* vel0_bar, double* xsph_bar, int mem);
+
+/* State file (no counterpart in the reference, whose frame files hold positions
+ * only and cannot be resumed from): a header ("DFSPHST1", version, bytes per
+ * real, scene count, fluid and wall counts, the last max |v|), the per-scene fluid counts,
+ * positions and velocities in the working type (original particle order) and
+ * the wall positions as float (input order). dfsph_load_state replaces the
+ * walls and the fluid of a context with the same scene count (reals of the
+ * other width are converted); the next step continues the saved run exactly. */
+int dfsph_save_state(dfsph_ctx* ctx, const char* path);
+int dfsph_load_state(dfsph_ctx* ctx, const char* path);
 
 /* Launch-shape tuning (no counterpart in the reference). Times the four
  * neighbour passes (density + alpha, both Jacobi halves, XSPH) at 64, 128 and

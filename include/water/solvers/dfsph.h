@@ -182,6 +182,37 @@ public:
         return sub;
     }
 
+    // State file of the run (dfsph_save_state): the store's fluid and the
+    // walls. No counterpart in the reference, which cannot resume.
+    void save_state(const std::string& path) {
+        const std::size_t n = fluid_.count();
+        detail::check(dfsph_set_fluid(ctx_.get(), reinterpret_cast<const float*>(fluid_.positions()),
+                                      reinterpret_cast<const float*>(fluid_.velocities()), static_cast<uint32_t>(n),
+                                      DFSPH_MEM_DEVICE),
+                      ctx_.get(), "DFSPHSolver::save_state");
+        detail::check(dfsph_save_state(ctx_.get(), path.c_str()), ctx_.get(), "DFSPHSolver::save_state");
+    }
+    // Resumes a saved run: the store is resized to the saved count (within its
+    // capacity) and takes the saved positions and velocities.
+    void load_state(const std::string& path) {
+        detail::check(dfsph_load_state(ctx_.get(), path.c_str()), ctx_.get(), "DFSPHSolver::load_state");
+        double count = 0.0;
+        detail::check(dfsph_get_scalar(ctx_.get(), DFSPH_SCALAR_FLUID_COUNT, &count), ctx_.get(),
+                      "DFSPHSolver::load_state");
+        const std::size_t n = static_cast<std::size_t>(count);
+        fluid_.resize(n);
+        if (n) {
+            detail::check(dfsph_get_field(ctx_.get(), DFSPH_FIELD_POSITION, fluid_.positions(), n * sizeof(Vec3f),
+                                          DFSPH_MEM_DEVICE),
+                          ctx_.get(), "DFSPHSolver::load_state");
+            detail::check(dfsph_get_field(ctx_.get(), DFSPH_FIELD_VELOCITY, fluid_.velocities(), n * sizeof(Vec3f),
+                                          DFSPH_MEM_DEVICE),
+                          ctx_.get(), "DFSPHSolver::load_state");
+        }
+        grid_dirty_ = true;
+        stats_dirty_ = true;
+    }
+
     // Largest particle speed after the last step (0 before the first step).
     f32 max_velocity() const noexcept {
         refresh_stats();

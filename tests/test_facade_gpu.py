@@ -58,3 +58,28 @@ def test_sim_cli_records_frames(tmp_path):
     assert np.isfinite(p3).all()
     bad = subprocess.run([exe, "--scene", str(tmp_path / "missing.json")], capture_output=True, text=True)
     assert bad.returncode == 1 and "cannot open" in bad.stderr
+
+
+def test_sim_cli_resumes_from_a_state_file(tmp_path):
+    # frames 0..3 in one run equal frames 0..2, a state file, then 2..3 resumed
+    from water_simulation_gb300 import _build
+
+    exe = _build.build_sim_cli()
+    scene = tmp_path / "drop.json"
+    scene.write_text("""{"schema_version": "1.0", "name": "small_drop",
+      "output": {"fps": 30, "frame_range": [0, 3], "format": "bin"},
+      "scene": {"fluid": {"solver": "dfsph", "particle_radius": 0.01, "rest_density": 1000.0,
+                          "viscosity": 0.001, "gravity": [0.0, -9.81, 0.0],
+                          "initial_block_min": [0.42, 0.30, 0.42], "initial_block_max": [0.58, 0.44, 0.58]}}}""")
+
+    def run(*extra):
+        r = subprocess.run([exe, "--scene", str(scene), "--no-vulkan", *extra], capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        return r.stdout
+
+    run("--frames", "0:3", "--record", "--out", str(tmp_path / "a"))
+    run("--frames", "0:2", "--save-state", str(tmp_path / "s.bin"))
+    out = run("--frames", "2:3", "--load-state", str(tmp_path / "s.bin"), "--record", "--out", str(tmp_path / "b"))
+    assert "resumed:" in out
+    assert (tmp_path / "a" / "frame_0003.bin").read_bytes() == (tmp_path / "b" / "frame_0003.bin").read_bytes()

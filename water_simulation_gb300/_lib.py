@@ -19,6 +19,7 @@ ERR_STATE = 4
 ERR_DEVICE_TIMEOUT = 5
 ERR_NONFINITE = 6
 ERR_NO_DEVICE = 7
+ERR_IO = 8
 
 MEM_HOST = 0
 MEM_DEVICE = 1
@@ -137,6 +138,8 @@ _SIGNATURES = [
     ("dfsph_profile_read", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_uint64)]),
     ("dfsph_autotune", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_uint32, ctypes.POINTER(ctypes.c_int32)]),
+    ("dfsph_save_state", ctypes.c_int, [_P, ctypes.c_char_p]),
+    ("dfsph_load_state", ctypes.c_int, [_P, ctypes.c_char_p]),
     ("dfsph_get_block_sizes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
     ("dfsph_frame_config_init", ctypes.c_int, [ctypes.POINTER(DfsphFrameConfig)]),
     ("dfsph_step_frames", ctypes.c_int, [_P, ctypes.POINTER(DfsphFrameConfig), ctypes.c_uint32,

@@ -4,12 +4,14 @@
 //
 //   sim_cli --scene PATH [--frames START:END] [--record] [--out DIR]
 //           [--no-vulkan] [--damping F] [--viscosity F] [--fixed-iters N]
-//           [--host-substeps]
+//           [--host-substeps] [--load-state PATH] [--save-state PATH]
 //
 // By default each frame is one DFSPHSolver::step_frame: with fixed iteration
 // counts (--fixed-iters N: N density iterations, eta = 0) the whole frame is
 // one CUDA graph launch whose substep size is chosen on the device;
 // --host-substeps runs the reference's host loop of next_dt + step instead.
+// --load-state resumes from a state file (positions, velocities, walls)
+// written by --save-state after the last frame.
 //
 // Frame file format (read by the reference's tools/*.py): little-endian u32 N
 // followed by N x 3 float32 positions. --no-vulkan is accepted for
@@ -47,11 +49,14 @@ struct Args {
     float viscosity = -1.0f;
     int fixed_iters = -1;
     bool host_substeps = false;
+    std::string load_state;
+    std::string save_state;
 };
 
 [[noreturn]] void usage_exit(int code) {
     std::puts("Usage: sim_cli --scene PATH [--frames START:END] [--record] "
-              "[--out DIR] [--no-vulkan] [--damping F] [--viscosity F] [--fixed-iters N] [--host-substeps]");
+              "[--out DIR] [--no-vulkan] [--damping F] [--viscosity F] [--fixed-iters N] [--host-substeps] "
+              "[--load-state PATH] [--save-state PATH]");
     std::exit(code);
 }
 
@@ -84,6 +89,10 @@ Args parse(int argc, char** argv) {
             a.fixed_iters = std::stoi(argv[++i]);
         } else if (s == "--host-substeps") {
             a.host_substeps = true;
+        } else if (s == "--load-state" && i + 1 < argc) {
+            a.load_state = argv[++i];
+        } else if (s == "--save-state" && i + 1 < argc) {
+            a.save_state = argv[++i];
         } else if (s == "-h" || s == "--help") {
             usage_exit(0);
         } else {
@@ -183,12 +192,20 @@ int main(int argc, char** argv) try {
 
     water::solvers::DFSPHSolver solver(store, boundary.get(), cfg);
     water::TimeStepper ts;
+    std::vector<water::Vec3f> start = initial;
+    if (!args.load_state.empty()) {
+        solver.load_state(args.load_state);
+        start.resize(store.count());
+        WATER_CUDA_CHECK(cudaMemcpy(start.data(), store.positions(), sizeof(water::Vec3f) * store.count(),
+                                    cudaMemcpyDeviceToHost));
+        std::printf("resumed:      %s (%zu particles)\n", args.load_state.c_str(), store.count());
+    }
 
     if (args.record) {
         make_dirs(args.out_dir);
         char fname[512];
         std::snprintf(fname, sizeof(fname), "%s/frame_%04d.bin", args.out_dir.c_str(), args.frames_start);
-        write_frame(fname, initial.data(), initial.size());
+        write_frame(fname, start.data(), start.size());
     }
 
     const float frame_dt = 1.0f / scene.output.fps;
@@ -215,6 +232,10 @@ int main(int argc, char** argv) try {
             std::snprintf(fname, sizeof(fname), "%s/frame_%04d.bin", args.out_dir.c_str(), f + 1);
             write_frame(fname, host.data(), host.size());
         }
+    }
+    if (!args.save_state.empty()) {
+        solver.save_state(args.save_state);
+        std::printf("saved:        %s\n", args.save_state.c_str());
     }
     std::printf("=== sim_cli OK ===\n");
     return 0;

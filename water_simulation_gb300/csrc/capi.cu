@@ -263,6 +263,22 @@ int dfsph_synchronize(dfsph_ctx* ctx) {
     });
 }
 
+int dfsph_save_state(dfsph_ctx* ctx, const char* path) {
+    if (!ctx || !path) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        ctx->solver->save_state(path);
+    });
+}
+
+int dfsph_load_state(dfsph_ctx* ctx, const char* path) {
+    if (!ctx || !path) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        ctx->solver->load_state(path);
+    });
+}
+
 int dfsph_autotune(dfsph_ctx* ctx, float dt, uint32_t steps, int32_t* block_sizes) {
     if (!ctx || !(dt > 0.0f) || dt > 1.0e30f || steps == 0 || steps > 1000) return DFSPH_ERR_INVALID_ARGUMENT;
     return guarded(ctx, [&] {
@@ -361,6 +377,7 @@ const char* dfsph_status_string(int s) {
         case DFSPH_ERR_DEVICE_TIMEOUT: return "device wait timed out";
         case DFSPH_ERR_NONFINITE: return "non-finite value";
         case DFSPH_ERR_NO_DEVICE: return "no CUDA device";
+        case DFSPH_ERR_IO: return "state file error";
         default: return "unknown status";
     }
 }

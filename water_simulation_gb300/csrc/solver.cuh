@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -187,6 +188,18 @@ public:
     }
 
     void set_fluid_batch(u32 n_scenes, const u32* counts, const float* xyz, const float* vel, int mem) override {
+        const u32 n = check_counts(n_scenes, counts);
+        const float* pos = upload(xyz, vel, n, mem);
+        const float* v = vel ? pos + 3 * size_t(n) : nullptr;
+        if (mem == DFSPH_MEM_DEVICE) { pos = xyz; v = vel; }
+        install_counts(n_scenes, counts, n);
+        if (n == 0) return;
+        launch_import(n, pos, v, xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
+        counts_valid_ = false;
+        have_state_ = true;
+    }
+
+    u32 check_counts(u32 n_scenes, const u32* counts) const {
         if (n_scenes != scenes_)
             throw Error(DFSPH_ERR_INVALID_ARGUMENT, "scene count differs from the context's n_scenes (" +
                                                         std::to_string(scenes_) + ")");
@@ -195,10 +208,12 @@ public:
         if (total > cap_)
             throw Error(DFSPH_ERR_OUT_OF_RANGE, "ParticleStore::resize: count " + std::to_string(total) +
                                                     " exceeds capacity " + std::to_string(cap_));
-        const u32 n = static_cast<u32>(total);
-        const float* pos = upload(xyz, vel, n, mem);
-        const float* v = vel ? pos + 3 * size_t(n) : nullptr;
-        if (mem == DFSPH_MEM_DEVICE) { pos = xyz; v = vel; }
+        return static_cast<u32>(total);
+    }
+
+    // New fluid counts: the slot -> scene map, and the captured graphs when
+    // the counts changed.
+    void install_counts(u32 n_scenes, const u32* counts, u32 n) {
         // captured graphs bake the particle counts in; new values of the same
         // counts keep them valid
         const bool same = n == n_ && scene_counts_.size() == n_scenes &&
@@ -217,10 +232,6 @@ public:
                                        stream_));
             DFSPH_CUDA(cudaStreamSynchronize(stream_));
         }
-        if (n == 0) return;
-        launch_import(n, pos, v, xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
-        counts_valid_ = false;
-        have_state_ = true;
     }
 
     void set_scene_viscosity(const float* eps, u32 n_scenes) override {
@@ -414,6 +425,130 @@ public:
         records_.swap(keep);
         *total_ms = t;
         *count = c;
+    }
+
+    // ------------------------------------------------------------ state file
+    // Header, per-scene counts, positions and velocities in the working type
+    // (original order), wall positions in their input order. Little-endian
+    // fixed-width fields; read back by load_state on either build machine.
+    struct StateHeader {
+        char magic[8];        // "DFSPHST1"
+        u32 version;          // 1
+        u32 real_bytes;       // 4 (float) or 8 (double)
+        u32 n_scenes;
+        u32 n;
+        u32 nb;
+        u32 stepped;          // 1: max_velocity holds the last step's value
+        u32 maxv_bits;        // max |v| after the last step (float bits)
+        u32 reserved;
+    };
+
+    void save_state(const char* path) override {
+        const size_t n = n_;
+        StateHeader h{};
+        std::memcpy(h.magic, "DFSPHST1", 8);
+        h.version = 1;
+        h.real_bytes = sizeof(R);
+        h.n_scenes = scenes_;
+        h.n = have_state_ ? n_ : 0;
+        h.nb = nb_;
+        if (stepped_) {
+            const float mv = float(get_scalar(DFSPH_SCALAR_MAX_VELOCITY));
+            h.stepped = 1u;
+            std::memcpy(&h.maxv_bits, &mv, sizeof(mv));
+        }
+        std::vector<u32> counts(scenes_, 0u);
+        if (h.n) {
+            if (scene_counts_.size() == scenes_) counts = scene_counts_;
+            else counts[0] = n_;
+        }
+        std::vector<R> xv(6 * size_t(h.n));
+        std::vector<float> xb(3 * size_t(nb_));
+        if (h.n) {
+            R* d = static_cast<R*>(scratch_bytes(6 * n * sizeof(R)));
+            launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, R>, blocks_for(n, 256), 256, int(n), id_[ci_].p,
+                   (const V4*)xk_[cx_].p, -1, d);
+            launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, R>, blocks_for(n, 256), 256, int(n), id_[ci_].p,
+                   (const V4*)vr_[cv_].p, -1, d + 3 * n);
+            DFSPH_CUDA(cudaMemcpyAsync(xv.data(), d, 6 * n * sizeof(R), cudaMemcpyDeviceToHost, stream_));
+            DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        }
+        if (nb_) {
+            float* d = static_cast<float*>(scratch_bytes(3 * size_t(nb_) * sizeof(float)));
+            launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, blocks_for(nb_, 256), 256, int(nb_), bid_[0].p,
+                   (const V4*)xb_[0].p, -1, d);
+            DFSPH_CUDA(cudaMemcpyAsync(xb.data(), d, 3 * size_t(nb_) * sizeof(float), cudaMemcpyDeviceToHost,
+                                       stream_));
+            DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        }
+        std::FILE* f = std::fopen(path, "wb");
+        if (!f) throw Error(DFSPH_ERR_IO, std::string("cannot open ") + path + " for writing");
+        bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 &&
+                  std::fwrite(counts.data(), sizeof(u32), counts.size(), f) == counts.size() &&
+                  std::fwrite(xv.data(), sizeof(R), xv.size(), f) == xv.size() &&
+                  std::fwrite(xb.data(), sizeof(float), xb.size(), f) == xb.size();
+        ok = (std::fclose(f) == 0) && ok;
+        if (!ok) throw Error(DFSPH_ERR_IO, std::string("short write to ") + path);
+    }
+
+    void load_state(const char* path) override {
+        std::FILE* f = std::fopen(path, "rb");
+        if (!f) throw Error(DFSPH_ERR_IO, std::string("cannot open ") + path);
+        struct Closer { std::FILE* f; ~Closer() { std::fclose(f); } } closer{f};
+        StateHeader h{};
+        if (std::fread(&h, sizeof(h), 1, f) != 1 || std::memcmp(h.magic, "DFSPHST1", 8) != 0 || h.version != 1)
+            throw Error(DFSPH_ERR_IO, std::string(path) + " is not a DFSPH state file");
+        if (h.real_bytes != 4 && h.real_bytes != 8) throw Error(DFSPH_ERR_IO, "bad real width in state file");
+        if (h.n_scenes != scenes_)
+            throw Error(DFSPH_ERR_INVALID_ARGUMENT, "state file holds " + std::to_string(h.n_scenes) +
+                                                        " scenes, the context " + std::to_string(scenes_));
+        std::vector<u32> counts(h.n_scenes);
+        if (std::fread(counts.data(), sizeof(u32), counts.size(), f) != counts.size())
+            throw Error(DFSPH_ERR_IO, "truncated state file");
+        unsigned long long total = 0;
+        for (u32 c : counts) total += c;
+        if (total != h.n) throw Error(DFSPH_ERR_IO, "inconsistent counts in state file");
+        if (h.nb > bcap_) throw Error(DFSPH_ERR_OUT_OF_RANGE, "state file walls exceed boundary_capacity");
+        const size_t n = h.n;
+        std::vector<R> xv(6 * n);
+        if (h.real_bytes == sizeof(R)) {
+            if (std::fread(xv.data(), sizeof(R), xv.size(), f) != xv.size())
+                throw Error(DFSPH_ERR_IO, "truncated state file");
+        } else if (h.real_bytes == 4) {
+            std::vector<float> t(6 * n);
+            if (std::fread(t.data(), sizeof(float), t.size(), f) != t.size())
+                throw Error(DFSPH_ERR_IO, "truncated state file");
+            for (size_t k = 0; k < t.size(); ++k) xv[k] = R(t[k]);
+        } else {
+            std::vector<double> t(6 * n);
+            if (std::fread(t.data(), sizeof(double), t.size(), f) != t.size())
+                throw Error(DFSPH_ERR_IO, "truncated state file");
+            for (size_t k = 0; k < t.size(); ++k) xv[k] = R(t[k]);
+        }
+        std::vector<float> xb(3 * size_t(h.nb));
+        if (std::fread(xb.data(), sizeof(float), xb.size(), f) != xb.size())
+            throw Error(DFSPH_ERR_IO, "truncated state file");
+        check_counts(h.n_scenes, counts.data());
+        set_boundary(xb.data(), h.nb, DFSPH_MEM_HOST);
+        install_counts(h.n_scenes, counts.data(), h.n);
+        ad_valid_ = false;
+        if (n == 0) return;
+        ensure_adjoint_buffers();
+        R* st = static_cast<R*>(ad_staging(6 * n * sizeof(R)));
+        DFSPH_CUDA(cudaMemcpyAsync(st, xv.data(), 6 * n * sizeof(R), cudaMemcpyHostToDevice, stream_));
+        const int nbk = blocks_for(n, 256);
+        launch(DFSPH_KERNEL_IO, pack3_kernel<R>, nbk, 256, int(n), (const R*)st, xg_.p);
+        launch(DFSPH_KERNEL_IO, pack3_kernel<R>, nbk, 256, int(n), (const R*)(st + 3 * n), vg_.p);
+        launch(DFSPH_KERNEL_IO, load_state_kernel<R>, nbk, 256, int(n), (const V4*)xg_.p, (const V4*)vg_.p,
+               xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
+        // the saved run's max |v|, which sizes the next CFL substep
+        DFSPH_CUDA(cudaMemsetAsync(ctl_.p->maxv_slot, 0, sizeof(ctl_.p->maxv_slot), stream_));
+        if (h.stepped)
+            DFSPH_CUDA(cudaMemcpyAsync(ctl_.p->maxv_slot, &h.maxv_bits, sizeof(u32), cudaMemcpyHostToDevice, stream_));
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        stepped_ = h.stepped != 0;
+        counts_valid_ = false;
+        have_state_ = true;
     }
 
     // ------------------------------------------------------------ tuning

@@ -35,6 +35,8 @@ struct SolverBase {
     virtual void profile_read(int kclass, double* total_ms, unsigned long long* count) = 0;
     virtual void step_frames(const dfsph_frame_config& fc, std::uint32_t n_frames, std::uint32_t* substeps) = 0;
     virtual void autotune(float dt, std::uint32_t steps, int* chosen) = 0;
+    virtual void save_state(const char* path) = 0;
+    virtual void load_state(const char* path) = 0;
     virtual void block_sizes(int* out) const = 0;
     // differentiable rollout; arrays hold the working type (float or double)
     virtual void adjoint_set_state(const void* pos, const void* vel, std::uint32_t n, int mem) = 0;

@@ -132,6 +132,18 @@ class Solver:
                                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))))
         return out[:n_frames]
 
+    def save_state(self, path: str) -> None:
+        self._check(self._lib.dfsph_save_state(self._ctx, str(path).encode()))
+
+    def load_state(self, path: str) -> None:
+        """Replaces walls and fluid with a saved state (see dfsph_save_state)."""
+        self._check(self._lib.dfsph_load_state(self._ctx, str(path).encode()))
+        import struct
+        with open(path, "rb") as f:
+            head = f.read(36)
+        _, _, _, n_scenes, n, nb = struct.unpack("<8sIIIII", head[:28])
+        self.n, self.nb = n, nb
+
     def autotune(self, dt: float, steps: int = 3) -> dict:
         """Pick threads per block of the neighbour passes; returns {kernel class: threads}."""
         out = (ctypes.c_int32 * _lib.KERNEL_CLASSES)()
