@@ -113,6 +113,9 @@ typedef struct dfsph_ctx dfsph_ctx;
                                                  2h of them (counted on demand, last grid) */
 #define DFSPH_SCALAR_FRAME_GRAPH          13  /* 1: the last dfsph_step_frames ran as device-stepped
                                                  graphs; 0: as the host loop */
+#define DFSPH_SCALAR_BOUNDS_VIOLATIONS    14  /* neighbour runs outside their cell_start range seen
+                                                 by the bounds-checked build (-DDFSPH_BOUNDS_CHECK),
+                                                 all contexts of the library; -1 in the normal build */
 
 /* Kernel classes for dfsph_profile_* (bit k of the mask selects class k). */
 #define DFSPH_KERNEL_GRID_COUNT       0   /* cell keys + per-cell counts          */

@@ -17,6 +17,9 @@ ROOT = os.path.dirname(PKG_DIR)
 CSRC = os.path.join(PKG_DIR, "csrc")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libdfsph_gb300.so")
+# the bounds-checked build (every neighbour run validated, violations counted)
+CHECKED_BUILD_DIR = os.path.join(PKG_DIR, "_build_checked")
+CHECKED_LIB_PATH = os.path.join(PKG_DIR, "libdfsph_gb300_checked.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ARCH + [
@@ -67,33 +70,37 @@ def _run(cmd: list[str]) -> None:
         raise RuntimeError("build failed:\n" + " ".join(cmd) + "\n" + r.stdout + r.stderr)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    """Compile libdfsph_gb300.so if any source is newer; returns its path."""
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> str:
+    """Compile libdfsph_gb300.so (or, checked=True, the bounds-checked
+    libdfsph_gb300_checked.so) if any source is newer; returns its path."""
+    lib_path = CHECKED_LIB_PATH if checked else LIB_PATH
+    build_dir = CHECKED_BUILD_DIR if checked else BUILD_DIR
     deps = _sources()
-    if not force and not _stale(LIB_PATH, deps):
-        return LIB_PATH
-    os.makedirs(BUILD_DIR, exist_ok=True)
+    if not force and not _stale(lib_path, deps):
+        return lib_path
+    os.makedirs(build_dir, exist_ok=True)
     nv = nvcc()
     jobs = []
     objs = []
+    defs = ["-DDFSPH_BOUNDS_CHECK"] if checked else []
     for src, extra in CUDA_UNITS:
-        obj = os.path.join(BUILD_DIR, src + ".o")
+        obj = os.path.join(build_dir, src + ".o")
         objs.append(obj)
-        jobs.append([nv] + NVCC_COMMON + extra + ["-c", os.path.join(CSRC, src), "-o", obj])
+        jobs.append([nv] + NVCC_COMMON + defs + extra + ["-c", os.path.join(CSRC, src), "-o", obj])
     for src in CXX_UNITS:
-        obj = os.path.join(BUILD_DIR, src + ".o")
+        obj = os.path.join(build_dir, src + ".o")
         objs.append(obj)
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
                      "-I", os.path.join(ROOT, "include"), "-I", "/usr/local/cuda/include",
                      "-c", os.path.join(CSRC, src), "-o", obj])
     with ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:
         list(ex.map(_run, jobs))
-    tmp = LIB_PATH + ".tmp"
+    tmp = lib_path + ".tmp"
     _run([nv] + ARCH + ["-shared", "-o", tmp] + objs + ["-Xcompiler", "-fPIC"])
-    os.replace(tmp, LIB_PATH)
+    os.replace(tmp, lib_path)
     if verbose:
-        print("built", LIB_PATH)
-    return LIB_PATH
+        print("built", lib_path)
+    return lib_path
 
 
 APPS_DIR = os.path.join(PKG_DIR, "apps")

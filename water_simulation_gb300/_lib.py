@@ -58,6 +58,7 @@ SCALAR_KERNEL_LAUNCHES = 10
 SCALAR_FLAGS = 11
 SCALAR_ACTIVE_BOUNDARY = 12
 SCALAR_FRAME_GRAPH = 13
+SCALAR_BOUNDS_VIOLATIONS = 14
 
 KERNEL_GRID_COUNT = 0
 KERNEL_GRID_SCAN = 1

@@ -121,12 +121,22 @@ __device__ __forceinline__ Centre stencil_centre(R px, R py, R pz, const GridDev
 // visited as 9 runs: for each valid (dx, dy) the cells z-1..z+1 are adjacent
 // keys, so their particles form one contiguous range of sorted slots
 // [cs[first], cs[last+1]). Same candidate set, fewer range lookups.
+#ifdef DFSPH_BOUNDS_CHECK
+// Checked build: every run is validated against the closing entry of its
+// cell_start array (the first slot beyond the grid's particles); a run out of
+// range or reversed is skipped and counted here instead of being read.
+static __device__ u32 g_bounds_violations;
+#endif
+
 template <class R, class F>
 __device__ __forceinline__ void for_each_run(const Centre& c, const GridDev<R>& g,
                                              const u32* __restrict__ cs, F&& f) {
     const int z0 = max(c.z - 1, 0);
     const int z1 = min(c.z + 1, g.nz - 1);
     if (z0 > z1) return;
+#ifdef DFSPH_BOUNDS_CHECK
+    const u32 limit = __ldg(cs + g.cells1);
+#endif
     // not unrolled: one copy of the pair loop keeps the instruction cache warm
 #pragma unroll 1
     for (int dx = -1; dx <= 1; ++dx) {
@@ -140,6 +150,12 @@ __device__ __forceinline__ void for_each_run(const Centre& c, const GridDev<R>& 
                              static_cast<u32>(g.nz);
             const u32 b = __ldg(cs + base + z0);
             const u32 e = __ldg(cs + base + z1 + 1);
+#ifdef DFSPH_BOUNDS_CHECK
+            if (b > e || e > limit) {
+                atomicAdd(&g_bounds_violations, 1u);
+                continue;
+            }
+#endif
             f(b, e);
         }
     }

@@ -17,6 +17,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "adjoint.cuh"
 #include "frames.cuh"
 #include "kernels.cuh"
@@ -40,6 +42,15 @@ template <class T> struct DevBuf {
 };
 
 inline int blocks_for(long long n, int block) { return static_cast<int>((n + block - 1) / block); }
+
+// NVTX range for profilers (Nsight Systems / Compute timelines); a few
+// nanoseconds when no tool is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 template <class R>
 class Solver final : public SolverBase {
@@ -377,6 +388,16 @@ public:
             case DFSPH_SCALAR_KERNEL_LAUNCHES: return double(launches_);
             case DFSPH_SCALAR_ACTIVE_BOUNDARY: return double(active_boundary());
             case DFSPH_SCALAR_FRAME_GRAPH: return double(last_frame_graph_);
+            case DFSPH_SCALAR_BOUNDS_VIOLATIONS: {
+#ifdef DFSPH_BOUNDS_CHECK
+                u32 v = 0;
+                DFSPH_CUDA(cudaStreamSynchronize(stream_));
+                DFSPH_CUDA(cudaMemcpyFromSymbol(&v, g_bounds_violations, sizeof(u32)));
+                return double(v);
+#else
+                return -1.0;
+#endif
+            }
             default: break;
         }
         read_ctl();
@@ -612,6 +633,7 @@ public:
     // whose dt is chosen on the device; otherwise the host runs the
     // reference's loop, reading max |v| back before every substep.
     void step_frames(const dfsph_frame_config& fc, u32 n_frames, u32* substeps) override {
+        const NvtxRange range("dfsph frames");
         if (!have_state_) throw Error(DFSPH_ERR_STATE, "no fluid state: call dfsph_set_fluid first");
         if (n_frames == 0) return;
         std::vector<u32> subs(n_frames, 0u);
@@ -739,6 +761,7 @@ public:
 
     void adjoint_backward(const void* xbar, const void* vbar, void* x0bar, void* v0bar, double* eps_bar,
                           int mem) override {
+        const NvtxRange range("dfsph adjoint backward");
         if (!ad_valid_ || n_ != ad_n_) throw Error(DFSPH_ERR_STATE, "no recorded rollout: call dfsph_adjoint_forward");
         if (cfg_.viscosity != ad_eps_) throw Error(DFSPH_ERR_STATE, "the XSPH coefficient changed since the rollout");
         check_adjoint_config();
@@ -769,10 +792,14 @@ public:
             const u32 s0 = s * ad_every_;
             const u32 cnt = std::min(ad_every_, ad_steps_ - s0);
             restore_checkpoint(s);
-            for (u32 k = 0; k < cnt; ++k) {
-                const StepTape<R> t = tape_at(k);
-                step_once(R(ad_dt_), true, &t);
+            {
+                const NvtxRange replay("adjoint segment replay");
+                for (u32 k = 0; k < cnt; ++k) {
+                    const StepTape<R> t = tape_at(k);
+                    step_once(R(ad_dt_), true, &t);
+                }
             }
+            const NvtxRange reverse("adjoint segment reverse");
             for (u32 k = cnt; k-- > 0;) backward_step(tape_at(k));
         }
         const size_t bytes = 3 * size_t(n) * sizeof(R);
@@ -1346,6 +1373,7 @@ private:
         sd.gz = R(cfg_.gravity[2]);
         sd.dev = fdev;
         const Tape1<R> t1{tp ? tp->x : nullptr, tp ? tp->g : nullptr, tp ? tp->id : nullptr};
+        const NvtxRange step_range("dfsph step");
         // 1. grid build (CellGrid::build, core/src/cell_grid.cu:73-138)
         if (!counts_valid_)
             launch(DFSPH_KERNEL_GRID_COUNT, count_kernel<R>, blocks_for(n, 256), 256, n, xk_[cx_].p, g_, key_.p,
