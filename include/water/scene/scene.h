@@ -32,6 +32,19 @@ struct OutputCfg {
     std::string video = "mp4";
 };
 
+// The design spec's solver_params block (docs/superpowers/specs/
+// 2026-04-23-water-simulation-rebuild-design.md:485-491). The reference's
+// loader does not read it; here it is parsed and `present` tells whether the
+// scene had one. sim_cli applies it only when asked (--solver-params).
+struct SolverParams {
+    bool present = false;
+    u32 max_density_iters = 100;
+    u32 max_divergence_iters = 100;
+    f32 eta_density = 1e-3f;
+    f32 eta_divergence = 1e-3f;
+    f32 cfl_lambda = 0.4f;
+};
+
 struct FluidCfg {
     std::string solver = "dfsph";
     f32 particle_radius = 0.0015f;
@@ -41,6 +54,7 @@ struct FluidCfg {
     Vec3f gravity{0.0f, -9.81f, 0.0f};
     Vec3f initial_block_min{0.4f, 0.05f, 0.4f};
     Vec3f initial_block_max{0.6f, 0.25f, 0.6f};
+    SolverParams solver_params;
 };
 
 struct Scene {
@@ -94,6 +108,17 @@ inline void parse_fluid(const Json& j, FluidCfg& f) {
     f.gravity = read_vec3(fl, "gravity", f.gravity);
     f.initial_block_min = read_vec3(fl, "initial_block_min", f.initial_block_min);
     f.initial_block_max = read_vec3(fl, "initial_block_max", f.initial_block_max);
+    if (fl.contains("solver_params")) {
+        const Json& sp = fl["solver_params"];
+        SolverParams& p = f.solver_params;
+        p.present = true;
+        if (sp.contains("max_density_iters")) p.max_density_iters = static_cast<u32>(sp["max_density_iters"].as_int());
+        if (sp.contains("max_divergence_iters"))
+            p.max_divergence_iters = static_cast<u32>(sp["max_divergence_iters"].as_int());
+        if (sp.contains("eta_density")) p.eta_density = sp["eta_density"].as_float();
+        if (sp.contains("eta_divergence")) p.eta_divergence = sp["eta_divergence"].as_float();
+        if (sp.contains("cfl_lambda")) p.cfl_lambda = sp["cfl_lambda"].as_float();
+    }
 }
 
 }  // namespace detail

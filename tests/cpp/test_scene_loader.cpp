@@ -90,4 +90,20 @@ TEST_CASE("JSON escapes, nesting and numbers") {
     CHECK(check::approx(s.output.fps, 25.0, 1e-7));
 }
 
+TEST_CASE("solver_params block (read here, ignored by the reference's loader)") {
+    const Scene none = parse_scene(R"({"schema_version": "1.0"})");
+    CHECK(!none.fluid.solver_params.present);
+    CHECK(none.fluid.solver_params.max_density_iters == 100u);
+    const Scene s = parse_scene(R"({"schema_version": "1.0", "scene": {"fluid": {"solver_params": {
+        "max_density_iters": 12, "max_divergence_iters": 3, "eta_density": 1e-4,
+        "eta_divergence": 2e-3, "cfl_lambda": 0.25}}}})");
+    CHECK(s.fluid.solver_params.present);
+    CHECK(s.fluid.solver_params.max_density_iters == 12u && s.fluid.solver_params.max_divergence_iters == 3u);
+    CHECK(check::approx(s.fluid.solver_params.eta_density, 1e-4, 1e-6));
+    CHECK(check::approx(s.fluid.solver_params.eta_divergence, 2e-3, 1e-6));
+    CHECK(check::approx(s.fluid.solver_params.cfl_lambda, 0.25, 1e-7));
+    CHECK_THROWS_AS(parse_scene(R"({"schema_version": "1.0", "scene": {"fluid": {"solver_params":
+        {"cfl_lambda": "big"}}}})"), std::runtime_error);
+}
+
 int main() { return check::run_all(); }

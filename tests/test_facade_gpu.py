@@ -83,3 +83,22 @@ def test_sim_cli_resumes_from_a_state_file(tmp_path):
     out = run("--frames", "2:3", "--load-state", str(tmp_path / "s.bin"), "--record", "--out", str(tmp_path / "b"))
     assert "resumed:" in out
     assert (tmp_path / "a" / "frame_0003.bin").read_bytes() == (tmp_path / "b" / "frame_0003.bin").read_bytes()
+
+
+def test_sim_cli_applies_solver_params_on_request(tmp_path):
+    from water_simulation_gb300 import _build
+
+    exe = _build.build_sim_cli()
+    scene = tmp_path / "sp.json"
+    scene.write_text("""{"schema_version": "1.0", "name": "sp",
+      "output": {"fps": 30, "frame_range": [0, 1], "format": "bin"},
+      "scene": {"fluid": {"solver": "dfsph", "particle_radius": 0.01,
+                          "initial_block_min": [0.42, 0.30, 0.42], "initial_block_max": [0.58, 0.44, 0.58],
+                          "solver_params": {"max_density_iters": 20, "max_divergence_iters": 5,
+                                            "eta_density": 1e-4, "eta_divergence": 1e-3, "cfl_lambda": 0.3}}}}""")
+    r = subprocess.run([exe, "--scene", str(scene), "--no-vulkan", "--solver-params"], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "solver_params: density 20 iters" in r.stdout and "cfl 0.30" in r.stdout
+    r = subprocess.run([exe, "--scene", str(scene), "--no-vulkan"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "solver_params:" not in r.stdout  # ignored by default, as the reference does

@@ -5,13 +5,16 @@
 //   sim_cli --scene PATH [--frames START:END] [--record] [--out DIR]
 //           [--no-vulkan] [--damping F] [--viscosity F] [--fixed-iters N]
 //           [--host-substeps] [--load-state PATH] [--save-state PATH]
+//           [--solver-params]
 //
 // By default each frame is one DFSPHSolver::step_frame: with fixed iteration
 // counts (--fixed-iters N: N density iterations, eta = 0) the whole frame is
 // one CUDA graph launch whose substep size is chosen on the device;
 // --host-substeps runs the reference's host loop of next_dt + step instead.
 // --load-state resumes from a state file (positions, velocities, walls)
-// written by --save-state after the last frame.
+// written by --save-state after the last frame. --solver-params applies the
+// scene's solver_params block (iteration caps, tolerances, divergence solve,
+// CFL factor), which the reference parses nowhere.
 //
 // Frame file format (read by the reference's tools/*.py): little-endian u32 N
 // followed by N x 3 float32 positions. --no-vulkan is accepted for
@@ -51,12 +54,13 @@ struct Args {
     bool host_substeps = false;
     std::string load_state;
     std::string save_state;
+    bool solver_params = false;
 };
 
 [[noreturn]] void usage_exit(int code) {
     std::puts("Usage: sim_cli --scene PATH [--frames START:END] [--record] "
               "[--out DIR] [--no-vulkan] [--damping F] [--viscosity F] [--fixed-iters N] [--host-substeps] "
-              "[--load-state PATH] [--save-state PATH]");
+              "[--load-state PATH] [--save-state PATH] [--solver-params]");
     std::exit(code);
 }
 
@@ -93,6 +97,8 @@ Args parse(int argc, char** argv) {
             a.load_state = argv[++i];
         } else if (s == "--save-state" && i + 1 < argc) {
             a.save_state = argv[++i];
+        } else if (s == "--solver-params") {
+            a.solver_params = true;
         } else if (s == "-h" || s == "--help") {
             usage_exit(0);
         } else {
@@ -175,6 +181,19 @@ int main(int argc, char** argv) try {
     cfg.domain_min = {0.0f, 0.0f, 0.0f};
     cfg.domain_max = {1.0f, 1.0f, 1.0f};
     if (args.damping >= 0.0f) cfg.damping = args.damping;
+    water::TimeStepper::Config tsc;
+    if (args.solver_params && scene.fluid.solver_params.present) {
+        const water::scene::SolverParams& sp = scene.fluid.solver_params;
+        cfg.max_density_iters = sp.max_density_iters;
+        cfg.max_divergence_iters = sp.max_divergence_iters;
+        cfg.eta_density = sp.eta_density;
+        cfg.eta_divergence = sp.eta_divergence;
+        cfg.enable_divergence_solver = sp.max_divergence_iters > 0;
+        tsc.cfl_lambda = sp.cfl_lambda;
+        std::printf("solver_params: density %u iters eta %.2g, divergence %u iters eta %.2g, cfl %.2f\n",
+                    sp.max_density_iters, double(sp.eta_density), sp.max_divergence_iters,
+                    double(sp.eta_divergence), double(sp.cfl_lambda));
+    }
     if (args.fixed_iters >= 0) {
         cfg.max_density_iters = static_cast<water::u32>(args.fixed_iters);
         cfg.eta_density = 0.0f;
@@ -191,7 +210,7 @@ int main(int argc, char** argv) try {
                                 cudaMemcpyHostToDevice));
 
     water::solvers::DFSPHSolver solver(store, boundary.get(), cfg);
-    water::TimeStepper ts;
+    water::TimeStepper ts(tsc);
     std::vector<water::Vec3f> start = initial;
     if (!args.load_state.empty()) {
         solver.load_state(args.load_state);
