@@ -1,7 +1,7 @@
 """Benchmark of the DFSPH step: particle-steps/s on the 1M-particle dam break.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload dam1m|dam128k|puddle]
+                    [--workload dam1m|dam128k|dam128k_div|puddle]
 
 A step is one DFSPHSolver::step of the whole scene. The default workload is the
 dam break at scale: an 80 x 160 x 80 column (1,024,000 fluid particles,
@@ -68,7 +68,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dam1m", choices=["dam1m", "dam128k", "puddle"])
+    ap.add_argument("--workload", default="dam1m", choices=["dam1m", "dam128k", "dam128k_div", "puddle"])
     ap.add_argument("--no-ref-cuda", action="store_true", help="skip timing the reference CUDA kernels")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
@@ -87,6 +87,8 @@ def make_scene(name):
         return scenes.dam_break(scale=2, reference_mode=True)
     if name == "dam128k":
         return scenes.dam_break(scale=1, reference_mode=True)
+    if name == "dam128k_div":  # with this build's 2 divergence iterations
+        return scenes.dam_break(scale=1, reference_mode=False)
     sc = scenes.puddle()
     sc.max_density_iters, sc.max_divergence_iters, sc.eta_density, sc.eta_divergence = 4, 0, 0.0, 0.0
     return sc
@@ -538,7 +540,9 @@ def reference_arm(args, rank, world):
     sec = time.perf_counter() - t0
     val = sc.n * done / sec
     return {
-        "impl": "reference", "metric": "particle-steps/s @1M dam break", "value": val, "unit": "particle-steps/s",
+        "impl": "reference",
+        "metric": "particle-steps/s @1M dam break" if args.workload == "dam1m" else f"particle-steps/s @{sc.name}",
+        "value": val, "unit": "particle-steps/s",
         "n_gpus": world, "steps": done, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * sec / max(done, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": sc.name, "particles": sc.n, "boundary_particles": sc.nb,
@@ -569,7 +573,7 @@ def main():
     achieved = alg / (avg_ms * 1e-3) / 1e9 if alg else None
     traffic = NCU_TRAFFIC_PER_PARTICLE.get(dom)
     line = {
-        "metric": "particle-steps/s @1M dam break",
+        "metric": "particle-steps/s @1M dam break" if args.workload == "dam1m" else f"particle-steps/s @{sc.name}",
         "value": res["work"] / (res["ms_total"] * 1e-3),
         "unit": "particle-steps/s",
         "n_gpus": world,
