@@ -149,6 +149,7 @@ public:
 
     ~Solver() override {
         drop_graph();
+        drop_adjoint_graph();
         if (capture_stream_) cudaStreamDestroy(capture_stream_);
         if (loop_stream_) cudaStreamDestroy(loop_stream_);
         if (host_ctl_) cudaFreeHost(host_ctl_);
@@ -169,6 +170,7 @@ public:
         nb_ = n;
         drop_pending_counts();
         drop_graph();
+        drop_adjoint_graph();  // it baked in the wall count
         ad_valid_ = false;  // a recorded rollout ran against the old walls
         if (n == 0) {
             DFSPH_CUDA(cudaMemsetAsync(bcs_.p, 0, (size_t(cells1_) + 1) * sizeof(u32), stream_));
@@ -618,6 +620,7 @@ public:
         profile_mask_ = saved_mask;
         stepped_ = saved_stepped;
         drop_graph();  // captured launches carry the old block sizes
+        drop_adjoint_graph();
         if (chosen)
             for (int k = 0; k < DFSPH_KERNEL_CLASSES; ++k) chosen[k] = bs_[k];
     }
@@ -787,11 +790,18 @@ public:
         DFSPH_CUDA(cudaMemsetAsync(eps_ctr_.p, 0, sizeof(u32), stream_));
         const u32 segs = (ad_steps_ + ad_every_ - 1) / ad_every_;
         ensure_tape(std::min(ad_every_, ad_steps_));
-        drop_graph();
         for (u32 s = segs; s-- > 0;) {
             const u32 s0 = s * ad_every_;
             const u32 cnt = std::min(ad_every_, ad_steps_ - s0);
             restore_checkpoint(s);
+            if (cnt == ad_every_ && profile_mask_ == 0) {
+                // a full segment: one launch of its captured graph
+                ensure_adjoint_graph(cnt);
+                DFSPH_CUDA(cudaGraphLaunch(adj_exec_, stream_));
+                launches_ += adj_kernels_;
+                counts_valid_ = true;  // the last replayed step counted the next one's cells
+                continue;
+            }
             {
                 const NvtxRange replay("adjoint segment replay");
                 for (u32 k = 0; k < cnt; ++k) {
@@ -882,7 +892,68 @@ private:
     }
     void ensure_tape(u32 steps) {
         const size_t need = tape_step_bytes() * steps;
-        if (tape_.n < need) tape_.alloc(need);
+        if (tape_.n < need) {
+            drop_adjoint_graph();  // its replays write the old records
+            tape_.alloc(need);
+        }
+    }
+
+    // Graph of one full segment of the backward pass: the k replayed steps
+    // with their records, then the k reverse steps. Steps leave the buffer
+    // parity unchanged and the records sit at fixed addresses, so one capture
+    // serves every full segment (and every backward pass with the same k, n,
+    // dt and XSPH coefficient). The checkpoint restore before it runs outside.
+    void ensure_adjoint_graph(u32 cnt) {
+        if (adj_exec_ && adj_len_ == cnt && adj_n_ == n_ && adj_dt_ == ad_dt_ && adj_eps_ == ad_eps_ &&
+            cx_ == adj_cx_ && cv_ == adj_cv_ && ci_ == adj_ci_)
+            return;
+        drop_adjoint_graph();
+        if (!capture_stream_) DFSPH_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
+        const cudaStream_t caller = stream_;
+        const unsigned long long k0 = graph_kernels_;
+        const bool counted = counts_valid_;
+        const int cx = cx_, cv = cv_, ci = ci_;
+        DFSPH_CUDA(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal));
+        stream_ = capture_stream_;
+        capturing_ = true;
+        try {
+            for (u32 k = 0; k < cnt; ++k) {
+                const StepTape<R> t = tape_at(k);
+                step_once(R(ad_dt_), true, &t);
+            }
+            for (u32 k = cnt; k-- > 0;) backward_step(tape_at(k));
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(capture_stream_, &g);
+            if (g) cudaGraphDestroy(g);
+            cudaGetLastError();
+            capturing_ = false;
+            stream_ = caller;
+            counts_valid_ = counted;
+            graph_kernels_ = k0;
+            cx_ = cx; cv_ = cv; ci_ = ci;
+            throw;
+        }
+        capturing_ = false;
+        stream_ = caller;
+        counts_valid_ = counted;
+        DFSPH_CUDA(cudaStreamEndCapture(capture_stream_, &adj_graph_));
+        if (cx_ != cx || cv_ != cv || ci_ != ci) throw Error(DFSPH_ERR_STATE, "a step changed buffer parity");
+        DFSPH_CUDA(cudaGraphInstantiate(&adj_exec_, adj_graph_, 0));
+        adj_kernels_ = graph_kernels_ - k0;
+        graph_kernels_ = k0;
+        adj_len_ = cnt;
+        adj_n_ = n_;
+        adj_dt_ = ad_dt_;
+        adj_eps_ = ad_eps_;
+        adj_cx_ = cx_; adj_cv_ = cv_; adj_ci_ = ci_;
+    }
+
+    void drop_adjoint_graph() {
+        if (adj_exec_) cudaGraphExecDestroy(adj_exec_);
+        if (adj_graph_) cudaGraphDestroy(adj_graph_);
+        adj_exec_ = nullptr;
+        adj_graph_ = nullptr;
     }
     StepTape<R> tape_at(u32 k) {
         const size_t np = tape_stride();
@@ -1492,6 +1563,12 @@ private:
     float ad_dt_ = 0.0f, ad_eps_ = 0.0f;
     DevBuf<V4> ck_;
     DevBuf<unsigned char> tape_, ad_staging_;
+    cudaGraph_t adj_graph_ = nullptr;
+    cudaGraphExec_t adj_exec_ = nullptr;
+    u32 adj_len_ = 0, adj_n_ = 0;
+    float adj_dt_ = 0.0f, adj_eps_ = 0.0f;
+    int adj_cx_ = 0, adj_cv_ = 0, adj_ci_ = 0;
+    unsigned long long adj_kernels_ = 0;
     DevBuf<V4> xg_, vg_, xbar_, vbar_[2], xr_, xq_, gq_;
     DevBuf<R> rhobar_, alphabar_;
     DevBuf<double> eps_part_, eps_acc_;
