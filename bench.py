@@ -602,6 +602,18 @@ def main():
                      "active_boundary_particles": res["nb_active"]},
         "kernel_share_warmup": res["warmup_share"],
     }
+    # the whole step against the same peak: compulsory bytes of one step
+    # N (192 + 84 I) + 4 (C + 1) + 16 N_b,active (1 + 2 I), I = solver
+    # iterations per step (x, v, rho, alpha, kappa and the grid arrays moved
+    # once per pass that needs them)
+    fixed = (sc.max_density_iters == 0 or sc.eta_density == 0) and (sc.max_divergence_iters == 0 or
+                                                                    sc.eta_divergence == 0)
+    if fixed:  # adaptive solves run a data-dependent number of iterations
+        iters = sc.max_density_iters + sc.max_divergence_iters
+        b_step = sc.n * (192 + 84 * iters) + 4 * (cells + 1) + 16 * res["nb_active"] * (1 + 2 * iters)
+        step_gbs = b_step * args.steps * world / (res["ms_total"] * 1e-3) / 1e9
+        line["step_roofline"] = {"bytes_per_step": b_step, "iterations_per_step": iters, "achieved": step_gbs,
+                                 "peak": hbm, "unit": "GB/s", "frac": step_gbs / hbm}
     if "e2e" in res:
         line["e2e"] = res["e2e"]
     if rank == 0 and not args.no_cpu:
