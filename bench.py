@@ -29,6 +29,10 @@ frames     sim_cli's frame loop on the puddle block: substeps chosen on the
            device inside one graph launch per frame, against the host loop.
 adjoint    the differentiable drop (32,768 particles, 200 steps, checkpoint
            every 20): backward time over forward time.
+lbvh       SpatialAccel::build on the workload's fluid positions: this
+           build's dfsph_lbvh_build (+ boxes) and dfsph_lbvh_refit against the
+           reference's own kernels under its restated orchestration, outputs
+           compared bit for bit.
 ref_cuda   the reference's own CUDA kernels (compiled from its sources for
            sm_103a, oracle/_ref) under its restated host orchestration, timed on
            the same GPU in the same run.
@@ -77,6 +81,7 @@ def parse():
     ap.add_argument("--no-precision", action="store_true", help="skip the FP32 vs FP64 field errors")
     ap.add_argument("--no-frames", action="store_true", help="skip the device-stepped frame timing")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default 128-thread neighbour passes")
+    ap.add_argument("--no-lbvh", action="store_true", help="skip the LBVH build/refit timing")
     return ap.parse_args()
 
 
@@ -494,6 +499,78 @@ def cpu_sample(sc, steps, threads=0):
             "ms_per_step": 1e3 * sec / steps}
 
 
+def bench_lbvh(sc, reps=20, warmup=3):
+    """dfsph_lbvh_build / dfsph_lbvh_refit on the fluid positions of the
+    workload (scene box = the domain), CUDA events over `reps` launches after
+    `warmup`; the reference's SpatialAccel::build on the same input when its
+    kernels are present, with codes, permutation, children, parents and leaf
+    boxes compared."""
+    import ctypes
+
+    import torch
+
+    from water_simulation_gb300 import _lib
+
+    lib = _lib.load()
+    n = sc.n
+    dev = "cuda"
+    x = torch.tensor(sc.fluid, device=dev)
+    m = max(n - 1, 1)
+    codes = torch.empty(n, dtype=torch.int32, device=dev)
+    idx = torch.empty(n, dtype=torch.int32, device=dev)
+    left = torch.empty(m, dtype=torch.int32, device=dev)
+    right = torch.empty(m, dtype=torch.int32, device=dev)
+    parent = torch.empty(2 * n - 1, dtype=torch.int32, device=dev)
+    boxes = torch.empty((2 * n - 1, 6), dtype=torch.float32, device=dev)
+    scratch = torch.empty(m, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream()
+    st = ctypes.c_void_p(stream.cuda_stream)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    smin, smax = _lib.fvec3(sc.domain_min), _lib.fvec3(sc.domain_max)
+
+    def build():
+        assert lib.dfsph_lbvh_build(P(x), n, smin, smax, ctypes.c_float(0.0), P(codes), P(idx), P(left), P(right),
+                                    P(parent), P(boxes), P(scratch), st) == 0
+
+    def refit():
+        assert lib.dfsph_lbvh_refit(P(x), n, ctypes.c_float(0.0), P(idx), P(left), P(right), P(parent), P(boxes),
+                                    P(scratch), st) == 0
+
+    def timed(f):
+        for _ in range(warmup):
+            f()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            f()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    build_ms = timed(build)
+    refit_ms = timed(refit)
+    build()
+    torch.cuda.synchronize()
+    res = {"workload": f"{sc.name} fluid positions", "particles": n, "build_ms": build_ms, "refit_ms": refit_ms,
+           "build_particles_per_s": n / (build_ms * 1e-3), "note": "build includes the internal boxes, which the "
+           "reference leaves unbuilt; refit = all boxes on the same topology"}
+    from oracle import reference as R
+
+    if not R.available():
+        res["reference"] = {"unavailable": "reference kernels (oracle/_ref fatbins) not present"}
+        return res
+    (rc, ri, rl, rr, rp, rb), ref_ms = R.lbvh_build(sc.fluid, sc.domain_min, sc.domain_max, reps=reps)
+    u = lambda t: t.cpu().numpy().view(np.uint32)  # noqa: E731
+    same = (np.array_equal(u(codes), rc) and np.array_equal(u(idx), ri) and np.array_equal(u(left), rl) and
+            np.array_equal(u(right), rr) and np.array_equal(u(parent)[1:], rp[1:]) and
+            np.array_equal(boxes.cpu().numpy()[n - 1:], rb))
+    res["reference"] = {"build_ms": ref_ms, "speedup": ref_ms / build_ms, "bit_exact": bool(same),
+                        "kind": "reference kernels from its sources, sm_103a, same GPU (stream-ordered allocations "
+                                "and CUB radix sort as SpatialAccel::build)"}
+    return res
+
+
 def bench_ref_cuda(sc, steps):
     from oracle import oracle as O
     from oracle import reference as R
@@ -644,6 +721,11 @@ def main():
                                                             graphed["backward_over_forward"])}
         except Exception as e:
             line["adjoint"] = {"unavailable": str(e)[:200]}
+    if rank == 0 and not args.no_lbvh:
+        try:
+            line["lbvh"] = bench_lbvh(sc)
+        except Exception as e:
+            line["lbvh"] = {"unavailable": str(e)[:200]}
     if rank == 0 and not args.no_ref_cuda:
         try:
             line["ref_cuda"] = bench_ref_cuda(sc, 3 if sc.n > 500000 else 10)

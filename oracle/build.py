@@ -3,12 +3,14 @@
 * liboracle.so      - the C++/OpenMP restatement in dfsph_oracle.cpp (g++).
 * _ref/*.fatbin     - the reference's own kernels, compiled from the reference
                       sources where they lie (solvers/dfsph/src/dfsph_kernels.cu,
-                      core/src/cell_grid.cu) with the reference's flags
-                      (-use_fast_math, CMakeLists.txt:56) for sm_103a. Only
+                      core/src/cell_grid.cu, core/src/spatial_accel.cu) with
+                      the reference's flags (-use_fast_math,
+                      CMakeLists.txt:56) for sm_103a. Only
                       possible where the reference tree exists; the fatbins are
                       device code, so they run on the Arm GPU machine unchanged.
 * _ref/libref_runner.so - ref_runner.cu: host orchestration restating
-                      DFSPHSolver / CellGrid::build around those fatbins (nvcc,
+                      DFSPHSolver / CellGrid::build / SpatialAccel::build
+                      around those fatbins (nvcc,
                       built wherever it runs).
 Nothing from the reference is copied into this repository; _ref/ is ignored.
 """
@@ -26,6 +28,7 @@ RUNNER_LIB = os.path.join(REF_OUT, "libref_runner.so")
 FATBINS = {
     "dfsph_kernels.fatbin": ("solvers/dfsph/src/dfsph_kernels.cu", ["core/include", "solvers/dfsph/include"]),
     "cell_grid.fatbin": ("core/src/cell_grid.cu", ["core/include"]),
+    "spatial_accel.fatbin": ("core/src/spatial_accel.cu", ["core/include"]),
 }
 REFERENCE_ROOT = os.environ.get("WATER_REFERENCE_ROOT", "/root/reference")
 

@@ -380,6 +380,92 @@ struct Runner {
 
 thread_local std::string g_err;
 
+// SpatialAccel (core/include/water/core/spatial_accel.h:19-53) around the
+// reference's own kernels from core/src/spatial_accel.cu. build() restates
+// SpatialAccel::build (spatial_accel.cu:110-179): the member buffers are
+// replaced by fresh stream-ordered allocations on every build, the Morton
+// codes of the positions normalised by the scene box, a CUB radix sort of
+// (code, index) over bits [0, 30) into two temporary buffers, two device
+// copies back, the internal nodes (Karras 2012) and the leaf boxes with
+// radius 0. Internal boxes and the root's parent are left unwritten there.
+struct AccelBox { Vec3f min, max; };
+
+struct Lbvh {
+    Module mod;
+    CUfunction morton = nullptr, internal = nullptr, leaves = nullptr;
+    Buf<u32> codes, idx, left, right, parent;
+    Buf<AccelBox> boxes;
+    size_t leaf_count = 0;
+
+    // DeviceBuffer<T>(count, stream) move-assigned over the member: the new
+    // allocation is made before the old one is released
+    template <class T> static void renew(Buf<T>& b, size_t n) {
+        Buf<T> t(n);
+        b = std::move(t);
+    }
+
+    Lbvh(const Lbvh&) = delete;
+    Lbvh& operator=(const Lbvh&) = delete;
+    ~Lbvh() {
+        cudaDeviceSynchronize();
+        if (mod.mod) cuModuleUnload(mod.mod);
+    }
+
+    explicit Lbvh(const std::string& dir) {
+        RT(cudaFree(nullptr));  // primary context
+        mod.load(dir + "/spatial_accel.fatbin");
+        const std::string a = "water::(anonymous namespace)::";
+        morton = mod.get(a + "compute_morton");
+        internal = mod.get(a + "build_internal_nodes");
+        leaves = mod.get(a + "init_leaf_aabbs");
+    }
+
+    void build(const Vec3f* pos, size_t count, Vec3f smin, Vec3f smax) {
+        if (count < 2) {  // spatial_accel.cu:112-125
+            leaf_count = count;
+            if (count == 1) {
+                renew(idx, 1);
+                renew(boxes, 1);
+                const u32 zero = 0;
+                RT(cudaMemcpyAsync(idx.p, &zero, sizeof(u32), cudaMemcpyHostToDevice, 0));
+            }
+            return;
+        }
+        leaf_count = count;
+        int n_internal = int(count) - 1;
+        renew(codes, count);
+        renew(idx, count);
+        renew(left, size_t(n_internal));
+        renew(right, size_t(n_internal));
+        renew(parent, count + size_t(n_internal));
+        renew(boxes, count + size_t(n_internal));
+        const Vec3f ext{smax.x - smin.x, smax.y - smin.y, smax.z - smin.z};
+        Vec3f inv{ext.x > 0 ? 1.0f / ext.x : 0.0f, ext.y > 0 ? 1.0f / ext.y : 0.0f,
+                  ext.z > 0 ? 1.0f / ext.z : 0.0f};
+        {
+            void* a[] = {(void*)&pos, &codes.p, &idx.p, &count, &smin, &inv};
+            launch(morton, unsigned((count + 255) / 256), 256, a);
+        }
+        Buf<u32> sk(count), sv(count);
+        size_t bytes = 0;
+        RT(cub::DeviceRadixSort::SortPairs(nullptr, bytes, codes.p, sk.p, idx.p, sv.p, int(count), 0, 30, 0));
+        Buf<unsigned char> temp(bytes);
+        RT(cub::DeviceRadixSort::SortPairs(temp.p, bytes, codes.p, sk.p, idx.p, sv.p, int(count), 0, 30, 0));
+        RT(cudaMemcpyAsync(codes.p, sk.p, count * sizeof(u32), cudaMemcpyDeviceToDevice, 0));
+        RT(cudaMemcpyAsync(idx.p, sv.p, count * sizeof(u32), cudaMemcpyDeviceToDevice, 0));
+        int n_leaves = int(count);
+        {
+            void* a[] = {&codes.p, &left.p, &right.p, &parent.p, &n_leaves};
+            launch(internal, unsigned((n_internal + 255) / 256), 256, a);
+        }
+        float radius = 0.0f;
+        {
+            void* a[] = {(void*)&pos, &idx.p, &boxes.p, &n_internal, &n_leaves, &radius};
+            launch(leaves, unsigned((n_leaves + 255) / 256), 256, a);
+        }
+    }
+};
+
 }  // namespace
 
 extern "C" {
@@ -473,6 +559,58 @@ int ref_get(void* h, int field, void* out) {
             case 14: if (r->bg) cp(r->bg->sorted.p, r->nb * 4); return 0;
             default: g_err = "unsupported field"; return 2;
         }
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return 1;
+    }
+}
+
+// SpatialAccel::build on n host positions (xyz[n][3]) and the scene box.
+// Host outputs, each may be NULL: codes[n], sorted index[n], left/right[n-1],
+// parent[2n-1] (the root's entry is whatever the allocation held) and the
+// leaf boxes leaf_boxes[n][6] (min xyz, max xyz). Then `reps` further builds
+// of the same input between CUDA events on stream 0: *ms = their mean.
+int ref_lbvh(const char* fatbin_dir, const float* xyz, u32 n, const float* smin, const float* smax, u32* codes,
+             u32* idx, u32* left, u32* right, u32* parent, float* leaf_boxes, u32 reps, double* ms) {
+    try {
+        Lbvh b(fatbin_dir);
+        Buf<Vec3f> pos(std::max<size_t>(n, 1));
+        if (n) RT(cudaMemcpy(pos.p, xyz, size_t(n) * sizeof(Vec3f), cudaMemcpyHostToDevice));
+        const Vec3f lo{smin[0], smin[1], smin[2]}, hi{smax[0], smax[1], smax[2]};
+        b.build(pos.p, n, lo, hi);
+        RT(cudaDeviceSynchronize());
+        auto cp = [](void* dst, const void* src, size_t bytes) {
+            if (dst && bytes) RT(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+        };
+        if (n >= 2) {
+            cp(codes, b.codes.p, size_t(n) * 4);
+            cp(idx, b.idx.p, size_t(n) * 4);
+            cp(left, b.left.p, size_t(n - 1) * 4);
+            cp(right, b.right.p, size_t(n - 1) * 4);
+            cp(parent, b.parent.p, size_t(2 * n - 1) * 4);
+            cp(leaf_boxes, b.boxes.p + (n - 1), size_t(n) * sizeof(AccelBox));
+        } else if (n == 1) {
+            cp(idx, b.idx.p, 4);
+        }
+        if (ms) {
+            *ms = 0.0;
+            if (reps) {
+                cudaEvent_t e0, e1;
+                RT(cudaEventCreate(&e0));
+                RT(cudaEventCreate(&e1));
+                RT(cudaEventRecord(e0, 0));
+                for (u32 r = 0; r < reps; ++r) b.build(pos.p, n, lo, hi);
+                RT(cudaEventRecord(e1, 0));
+                RT(cudaEventSynchronize(e1));
+                float t = 0;
+                RT(cudaEventElapsedTime(&t, e0, e1));
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                *ms = double(t) / reps;
+            }
+        }
+        RT(cudaDeviceSynchronize());
+        return 0;
     } catch (const std::exception& e) {
         g_err = e.what();
         return 1;

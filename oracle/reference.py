@@ -40,6 +40,8 @@ def load():
         L.ref_get.argtypes = [P, ctypes.c_int, P]
         L.ref_scalar.restype = ctypes.c_double
         L.ref_scalar.argtypes = [P, ctypes.c_int]
+        L.ref_lbvh.argtypes = [ctypes.c_char_p, P, ctypes.c_uint32, P, P, P, P, P, P, P, P, ctypes.c_uint32,
+                               ctypes.POINTER(ctypes.c_double)]
         _lib = L
     return _lib
 
@@ -109,3 +111,29 @@ class ReferenceRun:
 
     def last_density_iters(self):
         return int(self._L.ref_scalar(self._h, 2))
+
+
+def lbvh_build(xyz, smin, smax, reps: int = 0):
+    """The reference's SpatialAccel::build (core/src/spatial_accel.cu:110-179)
+    on its own kernels: (codes, sorted index, left, right, parent, leaf boxes
+    [n, 6]) as numpy arrays in the reference's node numbering, plus the mean
+    milliseconds of `reps` further builds (0.0 when reps = 0). parent[0] (the
+    root) is not written by the reference and is returned as found."""
+    L = load()
+    xyz = np.ascontiguousarray(xyz, dtype=np.float32).reshape(-1, 3)
+    n = xyz.shape[0]
+    codes = np.zeros(max(n, 1), np.uint32)
+    idx = np.zeros(max(n, 1), np.uint32)
+    left = np.zeros(max(n - 1, 1), np.uint32)
+    right = np.zeros(max(n - 1, 1), np.uint32)
+    parent = np.zeros(max(2 * n - 1, 1), np.uint32)
+    boxes = np.zeros((max(n, 1), 6), np.float32)
+    lo = np.asarray(smin, np.float32)
+    hi = np.asarray(smax, np.float32)
+    ms = ctypes.c_double(0.0)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    if L.ref_lbvh(_build.REF_OUT.encode(), p(xyz), n, p(lo), p(hi), p(codes), p(idx), p(left), p(right), p(parent),
+                  p(boxes), reps, ctypes.byref(ms)) != 0:
+        raise RuntimeError("reference lbvh: " + L.ref_last_error().decode())
+    return (codes[:n], idx[:n], left[: max(n - 1, 0)], right[: max(n - 1, 0)], parent[: max(2 * n - 1, 0)],
+            boxes[:n]), ms.value

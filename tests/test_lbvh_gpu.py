@@ -86,3 +86,29 @@ def test_cohesion_kernel_matches_oracle():
     ref = np.array([O.cohesion_C(float(v), float(np.float32(l))) for v in r])
     g = out.cpu().numpy().astype(np.float64)
     assert np.abs(g - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("n,seed", [(1, 5), (2, 6), (9, 7), (5000, 8), (400_000, 9)])
+def test_lbvh_build_matches_reference_kernels(n, seed):
+    """The reference's own SpatialAccel kernels (compiled from its sources)
+    under its build orchestration: codes, permutation, children, parents (the
+    reference leaves the root's unwritten) and leaf boxes (radius 0) equal
+    dfsph_lbvh_build's bit for bit."""
+    from oracle import reference as R
+
+    if not R.available():
+        pytest.skip("reference kernels (oracle/_ref) not built")
+    rng = np.random.default_rng(seed)
+    xyz = rng.uniform(-0.05, 1.05, size=(n, 3)).astype(np.float32)
+    if n > 100:
+        xyz[: n // 5] = xyz[1]  # equal codes
+    lo, hi = (0.0, -0.2, 0.1), (1.0, 1.3, 0.9)
+    (gc, gi, gl, gr, gp, gb), _ = gpu_lbvh(xyz, lo, hi, 0.0)
+    (rc, ri, rl, rr, rp, rb), _ = R.lbvh_build(xyz, lo, hi)
+    assert np.array_equal(gi, ri)
+    if n < 2:
+        return
+    assert np.array_equal(gc, rc)
+    assert np.array_equal(gl, rl) and np.array_equal(gr, rr)
+    assert np.array_equal(gp[1:], rp[1:])
+    assert np.array_equal(gb[n - 1:], rb)
