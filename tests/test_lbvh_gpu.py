@@ -112,3 +112,23 @@ def test_lbvh_build_matches_reference_kernels(n, seed):
     assert np.array_equal(gl, rl) and np.array_equal(gr, rr)
     assert np.array_equal(gp[1:], rp[1:])
     assert np.array_equal(gb[n - 1:], rb)
+
+
+def test_lbvh_refit_unaligned_boxes():
+    """A box array that is only 4-byte aligned takes the arrival-count refit;
+    its boxes equal the oracle's as the aligned path's do."""
+    import torch
+
+    rng = np.random.default_rng(12)
+    n = 50_000
+    xyz = rng.uniform(0, 1, size=(n, 3)).astype(np.float32)
+    (oc, oi, *_), (x, idx, left, right, parent, boxes, scratch) = gpu_lbvh(xyz, (0, 0, 0), (1, 1, 1), 0.002)
+    raw = torch.zeros(6 * (2 * n - 1) + 1, dtype=torch.float32, device="cuda")
+    shifted = raw[1:]  # 4 bytes past an aligned base
+    st = torch.cuda.current_stream().cuda_stream
+    assert _lib.load().dfsph_lbvh_refit(_ptr(x), n, ctypes.c_float(0.002), _ptr(idx), _ptr(left), _ptr(right),
+                                        _ptr(parent), _ptr(shifted), _ptr(scratch), ctypes.c_void_p(st)) == 0
+    torch.cuda.synchronize()
+    _, _, _, _, _, ob = O.lbvh_build(xyz, (0, 0, 0), (1, 1, 1), 0.002, codes=oc, sorted_idx=oi)
+    assert np.array_equal(shifted.cpu().numpy().reshape(-1, 6), ob)
+    assert np.array_equal(boxes.cpu().numpy(), ob)

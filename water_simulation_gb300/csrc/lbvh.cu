@@ -13,10 +13,12 @@
 // (sorted slot k) is node n-1+k.
 //
 // Refit: new leaf boxes from moved positions and internal boxes bottom-up on
-// the same topology. Every leaf walks towards the root; at each internal node
-// the first of its two children to arrive stops (atomic arrival count) and the
-// second merges both boxes and goes on. Nothing waits on another thread.
+// the same topology. Every leaf walks towards the root carrying its box in
+// registers; at each internal node the first of its two children to arrive
+// stops (acquire-release arrival count) and the second merges its box with
+// the sibling's and goes on. Nothing waits on another thread.
 #include <cstdint>
+#include <cuda_runtime.h>
 
 #include "../../include/dfsph_gb300.h"
 #include "common.cuh"
@@ -70,6 +72,15 @@ __global__ void __launch_bounds__(256) lbvh_internal_kernel(const u32* __restric
     parent[r] = static_cast<u32>(i);
 }
 
+// Arrival count with acquire-release semantics at device scope: the stores
+// made before it (the arriving child's box) are visible to the thread whose
+// add returns after it, and that thread sees the earlier arrival's stores.
+__device__ __forceinline__ u32 arrive(u32* p) {
+    u32 old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+
 __global__ void __launch_bounds__(256) lbvh_refit_kernel(const float* __restrict__ xyz, int n, float radius,
                                                          const u32* __restrict__ sorted, const u32* __restrict__ left,
                                                          const u32* __restrict__ right, const u32* __restrict__ parent,
@@ -78,22 +89,124 @@ __global__ void __launch_bounds__(256) lbvh_refit_kernel(const float* __restrict
     if (k >= n) return;
     const u32 p = sorted[k];
     const float x = xyz[3 * p], y = xyz[3 * p + 1], z = xyz[3 * p + 2];
-    u32 node = static_cast<u32>(n - 1 + k);
-    float* b = boxes + 6 * size_t(node);
-    b[0] = x - radius; b[1] = y - radius; b[2] = z - radius;
-    b[3] = x + radius; b[4] = y + radius; b[5] = z + radius;
-    __threadfence();
-    node = parent[node];
+    // the box this thread carries up, kept in registers
+    float b0 = x - radius, b1 = y - radius, b2 = z - radius;
+    float b3 = x + radius, b4 = y + radius, b5 = z + radius;
+    u32 child = static_cast<u32>(n - 1 + k);
+    float* o = boxes + 6 * size_t(child);
+    o[0] = b0; o[1] = b1; o[2] = b2; o[3] = b3; o[4] = b4; o[5] = b5;
+    u32 node = parent[child];
     while (node != 0xFFFFFFFFu) {
-        if (atomicAdd(arrivals + node, 1u) == 0u) return;  // the other child finishes this node
-        __threadfence();
-        const volatile float* a = boxes + 6 * size_t(left[node]);
-        const volatile float* c = boxes + 6 * size_t(right[node]);
-        float* o = boxes + 6 * size_t(node);
-        o[0] = fminf(a[0], c[0]); o[1] = fminf(a[1], c[1]); o[2] = fminf(a[2], c[2]);
-        o[3] = fmaxf(a[3], c[3]); o[4] = fmaxf(a[4], c[4]); o[5] = fmaxf(a[5], c[5]);
-        __threadfence();
-        node = parent[node];
+        // topology loads issued before the arrival (nothing writes them), so
+        // their latency overlaps the atomic's
+        const u32 l = left[node], r = right[node], up = parent[node];
+        // the first child to arrive stops; the second merges the two boxes
+        if (arrive(arrivals + node) == 0u) return;
+        const u32 sib = l == child ? r : l;
+        const float* q = boxes + 6 * size_t(sib);
+        // from L2, where the sibling's box was stored before its arrival
+        b0 = fminf(b0, __ldcg(q + 0)); b1 = fminf(b1, __ldcg(q + 1)); b2 = fminf(b2, __ldcg(q + 2));
+        b3 = fmaxf(b3, __ldcg(q + 3)); b4 = fmaxf(b4, __ldcg(q + 4)); b5 = fmaxf(b5, __ldcg(q + 5));
+        o = boxes + 6 * size_t(node);
+        o[0] = b0; o[1] = b1; o[2] = b2; o[3] = b3; o[4] = b4; o[5] = b5;
+        child = node;
+        node = up;
+    }
+}
+
+// Refit without fences, in two phases per warp of 32 consecutive leaves.
+//  1. In the warp: every lane starts at its leaf; lanes whose current nodes
+//     share a parent hold its two children, so they merge by shuffles (the
+//     lower lane goes on, the upper stops) until no two lanes pair up.
+//  2. The lanes left (roots of the warp's complete subtrees) walk on with
+//     three independent exchange walks, one per 8-byte pair of box words
+//     ((min x, min y), (min z, max x), (max y, max z)): a walk swaps its pair
+//     into the parent's slot with one 64-bit atomicExch; getting back the empty
+//     pattern means it arrived first and stops, otherwise it got the sibling's
+//     pair, merges, stores and goes on. The data travels inside the atomic, so
+//     no ordering of other memory operations is needed. Internal slots start
+//     as all-ones words, a NaN pattern that float arithmetic never produces
+//     (its results are canonical NaNs).
+constexpr unsigned long long EMPTY_PAIR = ~0ull;
+
+__device__ __forceinline__ unsigned long long pack_pair(float a, float b) {
+    return static_cast<unsigned long long>(__float_as_uint(a)) |
+           (static_cast<unsigned long long>(__float_as_uint(b)) << 32);
+}
+
+__device__ __forceinline__ unsigned long long* pair_slot(float* boxes, u32 node, int w) {
+    return reinterpret_cast<unsigned long long*>(boxes + 6 * size_t(node) + 2 * w);
+}
+
+__global__ void __launch_bounds__(256) lbvh_refit_pairs_kernel(const float* __restrict__ xyz, int n, float radius,
+                                                               const u32* __restrict__ sorted,
+                                                               const u32* __restrict__ parent, float* boxes) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    bool active = k < n;
+    float b[6] = {0, 0, 0, 0, 0, 0};
+    u32 node = 0, up = 0xFFFFFFFFu;
+    if (active) {
+        const u32 p = sorted[k];
+        const float x = xyz[3 * p], y = xyz[3 * p + 1], z = xyz[3 * p + 2];
+        b[0] = x - radius; b[1] = y - radius; b[2] = z - radius;
+        b[3] = x + radius; b[4] = y + radius; b[5] = z + radius;
+        node = static_cast<u32>(n - 1 + k);
+#pragma unroll
+        for (int w = 0; w < 3; ++w) *pair_slot(boxes, node, w) = pack_pair(b[2 * w], b[2 * w + 1]);
+        up = parent[node];
+    }
+    // 1. pairs inside the warp (node ids < 2^31; idle lanes use unique keys)
+    for (;;) {
+        const bool live = active && up != 0xFFFFFFFFu;
+        const u32 peers = __match_any_sync(0xffffffffu, live ? up : (0x80000000u | static_cast<u32>(lane)));
+        const bool pair = live && __popc(peers) == 2;
+        if (!__any_sync(0xffffffffu, pair)) break;
+        const int other = pair ? __ffs(peers & ~(1u << lane)) - 1 : lane;
+        float o[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) o[c] = __shfl_sync(0xffffffffu, b[c], other);
+        if (pair) {
+            if (lane < other) {
+                b[0] = fminf(b[0], o[0]); b[1] = fminf(b[1], o[1]); b[2] = fminf(b[2], o[2]);
+                b[3] = fmaxf(b[3], o[3]); b[4] = fmaxf(b[4], o[4]); b[5] = fmaxf(b[5], o[5]);
+                node = up;
+#pragma unroll
+                for (int w = 0; w < 3; ++w) *pair_slot(boxes, node, w) = pack_pair(b[2 * w], b[2 * w + 1]);
+                up = parent[node];
+            } else {
+                active = false;
+            }
+        }
+    }
+    if (!active || up == 0xFFFFFFFFu) return;
+    // 2. three exchange walks from the parent of this subtree's root
+    u32 cur[3] = {up, up, up};
+    float pa[3] = {b[0], b[2], b[4]}, pb[3] = {b[1], b[3], b[5]};
+    bool go[3] = {true, true, true};
+    while (go[0] || go[1] || go[2]) {
+        u32 nxt[3];
+        unsigned long long old[3];
+#pragma unroll
+        for (int w = 0; w < 3; ++w) {
+            nxt[w] = go[w] ? parent[cur[w]] : 0xFFFFFFFFu;
+            old[w] = go[w] ? atomicExch(pair_slot(boxes, cur[w], w), pack_pair(pa[w], pb[w])) : EMPTY_PAIR;
+        }
+#pragma unroll
+        for (int w = 0; w < 3; ++w) {
+            if (!go[w]) continue;
+            if (old[w] == EMPTY_PAIR) {  // the sibling's walk finishes this node
+                go[w] = false;
+                continue;
+            }
+            const float oa = __uint_as_float(static_cast<u32>(old[w]));
+            const float ob = __uint_as_float(static_cast<u32>(old[w] >> 32));
+            pa[w] = w <= 1 ? fminf(pa[w], oa) : fmaxf(pa[w], oa);
+            pb[w] = w == 0 ? fminf(pb[w], ob) : fmaxf(pb[w], ob);
+            *pair_slot(boxes, cur[w], w) = pack_pair(pa[w], pb[w]);
+            cur[w] = nxt[w];
+            go[w] = nxt[w] != 0xFFFFFFFFu;
+        }
     }
 }
 
@@ -133,6 +246,13 @@ void lbvh_build(const float* xyz, u32 n, const float smin[3], const float smax[3
 void lbvh_refit(const float* xyz, u32 n, float radius, const u32* sorted, const u32* left, const u32* right,
                 const u32* parent, float* boxes, u32* scratch, cudaStream_t st) {
     if (n == 0) return;
+    if ((reinterpret_cast<uintptr_t>(boxes) & 7u) == 0) {
+        // 8-byte aligned boxes: the exchange walks (internal slots emptied first)
+        if (n > 1) DFSPH_CUDA(cudaMemsetAsync(boxes, 0xFF, size_t(n - 1) * 6 * sizeof(float), st));
+        lbvh_refit_pairs_kernel<<<(n + 255) / 256, 256, 0, st>>>(xyz, int(n), radius, sorted, parent, boxes);
+        DFSPH_LAUNCHED();
+        return;
+    }
     if (n > 1) DFSPH_CUDA(cudaMemsetAsync(scratch, 0, size_t(n - 1) * sizeof(u32), st));
     lbvh_refit_kernel<<<(n + 255) / 256, 256, 0, st>>>(xyz, int(n), radius, sorted, left, right, parent, boxes,
                                                         scratch);

@@ -1,10 +1,21 @@
 // Morton-order variant of the neighbour sort (the reference's SpatialAccel,
 // core/src/spatial_accel.cu:11-40,158-179): 30-bit Morton codes of positions
-// normalised to the scene box, stably sorted. The sort is a least-significant-
-// digit radix sort of four 8-bit passes; each pass histograms 1024-element
-// tiles, scans the digit-major histogram and scatters with a rank that is
-// stable inside the tile (warp match + per-warp digit counts), so equal codes
-// keep ascending particle indices exactly as a stable sort of iota values.
+// normalised to the scene box, stably sorted.
+//
+// The sort is a least-significant-digit radix sort of four 8-bit passes over
+// tiles of 4096 keys, in nine launches:
+//   codes   Morton codes + iota indices, the first pass's per-tile digit
+//           counts (digit-major) and its digit totals;
+//   offsets one warp per digit: digit base from the totals, prefix of the
+//           digit's counts over the tiles -> each tile's scatter offsets;
+//   scatter a rank that is stable inside the tile (each warp ranks its own
+//           slice, then one block-wide pass over the per-warp digit counts)
+//           places the tile's keys in shared memory in digit order;
+//           each digit's run then leaves as consecutive stores, and the next
+//           pass's per-tile counts and totals are gathered on the way (the
+//           tile of a key in the next pass is its destination slot / 4096).
+// Equal codes keep ascending particle indices exactly as a stable sort of iota
+// values does. The last pass writes the caller's arrays directly.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -17,10 +28,14 @@ namespace dfsph {
 namespace {
 
 constexpr int RS_BLOCK = 256;
-constexpr int RS_ROUNDS = 4;
+constexpr int RS_ROUNDS = 16;
 constexpr int RS_TILE = RS_BLOCK * RS_ROUNDS;
-constexpr int RS_BINS = 256;
+constexpr int RS_BITS = 8;
+constexpr int RS_BINS = 1 << RS_BITS;
+constexpr u32 RS_MASK = RS_BINS - 1;
 constexpr int RS_WARPS = RS_BLOCK / 32;
+constexpr int RS_PASSES = 4;
+constexpr u32 NO_DIGIT = 0xFFFFFFFFu;
 
 // Spread the low 10 bits of v so that bit k lands on bit 3k.
 __device__ __forceinline__ u32 spread10(u32 v) {
@@ -38,69 +53,217 @@ __device__ __forceinline__ u32 quant10(float x) {
     return static_cast<u32>(q);
 }
 
-__global__ void __launch_bounds__(256) morton_code_kernel(int n, const float* __restrict__ xyz, float mx, float my,
-                                                          float mz, float ix, float iy, float iz,
-                                                          u32* __restrict__ codes, u32* __restrict__ idx) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const u32 qx = quant10((xyz[3 * i] - mx) * ix);
-    const u32 qy = quant10((xyz[3 * i + 1] - my) * iy);
-    const u32 qz = quant10((xyz[3 * i + 2] - mz) * iz);
-    codes[i] = (spread10(qx) << 2) | (spread10(qy) << 1) | spread10(qz);
-    idx[i] = static_cast<u32>(i);
+// counter_base[value] += 1 for every valid lane, one atomic per distinct
+// value in the warp (coherent inputs put most of a warp on one counter).
+__device__ __forceinline__ void warp_count(u32* counter_base, u32 value, bool valid) {
+    const u32 v = valid ? value : NO_DIGIT;
+    const u32 peers = __match_any_sync(0xffffffffu, v);
+    const u32 lt = (1u << (threadIdx.x & 31)) - 1u;
+    if (valid && (peers & lt) == 0u) atomicAdd(counter_base + value, static_cast<u32>(__popc(peers)));
 }
 
-__global__ void __launch_bounds__(RS_BLOCK) radix_hist_kernel(const u32* __restrict__ keys, int n, int shift,
-                                                              u32* __restrict__ hist, int n_tiles) {
+// Per-block digit counts -> the tile's column of the digit-major histogram
+// and the pass's digit totals.
+__device__ __forceinline__ void flush_tile_counts(const u32* h, u32* hist, int n_tiles, int tile, u32* totals) {
+#pragma unroll
+    for (int j = 0; j < RS_BINS / RS_BLOCK; ++j) {
+        const int d = threadIdx.x + RS_BLOCK * j;
+        const u32 c = h[d];
+        hist[size_t(d) * n_tiles + tile] = c;
+        if (c) atomicAdd(totals + d, c);
+    }
+}
+
+__global__ void __launch_bounds__(RS_BLOCK) morton_codes_kernel(int n, const float* __restrict__ xyz, float mx,
+                                                                float my, float mz, float ix, float iy, float iz,
+                                                                u32* __restrict__ codes, u32* __restrict__ idx,
+                                                                u32* __restrict__ hist, int n_tiles,
+                                                                u32* __restrict__ totals) {
     __shared__ u32 h[RS_BINS];
-    h[threadIdx.x] = 0u;
+#pragma unroll
+    for (int j = 0; j < RS_BINS / RS_BLOCK; ++j) h[threadIdx.x + RS_BLOCK * j] = 0u;
     __syncthreads();
     const int base = blockIdx.x * RS_TILE;
 #pragma unroll
     for (int k = 0; k < RS_ROUNDS; ++k) {
-        const int e = base + k * RS_BLOCK + threadIdx.x;
-        if (e < n) atomicAdd(&h[(keys[e] >> shift) & 0xffu], 1u);
+        const int i = base + k * RS_BLOCK + threadIdx.x;
+        const bool valid = i < n;
+        u32 code = 0;
+        if (valid) {
+            const u32 qx = quant10((xyz[3 * i] - mx) * ix);
+            const u32 qy = quant10((xyz[3 * i + 1] - my) * iy);
+            const u32 qz = quant10((xyz[3 * i + 2] - mz) * iz);
+            code = (spread10(qx) << 2) | (spread10(qy) << 1) | spread10(qz);
+            codes[i] = code;
+            idx[i] = static_cast<u32>(i);
+        }
+        warp_count(h, code & RS_MASK, valid);
     }
     __syncthreads();
-    hist[size_t(threadIdx.x) * n_tiles + blockIdx.x] = h[threadIdx.x];  // digit-major
+    flush_tile_counts(h, hist, n_tiles, blockIdx.x, totals);
 }
 
-__global__ void __launch_bounds__(RS_BLOCK) radix_scatter_kernel(const u32* __restrict__ keys_in,
-                                                                 const u32* __restrict__ vals_in, int n, int shift,
-                                                                 const u32* __restrict__ offs, int n_tiles,
-                                                                 u32* __restrict__ keys_out,
-                                                                 u32* __restrict__ vals_out) {
-    __shared__ u32 run[RS_BINS];
+// hist[d][t] (the pass's counts) becomes the slot of the first key of digit d
+// in tile t: the keys of smaller digits plus those of digit d in earlier
+// tiles. One warp per digit; it also clears the digit's row of the other
+// histogram, which the next scatter fills.
+__global__ void __launch_bounds__(256) radix_offsets_kernel(u32* __restrict__ hist, int n_tiles,
+                                                            const u32* __restrict__ totals,
+                                                            u32* __restrict__ next_hist) {
+    __shared__ u32 tot[RS_BINS];
+#pragma unroll
+    for (int j = 0; j < RS_BINS / 256; ++j) tot[threadIdx.x + 256 * j] = totals[threadIdx.x + 256 * j];
+    __syncthreads();
+    const int d = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    u32 base = 0;
+#pragma unroll
+    for (int j = 0; j < RS_BINS / 32; ++j) {
+        const int k = lane + 32 * j;
+        base += k < d ? tot[k] : 0u;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) base += __shfl_xor_sync(0xffffffffu, base, o);
+    // each lane a contiguous segment of the row: independent loads, then a
+    // warp scan of the segment sums
+    u32* row = hist + size_t(d) * n_tiles;
+    const int per = (n_tiles + 31) / 32;
+    const int t0 = min(lane * per, n_tiles), t1 = min(t0 + per, n_tiles);
+    u32 sum = 0;
+#pragma unroll 8
+    for (int t = t0; t < t1; ++t) sum += row[t];
+    u32 x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const u32 y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    u32 run = base + x - sum;
+#pragma unroll 8
+    for (int t = t0; t < t1; ++t) {
+        const u32 v = row[t];
+        row[t] = run;
+        run += v;
+    }
+    if (next_hist) {
+        u32* nrow = next_hist + size_t(d) * n_tiles;
+        for (int t = lane; t < n_tiles; t += 32) nrow[t] = 0u;  // stores only: nothing waits
+    }
+}
+
+// Each warp ranks its own contiguous 512-key slice of the tile (warp match,
+// a per-warp digit count in shared memory, no block barrier per round); one
+// block-wide pass then turns the per-warp counts into tile-local slots in
+// digit order (digit by digit, warp by warp), so the rank is stable.
+constexpr int RS_SLICE = RS_TILE / RS_WARPS;
+constexpr int RS_SLICE_ROUNDS = RS_SLICE / 32;
+
+__global__ void __launch_bounds__(RS_BLOCK) radix_scatter_kernel(
+    const u32* __restrict__ keys_in, const u32* __restrict__ vals_in, int n, int shift,
+    const u32* __restrict__ offs, int n_tiles, u32* __restrict__ keys_out, u32* __restrict__ vals_out,
+    u32* __restrict__ next_hist, u32* __restrict__ next_totals) {
+    __shared__ u32 start[RS_BINS];   // tile-local slot of the digit's first key
+    __shared__ u32 dst0[RS_BINS];    // global slot of the digit's first key of this tile
     __shared__ u32 wcnt[RS_WARPS][RS_BINS];
+    __shared__ u32 wsum[RS_WARPS];
+    __shared__ u32 ncount[RS_BINS];
+    __shared__ u32 skey[RS_TILE], sval[RS_TILE];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    run[threadIdx.x] = offs[size_t(threadIdx.x) * n_tiles + blockIdx.x];
-    const u32 lt_mask = (1u << lane) - 1u;
     const int base = blockIdx.x * RS_TILE;
-    for (int k = 0; k < RS_ROUNDS; ++k) {
+    const int count = min(RS_TILE, n - base);
+    const int slice = warp * RS_SLICE;
+    // this lane's keys of the warp's slice, all loads in flight at once
+    u32 keys[RS_SLICE_ROUNDS], vals[RS_SLICE_ROUNDS];
 #pragma unroll
-        for (int w = 0; w < RS_WARPS; ++w) wcnt[w][threadIdx.x] = 0u;
-        __syncthreads();
-        const int e = base + k * RS_BLOCK + threadIdx.x;
-        const bool valid = e < n;
-        const u32 key = valid ? keys_in[e] : 0u;
-        const u32 d = valid ? ((key >> shift) & 0xffu) : 0x100u;  // invalid lanes: their own group
+    for (int k = 0; k < RS_SLICE_ROUNDS; ++k) {
+        const int p = slice + k * 32 + lane;
+        keys[k] = p < count ? keys_in[base + p] : 0u;
+        vals[k] = p < count ? vals_in[base + p] : 0u;
+    }
+    ncount[threadIdx.x] = 0u;
+    dst0[threadIdx.x] = offs[size_t(threadIdx.x) * n_tiles + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; ++w) wcnt[w][threadIdx.x] = 0u;
+    __syncthreads();
+    const u32 lt_mask = (1u << lane) - 1u;
+    u32 rank[RS_SLICE_ROUNDS];
+#pragma unroll
+    for (int k = 0; k < RS_SLICE_ROUNDS; ++k) {
+        const bool valid = slice + k * 32 + lane < count;
+        const u32 d = valid ? ((keys[k] >> shift) & RS_MASK) : NO_DIGIT;  // invalid lanes: their own group
         const u32 peers = __match_any_sync(0xffffffffu, d);
-        const u32 rank_w = __popc(peers & lt_mask);
-        if (valid && rank_w == 0) wcnt[warp][d] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            u32 before = 0;
-            for (int w = 0; w < warp; ++w) before += wcnt[w][d];
-            const u32 dst = run[d] + before + rank_w;
-            keys_out[dst] = key;
-            vals_out[dst] = vals_in[e];
+        const int leader = __ffs(peers) - 1;
+        u32 old = 0;
+        if (valid && lane == leader) {
+            old = wcnt[warp][d];
+            wcnt[warp][d] = old + __popc(peers);
         }
-        __syncthreads();
-        u32 tot = 0;
+        rank[k] = __shfl_sync(0xffffffffu, old, leader) + __popc(peers & lt_mask);
+        __syncwarp();
+    }
+    __syncthreads();
+    // digit d (thread d): its tile count, exclusive prefix over digits, then
+    // each warp's first slot of the digit
+    {
+        const int d = threadIdx.x;
+        u32 c = 0;
 #pragma unroll
-        for (int w = 0; w < RS_WARPS; ++w) tot += wcnt[w][threadIdx.x];
-        run[threadIdx.x] += tot;
+        for (int w = 0; w < RS_WARPS; ++w) c += wcnt[w][d];
+        u32 x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
         __syncthreads();
+        u32 run = x - c;
+        for (int w = 0; w < warp; ++w) run += wsum[w];
+        start[d] = run;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; ++w) {
+            const u32 cw = wcnt[w][d];
+            wcnt[w][d] = run;
+            run += cw;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < RS_SLICE_ROUNDS; ++k) {
+        if (slice + k * 32 + lane < count) {
+            const u32 p = wcnt[warp][(keys[k] >> shift) & RS_MASK] + rank[k];
+            skey[p] = keys[k];
+            sval[p] = vals[k];
+        }
+    }
+    __syncthreads();
+    // runs leave in digit order, consecutive threads to consecutive slots
+#pragma unroll 4
+    for (int k = 0; k < RS_ROUNDS; ++k) {
+        const int p = k * RS_BLOCK + threadIdx.x;
+        const bool valid = p < count;
+        const u32 key = valid ? skey[p] : 0u;
+        u32 dst = 0;
+        if (valid) {
+            const u32 d = (key >> shift) & RS_MASK;
+            dst = dst0[d] + (static_cast<u32>(p) - start[d]);
+            keys_out[dst] = key;
+            vals_out[dst] = sval[p];
+        }
+        if (next_hist) {
+            // the next pass's digit and tile of this key
+            const u32 d2 = (key >> (shift + RS_BITS)) & RS_MASK;
+            const u32 t2 = dst / RS_TILE;
+            const u32 cell = (t2 << RS_BITS) | d2;
+            const u32 p2 = __match_any_sync(0xffffffffu, valid ? cell : NO_DIGIT);
+            if (valid && (p2 & lt_mask) == 0u)
+                atomicAdd(next_hist + size_t(d2) * n_tiles + t2, static_cast<u32>(__popc(p2)));
+            warp_count(ncount, d2, valid);
+        }
+    }
+    if (next_hist) {
+        __syncthreads();
+        if (ncount[threadIdx.x]) atomicAdd(next_totals + threadIdx.x, ncount[threadIdx.x]);
     }
 }
 
@@ -117,38 +280,34 @@ void morton_sort(const float* xyz, u32 n, const float smin[3], const float smax[
     }
     const int n_tiles = int((n + RS_TILE - 1) / RS_TILE);
     const size_t m = size_t(RS_BINS) * n_tiles;
-    const u32 scan_tiles_n = u32((m + SCAN_TILE - 1) / SCAN_TILE);
-    const size_t words = 4 * size_t(n) + m /*hist*/ + (m + 1) /*offsets*/ + scan_tiles_n + 1;
+    const size_t words = 4 * size_t(n) + 2 * m /*histograms*/ + RS_PASSES * RS_BINS /*digit totals*/;
     u32* mem = nullptr;
     DFSPH_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&mem), words * sizeof(u32), st));
     u32* ka = mem;
     u32* va = ka + n;
     u32* kb = va + n;
     u32* vb = kb + n;
-    u32* hist = vb + n;
-    u32* offs = hist + m;
-    u32* tsum = offs + m + 1;
-    const int nb = int((n + 255) / 256);
-    morton_code_kernel<<<nb, 256, 0, st>>>(int(n), xyz, smin[0], smin[1], smin[2], inv[0], inv[1], inv[2], ka, va);
+    u32* hist[2] = {vb + n, vb + n + m};
+    u32* totals = vb + n + 2 * m;
+    DFSPH_CUDA(cudaMemsetAsync(totals, 0, RS_PASSES * RS_BINS * sizeof(u32), st));
+    morton_codes_kernel<<<n_tiles, RS_BLOCK, 0, st>>>(int(n), xyz, smin[0], smin[1], smin[2], inv[0], inv[1],
+                                                      inv[2], ka, va, hist[0], n_tiles, totals);
     DFSPH_LAUNCHED();
-    for (int pass = 0; pass < 4; ++pass) {
-        const int shift = 8 * pass;
-        radix_hist_kernel<<<n_tiles, RS_BLOCK, 0, st>>>(ka, int(n), shift, hist, n_tiles);
+    for (int pass = 0; pass < RS_PASSES; ++pass) {
+        const bool last = pass == RS_PASSES - 1;
+        u32* cur = hist[pass & 1];
+        u32* nxt = last ? nullptr : hist[(pass + 1) & 1];
+        radix_offsets_kernel<<<RS_BINS / 8, 256, 0, st>>>(cur, n_tiles, totals + pass * RS_BINS, nxt);
         DFSPH_LAUNCHED();
-        // exclusive scan of the digit-major histogram (it is cleared on the way)
-        scan_tile_sums<<<scan_tiles_n, SCAN_BLOCK, 0, st>>>(hist, u32(m), tsum);
-        DFSPH_LAUNCHED();
-        scan_tile_offsets<<<1, 1024, 0, st>>>(tsum, scan_tiles_n, offs + m, nullptr, 0, nullptr, 0);
-        DFSPH_LAUNCHED();
-        scan_tiles<<<scan_tiles_n, SCAN_BLOCK, 0, st>>>(hist, u32(m), tsum, offs);
-        DFSPH_LAUNCHED();
-        radix_scatter_kernel<<<n_tiles, RS_BLOCK, 0, st>>>(ka, va, int(n), shift, offs, n_tiles, kb, vb);
+        // the last pass writes the caller's arrays where given
+        u32* ko = (last && sorted_codes) ? sorted_codes : kb;
+        u32* vo = (last && sorted_idx) ? sorted_idx : vb;
+        radix_scatter_kernel<<<n_tiles, RS_BLOCK, 0, st>>>(ka, va, int(n), RS_BITS * pass, cur, n_tiles, ko, vo,
+                                                           nxt, last ? nullptr : totals + (pass + 1) * RS_BINS);
         DFSPH_LAUNCHED();
         std::swap(ka, kb);
         std::swap(va, vb);
     }
-    if (sorted_codes) DFSPH_CUDA(cudaMemcpyAsync(sorted_codes, ka, size_t(n) * sizeof(u32), cudaMemcpyDeviceToDevice, st));
-    if (sorted_idx) DFSPH_CUDA(cudaMemcpyAsync(sorted_idx, va, size_t(n) * sizeof(u32), cudaMemcpyDeviceToDevice, st));
     DFSPH_CUDA(cudaFreeAsync(mem, st));
 }
 
