@@ -12,6 +12,8 @@
 // consecutive 16-byte records that the warp's other particles share in L1.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 
 namespace dfsph {
@@ -38,6 +40,25 @@ template <class R> __device__ __forceinline__ R4<R> ld(const R4<R>* p) { return 
 template <> __device__ __forceinline__ R4<float> ld(const R4<float>* p) {
     const float4 v = __ldg(reinterpret_cast<const float4*>(p));
     return {v.x, v.y, v.z, v.w};
+}
+// A record that other threads of the same launch write between grid barriers
+// (a persistent solve): a coherent cached load (ld.global.ca), never the
+// read-only path, which the compiler may pick for a plain load through a
+// const __restrict__ pointer. The barrier's device-scope fence orders it after
+// the writes of the previous phase.
+template <class R> __device__ __forceinline__ R4<R> ld_coh(const R4<R>* p);
+template <> __device__ __forceinline__ R4<float> ld_coh(const R4<float>* p) {
+    const float4 v = __ldca(reinterpret_cast<const float4*>(p));
+    return {v.x, v.y, v.z, v.w};
+}
+template <> __device__ __forceinline__ R4<double> ld_coh(const R4<double>* p) {
+    const double2* q = reinterpret_cast<const double2*>(p);
+    const double2 a = __ldca(q), b = __ldca(q + 1);
+    return {a.x, a.y, b.x, b.y};
+}
+template <class R, bool COHERENT> __device__ __forceinline__ R4<R> ld_rec(const R4<R>* p) {
+    if (COHERENT) return ld_coh(p);
+    return ld(p);
 }
 
 // ---------------------------------------------------------------------------
@@ -687,6 +708,83 @@ __global__ void __launch_bounds__(LB) forces_xsph_kernel(
     vr_out[i] = {vi.x * decay + gdx + dx, vi.y * decay + gdy + dy, vi.z * decay + gdz + dz, vi.w};
 }
 
+// One particle of the rate pass: rho_adv, kappa and (x, kappa / rho^2) of
+// particle i; returns its error term (the reduction's input).
+template <class R, bool DIVERGENCE, bool COHERENT = false>
+__device__ __forceinline__ double rate_particle(int i, const R4<R>* __restrict__ xk_in, R4<R>* __restrict__ xk_out,
+                                                const R4<R>* __restrict__ vr, const R* __restrict__ alpha,
+                                                R* __restrict__ rho_adv, R* __restrict__ kap,
+                                                const u32* __restrict__ cs, const GridDev<R>& g, const Phys<R>& p,
+                                                const BoundaryDev& bd, R dt, R4<R>* __restrict__ tape_v) {
+    double err = 0;
+    const R4<R> pi = ld_rec<R, COHERENT>(xk_in + i);
+    const R4<R> vi = ld_rec<R, COHERENT>(vr + i);
+    if (tape_v) tape_v[i] = vi;
+    const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
+    R rd = 0;
+    auto pair = [&](const R4<R>& pj, const R4<R>& vj) {
+        const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        R rinv;
+        const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
+        const R f = grad_factor(r, rinv, p);
+        rd += f * ((vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz);
+    };
+    if (COHERENT) {
+        // latency-bound: a column's records four at a time, summed in order
+        for_each_run_ahead(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+            for (u32 j0 = b; j0 < e; j0 += 4) {
+                R4<R> pj[4], vj[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const u32 j = min(j0 + u, e - 1);
+                    pj[u] = ld_coh(xk_in + j);
+                    vj[u] = ld_coh(vr + j);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (j0 + u < e) pair(pj[u], vj[u]);
+            }
+        });
+    } else {
+        for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+#pragma unroll 2
+            for (u32 j = b; j < e; ++j) pair(ld(xk_in + j), ld(vr + j));
+        });
+    }
+    rd *= p.mass;
+    if (bd.has && boundary_near(c, g, bd.mask)) {
+        const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
+        R rb = 0;
+        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+            for (u32 j = b; j < e; ++j) {
+                const R4<R> pj = ld(xb + j);
+                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+                R rinv;
+                const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
+                rb += pj.w * grad_factor(r, rinv, p) * (vi.x * rx + vi.y * ry + vi.z * rz);
+            }
+        });
+        rd += rb;
+    }
+    const R rho = vi.w;
+    R k;
+    if (!DIVERGENCE) {
+        const R rp = rho + dt * rd;
+        rho_adv[i] = rp;
+        const R over = rmax(rp - p.rho0, R(0));
+        k = over * alpha[i] / (dt * dt);
+        err = double(over);
+    } else {
+        const R s = rmax(rd, R(0));
+        rho_adv[i] = rd;  // the divergence solver's rho_dot scratch
+        k = s * alpha[i] / dt;
+        err = double(s);
+    }
+    kap[i] = k;
+    xk_out[i] = {pi.x, pi.y, pi.z, k / rmax(rho * rho, R(1e-9))};
+    return err;
+}
+
 // ---------------------------------------------------------------------------
 // Jacobi pressure iteration, first half: rho_dot = sum_j m (v_i - v_j).gradW
 // (fluid) + sum_b m_b v_i.gradW (density_change_kernel dfsph_kernels.cu:176-232).
@@ -719,56 +817,8 @@ __global__ void __launch_bounds__(LB) pressure_rate_kernel(
     const R dt = step_dt(sd);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double err = 0;
-    if (i < n) {
-        const R4<R> pi = ld(xk_in + i);
-        const R4<R> vi = ld(vr + i);
-        if (tape_v) tape_v[i] = vi;
-        const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
-        R rd = 0;
-        for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
-#pragma unroll 2
-            for (u32 j = b; j < e; ++j) {
-                const R4<R> pj = ld(xk_in + j);
-                const R4<R> vj = ld(vr + j);
-                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-                R rinv;
-                const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
-                const R f = grad_factor(r, rinv, p);
-                rd += f * ((vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz);
-            }
-        });
-        rd *= p.mass;
-        if (bd.has && boundary_near(c, g, bd.mask)) {
-            const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
-            R rb = 0;
-            for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
-                for (u32 j = b; j < e; ++j) {
-                    const R4<R> pj = ld(xb + j);
-                    const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-                    R rinv;
-                    const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
-                    rb += pj.w * grad_factor(r, rinv, p) * (vi.x * rx + vi.y * ry + vi.z * rz);
-                }
-            });
-            rd += rb;
-        }
-        const R rho = vi.w;
-        R k;
-        if (!DIVERGENCE) {
-            const R rp = rho + dt * rd;
-            rho_adv[i] = rp;
-            const R over = rmax(rp - p.rho0, R(0));
-            k = over * alpha[i] / (dt * dt);
-            err = double(over);
-        } else {
-            const R s = rmax(rd, R(0));
-            rho_adv[i] = rd;  // the divergence solver's rho_dot scratch
-            k = s * alpha[i] / dt;
-            err = double(s);
-        }
-        kap[i] = k;
-        xk_out[i] = {pi.x, pi.y, pi.z, k / rmax(rho * rho, R(1e-9))};
-    }
+    if (i < n)
+        err = rate_particle<R, DIVERGENCE>(i, xk_in, xk_out, vr, alpha, rho_adv, kap, cs, g, p, bd, dt, tape_v);
     if (REDUCE) {
         const double t = block_sum_dyn(err, sh);
         if (threadIdx.x == 0) finish_reduction(t, partials, ctl, iter, first_check, inv_n, threshold);
@@ -779,23 +829,37 @@ __global__ void __launch_bounds__(LB) pressure_rate_kernel(
 // v_i -= dt sum_j m (kfac_i + kfac_j) gradW over fluid and
 // dt sum_b m_b (kfac_i + kappa_i / max(rho0^2, 1e-9)) gradW over the boundary.
 // One particle of the apply pass: its velocity after the pressure update.
-template <class R>
+template <class R, bool COHERENT = false>
 __device__ __forceinline__ R4<R> apply_velocity(int i, const R4<R>* __restrict__ xk, const R4<R>* __restrict__ vr,
                                                 const R* __restrict__ kap, const u32* __restrict__ cs,
                                                 const GridDev<R>& g, const Phys<R>& p, const BoundaryDev& bd, R dt) {
-    const R4<R> pi = ld(xk + i);
+    const R4<R> pi = ld_rec<R, COHERENT>(xk + i);
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
     R ax = 0, ay = 0, az = 0;
-    for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
-        for (u32 j = b; j < e; ++j) {
-            const R4<R> pj = ld(xk + j);
-            const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-            R rinv;
-            const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
-            const R f = (pi.w + pj.w) * grad_factor(r, rinv, p);
-            ax += f * rx; ay += f * ry; az += f * rz;
-        }
-    });
+    auto pair = [&](const R4<R>& pj) {
+        const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+        R rinv;
+        const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
+        const R f = (pi.w + pj.w) * grad_factor(r, rinv, p);
+        ax += f * rx; ay += f * ry; az += f * rz;
+    };
+    if (COHERENT) {
+        // latency-bound: a column's records four at a time, summed in order
+        for_each_run_ahead(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+            for (u32 j0 = b; j0 < e; j0 += 4) {
+                R4<R> pj[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) pj[u] = ld_coh(xk + min(j0 + u, e - 1));
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (j0 + u < e) pair(pj[u]);
+            }
+        });
+    } else {
+        for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+            for (u32 j = b; j < e; ++j) pair(ld(xk + j));
+        });
+    }
     const R sf = -dt * p.mass;
     ax *= sf; ay *= sf; az *= sf;
     if (bd.has && boundary_near(c, g, bd.mask)) {
@@ -834,6 +898,63 @@ __global__ void __launch_bounds__(LB) pressure_apply_kernel(
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     vr[i] = apply_velocity(i, xk, vr, kap, cs, g, p, bd, dt);
+}
+
+// A whole adaptive Jacobi solve in one cooperative launch, every block
+// resident (small scenes, where a solve of many short passes is bound by
+// launches): per iteration the rate pass, a grid barrier, the stop decision,
+// the apply pass and a second barrier. Every block sums the block partials in
+// block order, as finish_reduction does, so all blocks take the same decision
+// and stop after the same iteration. Even iterations read positions from xa
+// and write (x, kappa / rho^2) to xb, odd ones the other way round, as the
+// graph-resident loop does. Launched with the rate pass's block size, so the
+// partial sums, and with them the iteration count, equal the per-launch
+// solve's. Records written inside the launch are read with ld_coh.
+constexpr int JACOBI_SOLVE_MAX_BLOCKS = 256;
+template <class R, bool DIV, int LB>
+__global__ void __launch_bounds__(LB) jacobi_solve_kernel(
+    int n, R4<R>* xa, R4<R>* xb, R4<R>* vr, const R* __restrict__ alpha, R* rho_adv, R* kap,
+    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, double* partials,
+    IterCtl* ctl, u32 max_iters, u32 first_check, double inv_n, double threshold) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double sh[LB / 32];
+    __shared__ double part[JACOBI_SOLVE_MAX_BLOCKS];
+    __shared__ int stop;
+    const R dt = step_dt(sd);
+    const int i = blockIdx.x * LB + threadIdx.x;
+    u32 it = 0;
+    while (it < max_iters) {
+        const R4<R>* xin = (it & 1u) ? xb : xa;
+        R4<R>* xout = (it & 1u) ? xa : xb;
+        double err = 0;
+        if (i < n)
+            err = rate_particle<R, DIV, true>(i, xin, xout, vr, alpha, rho_adv, kap, cs, g, p, bd, dt, nullptr);
+        const double t = block_sum_dyn(err, sh);
+        if (threadIdx.x == 0) partials[blockIdx.x] = t;
+        grid.sync();
+        // all partials in flight at once, then the sum in block order
+        for (u32 b = threadIdx.x; b < gridDim.x; b += LB) part[b] = __ldcg(partials + b);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0;
+            for (u32 b = 0; b < gridDim.x; ++b) s += part[b];
+            const bool done = it >= first_check && s * inv_n < threshold;
+            stop = done ? 1 : 0;
+            if (blockIdx.x == 0) {
+                ctl->err_sum = s;
+                if (done) ctl->stop_iter = it;
+                if (!(s == s)) ctl->flags |= 1u;
+            }
+        }
+        __syncthreads();
+        const bool done = stop != 0;
+        if (i < n) vr[i] = apply_velocity<R, true>(i, xout, vr, kap, cs, g, p, bd, dt);
+        ++it;
+        grid.sync();  // velocities complete before the next rate pass
+        if (done) break;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctl->iters = it;
 }
 
 // ---------------------------------------------------------------------------

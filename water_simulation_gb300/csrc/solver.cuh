@@ -1311,8 +1311,11 @@ private:
         const bool adaptive = eta > 0.0f;
         const double thr = double(eta) * double(cfg_.rest_density);
         const u32 first_check = DIV ? 0u : 1u;  // density: from the 2nd iteration (dfsph.cu:255)
-        if (capturing_ && adaptive && !tp) return solve_on_device<DIV>(sd, max_iters, thr, first_check, ctl, kap_out,
-                                                                       adv_out, cs);
+        if (adaptive && !tp) {
+            // small scenes: the whole solve in one cooperative launch
+            if (solve_cooperative<DIV>(sd, max_iters, thr, first_check, ctl, kap_out, adv_out, cs)) return max_iters;
+            if (capturing_) return solve_on_device<DIV>(sd, max_iters, thr, first_check, ctl, kap_out, adv_out, cs);
+        }
         const int w = DIV ? 0 : 1;
         u32 launched = 0;
         for (u32 it = 0; it < max_iters; ++it) {
@@ -1378,6 +1381,60 @@ private:
     // by its parity, so the body replays with fixed pointers. Both buffers hold
     // the step's positions afterwards (every rate pass copies them), so the
     // host-side parity does not depend on the iteration count.
+    // An adaptive solve as one cooperative launch of jacobi_solve_kernel when
+    // its blocks (at the rate pass's block size) fit one per SM; false when
+    // they do not or when the passes are being timed one by one.
+    // Like the graph-resident loop it leaves the step's positions in both
+    // buffers and the iteration count in IterCtl::iters.
+    template <bool DIV>
+    bool solve_cooperative(const StepDt<R>& sd, u32 max_iters, double thr, u32 first_check, IterCtl* ctl,
+                           R* kap_out, R* adv_out, const u32* cs) {
+        if (max_iters == 0 || profile_mask_ != 0) return false;
+        const int lb = bs_[DFSPH_KERNEL_PRESSURE_RATE];
+        if (lb != 128 && lb != 256) return false;
+        const int n = int(n_);
+        const int blocks = blocks_for(n, lb);
+        int& cap = coop_blocks_[DIV ? 1 : 0][lb == 256 ? 1 : 0];
+        if (cap < 0) {
+            int per_sm = 0, sms = 0;
+            if (lb == 128)
+                DFSPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_solve_kernel<R, DIV, 128>,
+                                                                         128, 0));
+            else
+                DFSPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_solve_kernel<R, DIV, 256>,
+                                                                         256, 0));
+            DFSPH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+            // at most one block per SM: beyond that the passes are long
+            // enough to hide their launches, and the per-pass kernels keep
+            // their neighbour gathers in L1
+            cap = std::min(std::min(per_sm, 1) * sms, JACOBI_SOLVE_MAX_BLOCKS);
+        }
+        if (blocks > cap) return false;
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3(unsigned(blocks));
+        lc.blockDim = dim3(unsigned(lb));
+        lc.stream = stream_;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        lc.attrs = attr;
+        lc.numAttrs = 1;
+        V4* xa = xk_[cx_].p;
+        V4* xb = xk_[cx_ ^ 1].p;
+        const double inv_n = 1.0 / double(n);
+        if (lb == 128)
+            DFSPH_CUDA(cudaLaunchKernelEx(&lc, jacobi_solve_kernel<R, DIV, 128>, n, xa, xb, vr_[cv_].p,
+                                          (const R*)alpha_.p, adv_out, kap_out, cs, g_, phys_, bdev(), sd,
+                                          partials_.p, ctl, max_iters, first_check, inv_n, thr));
+        else
+            DFSPH_CUDA(cudaLaunchKernelEx(&lc, jacobi_solve_kernel<R, DIV, 256>, n, xa, xb, vr_[cv_].p,
+                                          (const R*)alpha_.p, adv_out, kap_out, cs, g_, phys_, bdev(), sd,
+                                          partials_.p, ctl, max_iters, first_check, inv_n, thr));
+        if (capturing_) ++graph_kernels_;
+        else ++launches_;
+        return true;
+    }
+
     template <bool DIV>
     u32 solve_on_device(const StepDt<R>& sd, u32 max_iters, double thr, u32 first_check, IterCtl* ctl, R* kap_out,
                         R* adv_out, const u32* cs) {
@@ -1585,7 +1642,8 @@ private:
     unsigned long long frame_body_kernels_ = 0;
     int last_frame_graph_ = 0;
     cudaStream_t loop_stream_ = nullptr;
-    bool iters_on_device_ = false;  // the last step's iteration counts live in IterCtl::iters
+    bool iters_on_device_ = false;
+    int coop_blocks_[2][2] = {{-1, -1}, {-1, -1}};  // resident jacobi_solve_kernel blocks: [DIV][256 threads]  // the last step's iteration counts live in IterCtl::iters
     bool fuse_advect_ = true;  // last density iteration carries the integrator when it can
     DevBuf<V4> tune_ck_;
     DevBuf<IterCtl> tune_ctl_;
