@@ -15,9 +15,10 @@ pytestmark = pytest.mark.gpu
 ALL_CLASSES = (1 << _lib.KERNEL_CLASSES) - 1
 
 
-def _solver(sc, graph=False, damping=None):
+def _solver(sc, graph=False, damping=None, precision=_lib.PRECISION_FP32):
     cfg = sc.config()
     cfg.use_cuda_graph = 1 if graph else 0
+    cfg.precision = precision
     if damping is not None:
         cfg.damping = damping
     s = Solver(cfg)
@@ -26,8 +27,8 @@ def _solver(sc, graph=False, damping=None):
     return s
 
 
-def _run(sc, profile, steps):
-    s = _solver(sc)
+def _run(sc, profile, steps, precision=_lib.PRECISION_FP32):
+    s = _solver(sc, precision=precision)
     if profile:
         s.profile_enable(ALL_CLASSES)
     iters = []
@@ -40,13 +41,14 @@ def _run(sc, profile, steps):
     return out
 
 
-@pytest.mark.parametrize("sigma", [0.0, 0.4])
-def test_cooperative_solve_matches_per_pass_solve(sigma):
+@pytest.mark.parametrize("sigma,precision", [(0.0, _lib.PRECISION_FP32), (0.4, _lib.PRECISION_FP32),
+                                             (0.4, _lib.PRECISION_FP64)])
+def test_cooperative_solve_matches_per_pass_solve(sigma, precision):
     sc = scenes.puddle()
     if sigma:
         sc.velocity = np.random.default_rng(3).normal(0, sigma, size=sc.fluid.shape).astype(np.float32)
-    x0, v0, r0, it0, l0 = _run(sc, False, 12)
-    x1, v1, r1, it1, l1 = _run(sc, True, 12)
+    x0, v0, r0, it0, l0 = _run(sc, False, 12, precision)
+    x1, v1, r1, it1, l1 = _run(sc, True, 12, precision)
     assert it0 == it1
     assert sum(a + b for a, b in it0) > 3 * 12  # the solves iterate
     assert np.array_equal(x0, x1) and np.array_equal(v0, v1) and np.array_equal(r0, r1)
