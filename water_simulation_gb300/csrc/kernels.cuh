@@ -61,6 +61,36 @@ template <class R, bool COHERENT> __device__ __forceinline__ R4<R> ld_rec(const 
     return ld(p);
 }
 
+// Copies of a block's neighbour records in shared memory (slots lo ..): set by
+// a persistent solve for a block whose stencils read a short enough slot
+// range; x null means the records are read from global memory.
+template <class R> struct NbrSrc {
+    const R4<R>* x = nullptr;
+    const R4<R>* v = nullptr;
+    u32 lo = 0;
+    // the thread's 9 stencil runs, computed once per launch: run k of the
+    // thread is [rb[k * stride], re[k * stride]) (null: look them up)
+    const u32* rb = nullptr;
+    const u32* re = nullptr;
+    int stride = 0;
+};
+
+// The stencil's runs from NbrSrc's table when it has one, else from cell_start
+// (for_each_run_ahead); the same runs in the same order either way.
+template <class R, class F>
+__device__ __forceinline__ void for_each_run_src(const NbrSrc<R>& src, const Centre& c, const GridDev<R>& g,
+                                                 const u32* __restrict__ cs, F&& f) {
+    if (!src.rb) {
+        for_each_run_ahead(c, g, cs, f);
+        return;
+    }
+#pragma unroll 1
+    for (int k = 0; k < 9; ++k) {
+        const u32 b = src.rb[k * src.stride], e = src.re[k * src.stride];
+        if (b < e) f(b, e);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Pair terms. With r = |x_i - x_j| the cubic spline and its gradient factor
 // F(r) = (sigma/l) w'(r/l) / r (so that gradW = F(r) r_ij) are, per branch,
@@ -715,7 +745,8 @@ __device__ __forceinline__ double rate_particle(int i, const R4<R>* __restrict__
                                                 const R4<R>* __restrict__ vr, const R* __restrict__ alpha,
                                                 R* __restrict__ rho_adv, R* __restrict__ kap,
                                                 const u32* __restrict__ cs, const GridDev<R>& g, const Phys<R>& p,
-                                                const BoundaryDev& bd, R dt, R4<R>* __restrict__ tape_v) {
+                                                const BoundaryDev& bd, R dt, R4<R>* __restrict__ tape_v,
+                                                const NbrSrc<R>& src = NbrSrc<R>()) {
     double err = 0;
     const R4<R> pi = ld_rec<R, COHERENT>(xk_in + i);
     const R4<R> vi = ld_rec<R, COHERENT>(vr + i);
@@ -731,14 +762,19 @@ __device__ __forceinline__ double rate_particle(int i, const R4<R>* __restrict__
     };
     if (COHERENT) {
         // latency-bound: a column's records four at a time, summed in order
-        for_each_run_ahead(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+        for_each_run_src(src, c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
             for (u32 j0 = b; j0 < e; j0 += 4) {
                 R4<R> pj[4], vj[4];
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
                     const u32 j = min(j0 + u, e - 1);
-                    pj[u] = ld_coh(xk_in + j);
-                    vj[u] = ld_coh(vr + j);
+                    if (src.x) {
+                        pj[u] = src.x[j - src.lo];
+                        vj[u] = src.v[j - src.lo];
+                    } else {
+                        pj[u] = ld_coh(xk_in + j);
+                        vj[u] = ld_coh(vr + j);
+                    }
                 }
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
@@ -832,7 +868,8 @@ __global__ void __launch_bounds__(LB) pressure_rate_kernel(
 template <class R, bool COHERENT = false>
 __device__ __forceinline__ R4<R> apply_velocity(int i, const R4<R>* __restrict__ xk, const R4<R>* __restrict__ vr,
                                                 const R* __restrict__ kap, const u32* __restrict__ cs,
-                                                const GridDev<R>& g, const Phys<R>& p, const BoundaryDev& bd, R dt) {
+                                                const GridDev<R>& g, const Phys<R>& p, const BoundaryDev& bd, R dt,
+                                                const NbrSrc<R>& src = NbrSrc<R>()) {
     const R4<R> pi = ld_rec<R, COHERENT>(xk + i);
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
     R ax = 0, ay = 0, az = 0;
@@ -845,11 +882,14 @@ __device__ __forceinline__ R4<R> apply_velocity(int i, const R4<R>* __restrict__
     };
     if (COHERENT) {
         // latency-bound: a column's records four at a time, summed in order
-        for_each_run_ahead(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+        for_each_run_src(src, c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
             for (u32 j0 = b; j0 < e; j0 += 4) {
                 R4<R> pj[4];
 #pragma unroll
-                for (int u = 0; u < 4; ++u) pj[u] = ld_coh(xk + min(j0 + u, e - 1));
+                for (int u = 0; u < 4; ++u) {
+                    const u32 j = min(j0 + u, e - 1);
+                    pj[u] = src.x ? src.x[j - src.lo] : ld_coh(xk + j);
+                }
 #pragma unroll
                 for (int u = 0; u < 4; ++u)
                     if (j0 + u < e) pair(pj[u]);
@@ -909,27 +949,82 @@ __global__ void __launch_bounds__(LB) pressure_apply_kernel(
 // and write (x, kappa / rho^2) to xb, odd ones the other way round, as the
 // graph-resident loop does. Launched with the rate pass's block size, so the
 // partial sums, and with them the iteration count, equal the per-launch
-// solve's. Records written inside the launch are read with ld_coh.
+// solve's. Records written inside the launch are read with ld_coh; a block
+// whose stencils read at most stage_cap consecutive slots copies them into
+// shared memory once per pass (dynamic shared memory: 2 x stage_cap records).
 constexpr int JACOBI_SOLVE_MAX_BLOCKS = 256;
 template <class R, bool DIV, int LB>
 __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
     int n, R4<R>* xa, R4<R>* xb, R4<R>* vr, const R* __restrict__ alpha, R* rho_adv, R* kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, double* partials,
-    IterCtl* ctl, u32 max_iters, u32 first_check, double inv_n, double threshold) {
+    IterCtl* ctl, u32 max_iters, u32 first_check, double inv_n, double threshold, u32 stage_cap) {
     namespace cg = cooperative_groups;
     cg::grid_group grid = cg::this_grid();
+    extern __shared__ __align__(16) unsigned char jacobi_stage[];
+    R4<R>* sx = reinterpret_cast<R4<R>*>(jacobi_stage);
+    R4<R>* sv = sx + stage_cap;
     __shared__ double sh[LB / 32];
     __shared__ double part[JACOBI_SOLVE_MAX_BLOCKS];
     __shared__ int stop;
+    __shared__ u32 span_lo, span_hi;
+    __shared__ u32 run_b[9 * LB], run_e[9 * LB];
     const R dt = step_dt(sd);
     const int i = blockIdx.x * LB + threadIdx.x;
+    // the slot range [lo, hi) that this block's stencils read (the grid does
+    // not change during the solve); staged in shared memory when it fits
+    if (threadIdx.x == 0) {
+        span_lo = 0xFFFFFFFFu;
+        span_hi = 0u;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        run_b[k * LB + threadIdx.x] = 0u;
+        run_e[k * LB + threadIdx.x] = 0u;
+    }
+    if (i < n) {
+        const R4<R> pi = ld_coh(xa + i);
+        u32 lo = 0xFFFFFFFFu, hi = 0u;
+        int k = 0;  // runs come in column order; empty and off-grid ones are skipped
+        for_each_run(stencil_centre(pi.x, pi.y, pi.z, g), g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+            if (b < e) {
+                run_b[k * LB + threadIdx.x] = b;
+                run_e[k * LB + threadIdx.x] = e;
+                ++k;
+                lo = min(lo, b);
+                hi = max(hi, e);
+            }
+        });
+        if (hi > lo) {
+            atomicMin(&span_lo, lo);
+            atomicMax(&span_hi, hi);
+        }
+    }
+    __syncthreads();
+    const u32 lo = span_lo, hi = span_hi;
+    const bool staged = hi > lo && hi - lo <= stage_cap;
+    const u32 count = staged ? hi - lo : 0u;
     u32 it = 0;
     while (it < max_iters) {
         const R4<R>* xin = (it & 1u) ? xb : xa;
         R4<R>* xout = (it & 1u) ? xa : xb;
+        NbrSrc<R> src;
+        src.rb = run_b + threadIdx.x;
+        src.re = run_e + threadIdx.x;
+        src.stride = LB;
+        if (staged) {
+            for (u32 k = threadIdx.x; k < count; k += LB) {
+                sx[k] = ld_coh(xin + lo + k);
+                sv[k] = ld_coh(vr + lo + k);
+            }
+            __syncthreads();
+            src.x = sx;
+            src.v = sv;
+            src.lo = lo;
+        }
         double err = 0;
         if (i < n)
-            err = rate_particle<R, DIV, true>(i, xin, xout, vr, alpha, rho_adv, kap, cs, g, p, bd, dt, nullptr);
+            err = rate_particle<R, DIV, true>(i, xin, xout, vr, alpha, rho_adv, kap, cs, g, p, bd, dt, nullptr, src);
         const double t = block_sum_dyn(err, sh);
         if (threadIdx.x == 0) partials[blockIdx.x] = t;
         grid.sync();
@@ -949,7 +1044,12 @@ __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
         }
         __syncthreads();
         const bool done = stop != 0;
-        if (i < n) vr[i] = apply_velocity<R, true>(i, xout, vr, kap, cs, g, p, bd, dt);
+        if (staged) {
+            // the block's rate pass finished reading sx, sv before the barrier
+            for (u32 k = threadIdx.x; k < count; k += LB) sx[k] = ld_coh(xout + lo + k);
+            __syncthreads();
+        }
+        if (i < n) vr[i] = apply_velocity<R, true>(i, xout, vr, kap, cs, g, p, bd, dt, src);
         ++it;
         grid.sync();  // velocities complete before the next rate pass
         if (done) break;

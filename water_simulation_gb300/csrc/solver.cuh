@@ -1394,15 +1394,23 @@ private:
         if (lb != 128 && lb != 256) return false;
         const int n = int(n_);
         const int blocks = blocks_for(n, lb);
+        // neighbour records staged per block: 2 x stage_cap of them
+        constexpr size_t kStageBytes = 96 * 1024;
+        const u32 stage_cap = static_cast<u32>(kStageBytes / (2 * sizeof(V4)));
         int& cap = coop_blocks_[DIV ? 1 : 0][lb == 256 ? 1 : 0];
         if (cap < 0) {
             int per_sm = 0, sms = 0;
-            if (lb == 128)
+            if (lb == 128) {
+                DFSPH_CUDA(cudaFuncSetAttribute(jacobi_solve_kernel<R, DIV, 128>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, int(kStageBytes)));
                 DFSPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_solve_kernel<R, DIV, 128>,
-                                                                         128, 0));
-            else
+                                                                         128, kStageBytes));
+            } else {
+                DFSPH_CUDA(cudaFuncSetAttribute(jacobi_solve_kernel<R, DIV, 256>,
+                                                cudaFuncAttributeMaxDynamicSharedMemorySize, int(kStageBytes)));
                 DFSPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_solve_kernel<R, DIV, 256>,
-                                                                         256, 0));
+                                                                         256, kStageBytes));
+            }
             DFSPH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
             // at most one block per SM: beyond that the passes are long
             // enough to hide their launches, and the per-pass kernels keep
@@ -1413,6 +1421,7 @@ private:
         cudaLaunchConfig_t lc = {};
         lc.gridDim = dim3(unsigned(blocks));
         lc.blockDim = dim3(unsigned(lb));
+        lc.dynamicSmemBytes = kStageBytes;
         lc.stream = stream_;
         cudaLaunchAttribute attr[1];
         attr[0].id = cudaLaunchAttributeCooperative;
@@ -1425,11 +1434,11 @@ private:
         if (lb == 128)
             DFSPH_CUDA(cudaLaunchKernelEx(&lc, jacobi_solve_kernel<R, DIV, 128>, n, xa, xb, vr_[cv_].p,
                                           (const R*)alpha_.p, adv_out, kap_out, cs, g_, phys_, bdev(), sd,
-                                          partials_.p, ctl, max_iters, first_check, inv_n, thr));
+                                          partials_.p, ctl, max_iters, first_check, inv_n, thr, stage_cap));
         else
             DFSPH_CUDA(cudaLaunchKernelEx(&lc, jacobi_solve_kernel<R, DIV, 256>, n, xa, xb, vr_[cv_].p,
                                           (const R*)alpha_.p, adv_out, kap_out, cs, g_, phys_, bdev(), sd,
-                                          partials_.p, ctl, max_iters, first_check, inv_n, thr));
+                                          partials_.p, ctl, max_iters, first_check, inv_n, thr, stage_cap));
         if (capturing_) ++graph_kernels_;
         else ++launches_;
         return true;
