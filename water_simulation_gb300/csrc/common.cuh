@@ -103,6 +103,13 @@ __device__ __forceinline__ u32 cell_key(R px, R py, R pz, const GridDev<R>& g) {
                static_cast<u32>(g.nz) + static_cast<u32>(cz);
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialization may start while the kernel before it on the stream drains;
+// this waits until that kernel has completed and its memory is visible
+// (griddepcontrol.wait; without the launch attribute it returns at once).
+// Every kernel of the step calls it before touching global memory.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Stencil-centre cell (dfsph_kernels.cu:15-17) clamped to [-2, dims+1]: any
 // value outside that range selects no cell on that axis, exactly as the
 // unclamped coordinate would, and the clamp keeps the +-1 arithmetic in range.

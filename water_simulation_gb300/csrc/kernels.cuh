@@ -252,6 +252,7 @@ template <class R>
 __global__ void __launch_bounds__(256) count_kernel(int n, const R4<R>* __restrict__ xk,
                                                     GridDev<R> g, u32* __restrict__ key,
                                                     u32* __restrict__ rank, u32* __restrict__ count) {
+    pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const R4<R> p = ld(xk + s);
@@ -269,6 +270,7 @@ constexpr int SCAN_TILE = SCAN_BLOCK * SCAN_ITEMS;
 
 static __global__ void __launch_bounds__(SCAN_BLOCK) scan_tile_sums(const u32* __restrict__ count, u32 m,
                                                              u32* __restrict__ tile_sums) {
+    pdl_wait();
     __shared__ u32 sh[SCAN_BLOCK / 32];
     const u32 base = blockIdx.x * SCAN_TILE;
     u32 t = 0;
@@ -296,6 +298,7 @@ static __global__ void __launch_bounds__(SCAN_BLOCK) scan_tile_sums(const u32* _
 static __global__ void __launch_bounds__(1024) scan_tile_offsets(u32* __restrict__ tile_sums, u32 n_tiles,
                                                           u32* __restrict__ total_out, IterCtl* ctl, int n_ctl,
                                                           u32* __restrict__ maxv_scene, int n_scenes) {
+    pdl_wait();
     __shared__ u32 warp_tot[32];
     __shared__ u32 carry;
     if (threadIdx.x == 0) carry = 0;
@@ -351,6 +354,7 @@ __device__ __forceinline__ u32 scan_pad(u32 i) { return i + (i >> 5); }
 static __global__ void __launch_bounds__(SCAN_BLOCK) scan_tiles(u32* __restrict__ count, u32 m,
                                                          const u32* __restrict__ tile_offsets,
                                                          u32* __restrict__ cell_start) {
+    pdl_wait();
     __shared__ u32 warp_tot[SCAN_BLOCK / 32];
     __shared__ u32 tile[SCAN_TILE + SCAN_TILE / 32];
     const u32 base = blockIdx.x * SCAN_TILE;
@@ -410,6 +414,7 @@ static __global__ void __launch_bounds__(256) scatter_kernel(int n, const u32* _
                                                       const u32* __restrict__ cell_start,
                                                       const u32* __restrict__ id_old,
                                                       u32* __restrict__ tmp_src, u32* __restrict__ tmp_id) {
+    pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const u32 d = cell_start[key[s]] + rank[s];
@@ -431,6 +436,7 @@ __global__ void __launch_bounds__(256) reorder_kernel(
     u32 sentinel_cap, const R4<R>* __restrict__ xk_old, const R4<R>* __restrict__ vr_old,
     R4<R>* __restrict__ xk_new, R4<R>* __restrict__ vr_new, u32* __restrict__ id_new,
     u32* __restrict__ key_sorted, IterCtl* ctl) {
+    pdl_wait();
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
     const u32 src = tmp_src[t];
@@ -620,6 +626,7 @@ __global__ void __launch_bounds__(LB) density_alpha_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, R* __restrict__ alpha,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, u32* __restrict__ nbr_f,
     u32* __restrict__ nbr_b, const u32* __restrict__ id, Tape1<R> tp) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R4<R> pi = ld(xk + i);
@@ -705,6 +712,7 @@ __global__ void __launch_bounds__(LB) forces_xsph_kernel(
     int n, const R4<R>* __restrict__ xk, const R4<R>* __restrict__ vr_in, R4<R>* __restrict__ vr_out,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, StepDt<R> sd, R eps,
     const R* __restrict__ eps_scene, int do_xsph, R4<R>* __restrict__ tape_v) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R dt = step_dt(sd);
@@ -837,6 +845,7 @@ __global__ void __launch_bounds__(LB) pressure_rate_kernel(
     R* __restrict__ kap, const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd,
     StepDt<R> sd, double* __restrict__ partials, IterCtl* ctl, u32 iter, u32 first_check, double inv_n,
     double threshold, R4<R>* __restrict__ tape_v, const u32* dev_iter) {
+    pdl_wait();
     __shared__ double sh[LB / 32];
     // Inside a device-resident loop (DEVLOOP) the iteration comes from the
     // device and even iterations read xk_in / write xk_out, odd ones the other
@@ -929,6 +938,7 @@ __global__ void __launch_bounds__(LB) pressure_apply_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, const R* __restrict__ kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, const IterCtl* ctl,
     u32 iter, const R4<R>* xk_odd, const u32* dev_iter) {
+    pdl_wait();
     if (DEVLOOP) {
         iter = *((volatile const u32*)dev_iter);
         if (iter & 1u) xk = xk_odd;
@@ -1134,6 +1144,7 @@ __global__ void __launch_bounds__(256) advect_kernel(
     int n, const R4<R>* xk, R4<R>* xk_out, R4<R>* __restrict__ vr, StepDt<R> sd, Domain<R> d, GridDev<R> g,
     u32* __restrict__ key, u32* __restrict__ rank, u32* __restrict__ count, IterCtl* ctl,
     u32* __restrict__ maxv_scene, R4<R>* __restrict__ tape_v, unsigned char* __restrict__ tape_mask) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const R dt = step_dt(sd);
     u32 vbits = 0;
@@ -1158,6 +1169,7 @@ __global__ void __launch_bounds__(LB) apply_advect_kernel(
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, Domain<R> d,
     u32* __restrict__ key, u32* __restrict__ rank, u32* __restrict__ count, IterCtl* ctl,
     u32* __restrict__ maxv_scene) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const R dt = step_dt(sd);
     u32 vbits = 0;

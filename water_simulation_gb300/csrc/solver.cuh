@@ -1034,8 +1034,24 @@ private:
             b = take_event();
             DFSPH_CUDA(cudaEventRecord(a, stream_));
         }
-        kernel<<<grid, block, 0, stream_>>>(args...);
-        DFSPH_LAUNCHED();
+        if (!prof && kclass <= DFSPH_KERNEL_ADVECT) {
+            // the step's kernels (they all begin with pdl_wait): launched with
+            // programmatic stream serialization, so a kernel's launch and
+            // block scheduling overlap the drain of the one before it
+            cudaLaunchConfig_t lc = {};
+            lc.gridDim = dim3(unsigned(grid));
+            lc.blockDim = dim3(unsigned(block));
+            lc.stream = stream_;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            at[0].val.programmaticStreamSerializationAllowed = 1;
+            lc.attrs = at;
+            lc.numAttrs = 1;
+            DFSPH_CUDA(cudaLaunchKernelEx(&lc, kernel, args...));
+        } else {
+            kernel<<<grid, block, 0, stream_>>>(args...);
+            DFSPH_LAUNCHED();
+        }
         if (capturing_) ++graph_kernels_;
         else ++launches_;
         if (prof) {
