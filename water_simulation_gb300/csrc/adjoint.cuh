@@ -79,6 +79,7 @@ __global__ void __launch_bounds__(256) adjoint_advect_kernel(
     int n, const u32* __restrict__ id, const R4<R>* __restrict__ va, const unsigned char* __restrict__ amask, R dt,
     const R4<R>* __restrict__ xg, const R4<R>* __restrict__ vg, R4<R>* __restrict__ xbar, R4<R>* __restrict__ vbar,
     R* __restrict__ rhobar, R* __restrict__ alphabar) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const u32 o = id[i];
@@ -118,6 +119,7 @@ __global__ void __launch_bounds__(128) adjoint_apply_kernel(
     const R* __restrict__ kap, const R* __restrict__ adv, const R4<R>* __restrict__ vbar,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, R dt, R4<R>* __restrict__ xbar,
     R* __restrict__ rhobar, R* __restrict__ alphabar, R4<R>* __restrict__ xr) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R4<R> pi = ld(xkf + i);
@@ -205,6 +207,7 @@ template <class R>
 __global__ void __launch_bounds__(128) adjoint_rate_kernel(
     int n, const R4<R>* __restrict__ xr, const R4<R>* __restrict__ vel, const u32* __restrict__ cs, GridDev<R> g,
     Phys<R> p, BoundaryDev bd, R4<R>* __restrict__ vbar, R4<R>* __restrict__ xbar) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R4<R> pi = ld(xr + i);
@@ -286,6 +289,7 @@ __global__ void __launch_bounds__(128) adjoint_xsph_kernel(
     R4<R>* __restrict__ vbar_out, const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, R decay, R eps,
     R4<R>* __restrict__ xbar, R* __restrict__ rhobar, double* __restrict__ partials, u32* counter,
     double* eps_acc) {
+    pdl_wait();
     __shared__ double sh[4];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double part = 0;
@@ -336,6 +340,7 @@ template <class R>
 __global__ void __launch_bounds__(256) adjoint_density_prep_kernel(
     int n, const R4<R>* __restrict__ tx, const R4<R>* __restrict__ tg, const R* __restrict__ rhobar,
     const R* __restrict__ alphabar, R4<R>* __restrict__ xq, R4<R>* __restrict__ gq) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R4<R> ti = tx[i];
@@ -359,6 +364,7 @@ __global__ void __launch_bounds__(128) adjoint_density_kernel(
     int n, const R4<R>* __restrict__ xq, const R4<R>* __restrict__ gq, const R4<R>* __restrict__ vbar,
     const R4<R>* __restrict__ xbar, const u32* __restrict__ id, const u32* __restrict__ cs, GridDev<R> g, Phys<R> p,
     BoundaryDev bd, R4<R>* __restrict__ xg, R4<R>* __restrict__ vg) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const R4<R> xi = ld(xq + i);

@@ -1034,8 +1034,8 @@ private:
             b = take_event();
             DFSPH_CUDA(cudaEventRecord(a, stream_));
         }
-        if (!prof && kclass <= DFSPH_KERNEL_ADVECT) {
-            // the step's kernels (they all begin with pdl_wait): launched with
+        if (!prof && (kclass <= DFSPH_KERNEL_ADVECT || kclass == DFSPH_KERNEL_ADJOINT)) {
+            // the step's and the adjoint's kernels (they all begin with pdl_wait): launched with
             // programmatic stream serialization, so a kernel's launch and
             // block scheduling overlap the drain of the one before it
             cudaLaunchConfig_t lc = {};
