@@ -1447,14 +1447,23 @@ private:
         V4* xa = xk_[cx_].p;
         V4* xb = xk_[cx_ ^ 1].p;
         const double inv_n = 1.0 / double(n);
+        cudaError_t e;
         if (lb == 128)
-            DFSPH_CUDA(cudaLaunchKernelEx(&lc, jacobi_solve_kernel<R, DIV, 128>, n, xa, xb, vr_[cv_].p,
-                                          (const R*)alpha_.p, adv_out, kap_out, cs, g_, phys_, bdev(), sd,
-                                          partials_.p, ctl, max_iters, first_check, inv_n, thr, stage_cap));
+            e = cudaLaunchKernelEx(&lc, jacobi_solve_kernel<R, DIV, 128>, n, xa, xb, vr_[cv_].p, (const R*)alpha_.p,
+                                   adv_out, kap_out, cs, g_, phys_, bdev(), sd, partials_.p, ctl, max_iters,
+                                   first_check, inv_n, thr, stage_cap);
         else
-            DFSPH_CUDA(cudaLaunchKernelEx(&lc, jacobi_solve_kernel<R, DIV, 256>, n, xa, xb, vr_[cv_].p,
-                                          (const R*)alpha_.p, adv_out, kap_out, cs, g_, phys_, bdev(), sd,
-                                          partials_.p, ctl, max_iters, first_check, inv_n, thr, stage_cap));
+            e = cudaLaunchKernelEx(&lc, jacobi_solve_kernel<R, DIV, 256>, n, xa, xb, vr_[cv_].p, (const R*)alpha_.p,
+                                   adv_out, kap_out, cs, g_, phys_, bdev(), sd, partials_.p, ctl, max_iters,
+                                   first_check, inv_n, thr, stage_cap);
+        if (e == cudaErrorCooperativeLaunchTooLarge && !capturing_) {
+            // fewer SMs than the device reports (a partitioned GPU): the
+            // per-pass solve from now on
+            cudaGetLastError();
+            cap = 0;
+            return false;
+        }
+        DFSPH_CUDA(e);
         if (capturing_) ++graph_kernels_;
         else ++launches_;
         return true;
