@@ -2,9 +2,10 @@
 //
 // TEST INFRASTRUCTURE ONLY — the CPU oracle for the DFSPH step.
 //
-// Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load this
-// library, and only as the checker (or as the timed CPU baseline). The product
-// path (water_simulation_gb300/csrc) never links, loads or calls it.
+// Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg and
+// reference arm load this library, and only as the checker (or as the timed
+// CPU baseline). The product path (water_simulation_gb300/csrc) never links,
+// loads or calls it.
 //
 // This is a plain C++/OpenMP restatement of the reference DFSPH step of
 // Qervas/water_simulation, templated on the real type:
@@ -16,7 +17,7 @@
 // gathered through the sorted permutation) and its arithmetic order, without
 // the reference's -use_fast_math approximations.
 //
-// Deliberate deviations (also listed in the design doc):
+// Deliberate deviations:
 //   * XSPH is Jacobi (every particle reads the pre-XSPH velocities). The
 //     reference updates velocities in place while neighbours read them
 //     (solvers/dfsph/src/dfsph_kernels.cu:327,338-340), a data race whose result

@@ -1,7 +1,7 @@
 """ctypes face of liboracle.so — TEST INFRASTRUCTURE ONLY.
 
 The CPU restatement of the reference DFSPH step (dfsph_oracle.cpp). Only the
-tests, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it, as the
+tests, __graft_entry__.smoke() and bench.py's baseline legs use it, as the
 checker or as the timed CPU baseline; the product never does.
 """
 from __future__ import annotations
