@@ -93,7 +93,7 @@ def make_scene(name):
         return scenes.dam_break(scale=2, reference_mode=True)
     if name == "dam128k":
         return scenes.dam_break(scale=1, reference_mode=True)
-    if name == "dam128k_div":  # with this build's 2 divergence iterations
+    if name == "dam128k_div":  # with 2 divergence-solver iterations (the reference has none)
         return scenes.dam_break(scale=1, reference_mode=False)
     sc = scenes.puddle()
     if name == "puddle_adaptive":  # the settled puddle as the reference runs it: adaptive density solve
@@ -582,7 +582,7 @@ def bench_lbvh(sc, reps=20, warmup=3):
             np.array_equal(u(right), rr) and np.array_equal(u(parent)[1:], rp[1:]) and
             np.array_equal(boxes.cpu().numpy()[n - 1:], rb))
     # the reference's build stops at the leaf boxes: the like-for-like part of
-    # this build is the build without its box pass
+    # dfsph_lbvh_build is the build without its box pass
     topo_ms = max(build_ms - refit_ms, 1e-9)
     res["topology_ms"] = topo_ms
     res["reference"] = {"build_ms": ref_ms, "speedup": ref_ms / build_ms, "speedup_topology": ref_ms / topo_ms,
@@ -606,7 +606,7 @@ def bench_ref_cuda(sc, steps, warmup=1):
     probe.close()
     ocfg = O.config_from(sc.config(), stencil_inv_cell=inv)
     ref = R.ReferenceRun(ocfg, sc.fluid, sc.velocity, sc.boundary)
-    ref.step(sc.dt, max(warmup, 1))  # the same steps as this build's timed ones (adaptive solves vary)
+    ref.step(sc.dt, max(warmup, 1))  # the same steps as the timed ones above (adaptive solves vary)
     ms = ref.time_steps(sc.dt, steps)
     ref.close()
     return {"value": sc.n * steps / (ms * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms / steps,

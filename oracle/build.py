@@ -1,4 +1,4 @@
-"""Build recipes of the checker (test infrastructure only).
+"""Build recipes of the oracle (test infrastructure only).
 
 * liboracle.so      - the C++/OpenMP restatement in dfsph_oracle.cpp (g++).
 * _ref/*.fatbin     - the reference's own kernels, compiled from the reference
@@ -7,7 +7,7 @@
                       the reference's flags (-use_fast_math,
                       CMakeLists.txt:56) for sm_103a. Only
                       possible where the reference tree exists; the fatbins are
-                      device code, so they run on the Arm GPU machine unchanged.
+                      device code, so they run on Arm GPU hosts unchanged.
 * _ref/libref_runner.so - ref_runner.cu: host orchestration restating
                       DFSPHSolver / CellGrid::build / SpatialAccel::build
                       around those fatbins (nvcc,

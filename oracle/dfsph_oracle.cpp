@@ -3,14 +3,14 @@
 // TEST INFRASTRUCTURE ONLY — the CPU oracle for the DFSPH step.
 //
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg and
-// reference arm load this library, and only as the checker (or as the timed
+// reference arm load this library, and only as the parity reference (or as the timed
 // CPU baseline). The product path (water_simulation_gb300/csrc) never links,
 // loads or calls it.
 //
 // This is a plain C++/OpenMP restatement of the reference DFSPH step of
 // Qervas/water_simulation, templated on the real type:
 //   * Real = float  : the FP32 instance (the timed CPU baseline, and the
-//                     checker for bit-exact grid/neighbour structure);
+//                     reference for bit-exact grid/neighbour structure);
 //   * Real = double : the FP64 oracle that field errors are reported against.
 // Each function cites the reference file:line it restates. It follows the
 // reference's data layout (particles kept in their ORIGINAL order, neighbours
@@ -74,7 +74,7 @@ template <class R> struct V3 { R x, y, z; };
 // Forward-mode dual number: a value and its derivative along one direction.
 // Solver<Dual> runs the FP64 step on the values (every branch, max(0, .),
 // clamp and neighbour set decided by them) and carries the exact directional
-// derivative of the step along, which is the checker of the GPU adjoint
+// derivative of the step along, against which the GPU adjoint is tested
 // (dfsph_adjoint_backward): <gradient, direction> must equal it.
 struct Dual {
     double v = 0.0, d = 0.0;
@@ -923,7 +923,7 @@ double oracle_scalar(void* p, int which) {
 
 // Forward-mode (dual number) instance: the same FP64 step carrying the
 // derivative along the direction (dx, dv, d_xsph) of the initial positions,
-// velocities and XSPH coefficient. Checker of the GPU adjoint only.
+// velocities and XSPH coefficient. Used to test the GPU adjoint only.
 void* oracle_dual_create(const Config* cfg, const float* fluid_xyz, const float* fluid_v, u32 n,
                          const float* boundary_xyz, u32 nb, const double* dx, const double* dv, double d_xsph) {
     auto* s = new Solver<oracle::Dual>;

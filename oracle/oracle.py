@@ -2,7 +2,7 @@
 
 The CPU restatement of the reference DFSPH step (dfsph_oracle.cpp). Only the
 tests, __graft_entry__.smoke() and bench.py's baseline legs use it, as the
-checker or as the timed CPU baseline; the product never does.
+parity reference or as the timed CPU baseline; the product never does.
 """
 from __future__ import annotations
 
@@ -248,7 +248,7 @@ class DualOracle:
     """The FP64 oracle step in forward mode: values plus the exact derivative
     along one direction (dx, dv) of the initial state and d_xsph of the XSPH
     coefficient, every branch and neighbour set decided by the values. The
-    checker of the GPU adjoint: <gradient, direction> = d(loss) along it."""
+    reference for the GPU adjoint: <gradient, direction> = d(loss) along it."""
 
     def __init__(self, cfg: OracleConfig, fluid, vel, boundary, dx=None, dv=None, d_xsph=0.0, threads=0):
         L = load()

@@ -4,7 +4,7 @@ Runs the reference's own compiled DFSPH kernels (oracle/_ref/*.fatbin, built
 from the reference sources by oracle/build.py) under the restated host
 orchestration of oracle/ref_runner.cu. Needs a GPU and the fatbins. Used by
 the tests (parity against the reference itself) and by bench.py, which times
-the reference's kernels beside this build's (`ref_cuda`, `lbvh.reference`);
+the reference's kernels beside the product's (`ref_cuda`, `lbvh.reference`);
 the product never uses it.
 """
 from __future__ import annotations

@@ -107,5 +107,5 @@ def test_reference_run_to_run_spread_with_xsph():
         gpu.step(sc.dt)
     spread = np.abs(ref.field(1) - ref2.field(1)).max()
     diff = np.abs(gpu.velocities() - ref.field(1)).max()
-    print(f"reference run-to-run velocity spread {spread:.3e}, this build vs reference {diff:.3e}")
+    print(f"reference run-to-run velocity spread {spread:.3e}, GPU vs reference {diff:.3e}")
     assert diff < max(1e-2, 10 * spread)

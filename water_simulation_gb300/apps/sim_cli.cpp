@@ -84,7 +84,7 @@ Args parse(int argc, char** argv) {
         } else if (s == "--out" && i + 1 < argc) {
             a.out_dir = argv[++i];
         } else if (s == "--no-vulkan") {
-            // accepted: this build has no graphics path
+            // accepted: there is no graphics path
         } else if (s == "--damping" && i + 1 < argc) {
             a.damping = std::stof(argv[++i]);
         } else if (s == "--viscosity" && i + 1 < argc) {
