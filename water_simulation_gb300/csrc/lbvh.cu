@@ -114,19 +114,20 @@ __global__ void __launch_bounds__(256) lbvh_refit_kernel(const float* __restrict
     }
 }
 
-// Refit without fences, in two phases per warp of 32 consecutive leaves.
-//  1. In the warp: every lane starts at its leaf; lanes whose current nodes
-//     share a parent hold its two children, so they merge by shuffles (the
-//     lower lane goes on, the upper stops) until no two lanes pair up.
-//  2. The lanes left (roots of the warp's complete subtrees) walk on with
-//     three independent exchange walks, one per 8-byte pair of box words
-//     ((min x, min y), (min z, max x), (max y, max z)): a walk swaps its pair
-//     into the parent's slot with one 64-bit atomicExch; getting back the empty
-//     pattern means it arrived first and stops, otherwise it got the sibling's
-//     pair, merges, stores and goes on. The data travels inside the atomic, so
-//     no ordering of other memory operations is needed. Internal slots start
-//     as all-ones words, a NaN pattern that float arithmetic never produces
-//     (its results are canonical NaNs).
+// Refit without fences, in two phases per block of 256 consecutive leaves.
+//  1. In the block: every lane starts at its leaf; lanes whose current nodes
+//     share a parent meet in shared memory, one merges and climbs on, until
+//     no two lanes meet (the subtrees of the block's leaves are complete).
+//  2. The lanes left (roots of the block's complete subtrees, and lanes whose
+//     partner lies in another block) walk on with three independent exchange
+//     walks, one per 8-byte pair of box words ((min x, min y), (min z, max x),
+//     (max y, max z)): a walk swaps its pair into the parent's slot with one
+//     64-bit atomicExch; getting back the empty pattern means it arrived first
+//     and stops, otherwise it got the sibling's pair, merges, stores and goes
+//     on. The data travels inside the atomic, so no ordering of other memory
+//     operations is needed. Internal slots start as all-ones words, a NaN
+//     pattern that float arithmetic never produces (its results are canonical
+//     NaNs).
 constexpr unsigned long long EMPTY_PAIR = ~0ull;
 
 __device__ __forceinline__ unsigned long long pack_pair(float a, float b) {
@@ -142,7 +143,6 @@ __global__ void __launch_bounds__(256) lbvh_refit_pairs_kernel(const float* __re
                                                                const u32* __restrict__ sorted,
                                                                const u32* __restrict__ parent, float* boxes) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
     bool active = k < n;
     float b[6] = {0, 0, 0, 0, 0, 0};
     u32 node = 0, up = 0xFFFFFFFFu;
@@ -156,28 +156,48 @@ __global__ void __launch_bounds__(256) lbvh_refit_pairs_kernel(const float* __re
         for (int w = 0; w < 3; ++w) *pair_slot(boxes, node, w) = pack_pair(b[2 * w], b[2 * w + 1]);
         up = parent[node];
     }
-    // 1. pairs inside the warp (node ids < 2^31; idle lanes use unique keys)
-    for (;;) {
-        const bool live = active && up != 0xFFFFFFFFu;
-        const u32 peers = __match_any_sync(0xffffffffu, live ? up : (0x80000000u | static_cast<u32>(lane)));
-        const bool pair = live && __popc(peers) == 2;
-        if (!__any_sync(0xffffffffu, pair)) break;
-        const int other = pair ? __ffs(peers & ~(1u << lane)) - 1 : lane;
-        float o[6];
+    // 1. merges inside the block. A parent P whose both children hold leaves
+    //    of this block has its whole range among them, so P, an endpoint of
+    //    its range, lies in [L, L + 256); a parent outside has a child outside.
+    //    Per round: lanes at such a parent count their arrival in shared
+    //    memory; the first leaves its box there and waits, the second merges
+    //    it (after a barrier) and climbs on. Rounds stop when nothing merged
+    //    (or after 64 levels); lanes still waiting then climb globally.
+    __shared__ u32 arrivals[256];
+    __shared__ float waiting[256][6];
+    __shared__ int merged;
+    const u32 L = blockIdx.x * 256u;
+    arrivals[threadIdx.x] = 0u;
+    bool parked = false;
+    for (int round = 0; round < 64; ++round) {
+        if (threadIdx.x == 0) merged = 0;
+        __syncthreads();
+        const bool meet = active && !parked && up != 0xFFFFFFFFu && up >= L && up - L < 256u;
+        u32 rank = 2u;
+        if (meet) {
+            rank = atomicAdd(&arrivals[up - L], 1u);
+            if (rank == 0u) {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) o[c] = __shfl_sync(0xffffffffu, b[c], other);
-        if (pair) {
-            if (lane < other) {
-                b[0] = fminf(b[0], o[0]); b[1] = fminf(b[1], o[1]); b[2] = fminf(b[2], o[2]);
-                b[3] = fmaxf(b[3], o[3]); b[4] = fmaxf(b[4], o[4]); b[5] = fmaxf(b[5], o[5]);
-                node = up;
-#pragma unroll
-                for (int w = 0; w < 3; ++w) *pair_slot(boxes, node, w) = pack_pair(b[2 * w], b[2 * w + 1]);
-                up = parent[node];
-            } else {
-                active = false;
+                for (int c = 0; c < 6; ++c) waiting[up - L][c] = b[c];
+                parked = true;
             }
         }
+        __syncthreads();
+        if (meet && rank == 1u) {
+            const float* o = waiting[up - L];
+            b[0] = fminf(b[0], o[0]); b[1] = fminf(b[1], o[1]); b[2] = fminf(b[2], o[2]);
+            b[3] = fmaxf(b[3], o[3]); b[4] = fmaxf(b[4], o[4]); b[5] = fmaxf(b[5], o[5]);
+            node = up;
+#pragma unroll
+            for (int w = 0; w < 3; ++w) *pair_slot(boxes, node, w) = pack_pair(b[2 * w], b[2 * w + 1]);
+            up = parent[node];
+            merged = 1;
+        } else if (parked && arrivals[up - L] == 2u) {
+            active = false;  // the partner took this box up
+            parked = false;
+        }
+        __syncthreads();
+        if (!merged) break;
     }
     if (!active || up == 0xFFFFFFFFu) return;
     // 2. three exchange walks from the parent of this subtree's root
