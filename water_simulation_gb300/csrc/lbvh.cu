@@ -114,7 +114,8 @@ __global__ void __launch_bounds__(256) lbvh_refit_kernel(const float* __restrict
     }
 }
 
-// Refit without fences, in two phases per block of 256 consecutive leaves.
+// Refit without fences, in two phases per block of REFIT_BLOCK consecutive
+// leaves.
 //  1. In the block: every lane starts at its leaf; lanes whose current nodes
 //     share a parent meet in shared memory, one merges and climbs on, until
 //     no two lanes meet (the subtrees of the block's leaves are complete).
@@ -129,6 +130,7 @@ __global__ void __launch_bounds__(256) lbvh_refit_kernel(const float* __restrict
 //     pattern that float arithmetic never produces (its results are canonical
 //     NaNs).
 constexpr unsigned long long EMPTY_PAIR = ~0ull;
+constexpr int REFIT_BLOCK = 128;  // leaves merged in shared memory before the global walks
 
 __device__ __forceinline__ unsigned long long pack_pair(float a, float b) {
     return static_cast<unsigned long long>(__float_as_uint(a)) |
@@ -139,7 +141,7 @@ __device__ __forceinline__ unsigned long long* pair_slot(float* boxes, u32 node,
     return reinterpret_cast<unsigned long long*>(boxes + 6 * size_t(node) + 2 * w);
 }
 
-__global__ void __launch_bounds__(256) lbvh_refit_pairs_kernel(const float* __restrict__ xyz, int n, float radius,
+__global__ void __launch_bounds__(REFIT_BLOCK) lbvh_refit_pairs_kernel(const float* __restrict__ xyz, int n, float radius,
                                                                const u32* __restrict__ sorted,
                                                                const u32* __restrict__ parent, float* boxes) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -158,21 +160,22 @@ __global__ void __launch_bounds__(256) lbvh_refit_pairs_kernel(const float* __re
     }
     // 1. merges inside the block. A parent P whose both children hold leaves
     //    of this block has its whole range among them, so P, an endpoint of
-    //    its range, lies in [L, L + 256); a parent outside has a child outside.
+    //    its range, lies in [L, L + REFIT_BLOCK); a parent outside has a child
+    //    outside.
     //    Per round: lanes at such a parent count their arrival in shared
     //    memory; the first leaves its box there and waits, the second merges
     //    it (after a barrier) and climbs on. Rounds stop when nothing merged
     //    (or after 64 levels); lanes still waiting then climb globally.
-    __shared__ u32 arrivals[256];
-    __shared__ float waiting[256][6];
+    __shared__ u32 arrivals[REFIT_BLOCK];
+    __shared__ float waiting[REFIT_BLOCK][6];
     __shared__ int merged;
-    const u32 L = blockIdx.x * 256u;
+    const u32 L = blockIdx.x * static_cast<u32>(REFIT_BLOCK);
     arrivals[threadIdx.x] = 0u;
     bool parked = false;
     for (int round = 0; round < 64; ++round) {
         if (threadIdx.x == 0) merged = 0;
         __syncthreads();
-        const bool meet = active && !parked && up != 0xFFFFFFFFu && up >= L && up - L < 256u;
+        const bool meet = active && !parked && up != 0xFFFFFFFFu && up >= L && up - L < static_cast<u32>(REFIT_BLOCK);
         u32 rank = 2u;
         if (meet) {
             rank = atomicAdd(&arrivals[up - L], 1u);
@@ -269,7 +272,8 @@ void lbvh_refit(const float* xyz, u32 n, float radius, const u32* sorted, const 
     if ((reinterpret_cast<uintptr_t>(boxes) & 7u) == 0) {
         // 8-byte aligned boxes: the exchange walks (internal slots emptied first)
         if (n > 1) DFSPH_CUDA(cudaMemsetAsync(boxes, 0xFF, size_t(n - 1) * 6 * sizeof(float), st));
-        lbvh_refit_pairs_kernel<<<(n + 255) / 256, 256, 0, st>>>(xyz, int(n), radius, sorted, parent, boxes);
+        lbvh_refit_pairs_kernel<<<(n + REFIT_BLOCK - 1) / REFIT_BLOCK, REFIT_BLOCK, 0, st>>>(xyz, int(n), radius, sorted,
+                                                                                            parent, boxes);
         DFSPH_LAUNCHED();
         return;
     }
