@@ -2,8 +2,8 @@
 // core/src/spatial_accel.cu:11-40,158-179): 30-bit Morton codes of positions
 // normalised to the scene box, stably sorted.
 //
-// The sort is a least-significant-digit radix sort of four 8-bit passes over
-// tiles of 4096 keys, in nine launches:
+// The sort is a least-significant-digit radix sort of three 10-bit passes over
+// tiles of 4096 keys, in seven launches:
 //   codes   Morton codes + iota indices, the first pass's per-tile digit
 //           counts (digit-major) and its digit totals;
 //   offsets one warp per digit: digit base from the totals, prefix of the
@@ -30,11 +30,13 @@ namespace {
 constexpr int RS_BLOCK = 256;
 constexpr int RS_ROUNDS = 16;
 constexpr int RS_TILE = RS_BLOCK * RS_ROUNDS;
-constexpr int RS_BITS = 8;
+constexpr int RS_BITS = 10;
 constexpr int RS_BINS = 1 << RS_BITS;
 constexpr u32 RS_MASK = RS_BINS - 1;
 constexpr int RS_WARPS = RS_BLOCK / 32;
-constexpr int RS_PASSES = 4;
+constexpr int RS_PASSES = 3;
+constexpr int RS_DPT = RS_BINS / RS_BLOCK;  // digits per thread in the block-wide digit passes
+static_assert(RS_BINS % RS_BLOCK == 0 && RS_BITS * RS_PASSES >= 30, "radix layout");
 constexpr u32 NO_DIGIT = 0xFFFFFFFFu;
 
 // Spread the low 10 bits of v so that bit k lands on bit 3k.
@@ -158,16 +160,23 @@ __global__ void __launch_bounds__(256) radix_offsets_kernel(u32* __restrict__ hi
 constexpr int RS_SLICE = RS_TILE / RS_WARPS;
 constexpr int RS_SLICE_ROUNDS = RS_SLICE / 32;
 
+// Shared memory of the scatter (dynamic: above the static limit at 10-bit
+// digits): start, dst0, ncount [RS_BINS] each, wcnt [RS_WARPS][RS_BINS],
+// skey, sval [RS_TILE] each.
+constexpr size_t RS_SCATTER_SMEM = sizeof(u32) * (3 * RS_BINS + RS_WARPS * RS_BINS + 2 * RS_TILE);
+
 __global__ void __launch_bounds__(RS_BLOCK) radix_scatter_kernel(
     const u32* __restrict__ keys_in, const u32* __restrict__ vals_in, int n, int shift,
     const u32* __restrict__ offs, int n_tiles, u32* __restrict__ keys_out, u32* __restrict__ vals_out,
     u32* __restrict__ next_hist, u32* __restrict__ next_totals) {
-    __shared__ u32 start[RS_BINS];   // tile-local slot of the digit's first key
-    __shared__ u32 dst0[RS_BINS];    // global slot of the digit's first key of this tile
-    __shared__ u32 wcnt[RS_WARPS][RS_BINS];
+    extern __shared__ u32 rs_smem[];
+    u32* start = rs_smem;             // tile-local slot of the digit's first key
+    u32* dst0 = start + RS_BINS;      // global slot of the digit's first key of this tile
+    u32* ncount = dst0 + RS_BINS;     // next pass's digit counts of this tile's keys
+    u32* wcnt = ncount + RS_BINS;     // [warp][digit]: counts, then first slots
+    u32* skey = wcnt + RS_WARPS * RS_BINS;
+    u32* sval = skey + RS_TILE;
     __shared__ u32 wsum[RS_WARPS];
-    __shared__ u32 ncount[RS_BINS];
-    __shared__ u32 skey[RS_TILE], sval[RS_TILE];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int base = blockIdx.x * RS_TILE;
     const int count = min(RS_TILE, n - base);
@@ -180,10 +189,14 @@ __global__ void __launch_bounds__(RS_BLOCK) radix_scatter_kernel(
         keys[k] = p < count ? keys_in[base + p] : 0u;
         vals[k] = p < count ? vals_in[base + p] : 0u;
     }
-    ncount[threadIdx.x] = 0u;
-    dst0[threadIdx.x] = offs[size_t(threadIdx.x) * n_tiles + blockIdx.x];
 #pragma unroll
-    for (int w = 0; w < RS_WARPS; ++w) wcnt[w][threadIdx.x] = 0u;
+    for (int j = 0; j < RS_DPT; ++j) {
+        const int d = threadIdx.x + RS_BLOCK * j;
+        ncount[d] = 0u;
+        dst0[d] = offs[size_t(d) * n_tiles + blockIdx.x];
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; ++w) wcnt[w * RS_BINS + d] = 0u;
+    }
     __syncthreads();
     const u32 lt_mask = (1u << lane) - 1u;
     u32 rank[RS_SLICE_ROUNDS];
@@ -195,20 +208,26 @@ __global__ void __launch_bounds__(RS_BLOCK) radix_scatter_kernel(
         const int leader = __ffs(peers) - 1;
         u32 old = 0;
         if (valid && lane == leader) {
-            old = wcnt[warp][d];
-            wcnt[warp][d] = old + __popc(peers);
+            old = wcnt[warp * RS_BINS + d];
+            wcnt[warp * RS_BINS + d] = old + __popc(peers);
         }
         rank[k] = __shfl_sync(0xffffffffu, old, leader) + __popc(peers & lt_mask);
         __syncwarp();
     }
     __syncthreads();
-    // digit d (thread d): its tile count, exclusive prefix over digits, then
-    // each warp's first slot of the digit
+    // digits [RS_DPT t, RS_DPT (t + 1)) (thread t): their tile counts,
+    // exclusive prefix over digits, then each warp's first slot of the digit
     {
-        const int d = threadIdx.x;
+        u32 cd[RS_DPT];
         u32 c = 0;
 #pragma unroll
-        for (int w = 0; w < RS_WARPS; ++w) c += wcnt[w][d];
+        for (int j = 0; j < RS_DPT; ++j) {
+            const int d = RS_DPT * threadIdx.x + j;
+            cd[j] = 0;
+#pragma unroll
+            for (int w = 0; w < RS_WARPS; ++w) cd[j] += wcnt[w * RS_BINS + d];
+            c += cd[j];
+        }
         u32 x = c;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -219,19 +238,23 @@ __global__ void __launch_bounds__(RS_BLOCK) radix_scatter_kernel(
         __syncthreads();
         u32 run = x - c;
         for (int w = 0; w < warp; ++w) run += wsum[w];
-        start[d] = run;
 #pragma unroll
-        for (int w = 0; w < RS_WARPS; ++w) {
-            const u32 cw = wcnt[w][d];
-            wcnt[w][d] = run;
-            run += cw;
+        for (int j = 0; j < RS_DPT; ++j) {
+            const int d = RS_DPT * threadIdx.x + j;
+            start[d] = run;
+#pragma unroll
+            for (int w = 0; w < RS_WARPS; ++w) {
+                const u32 cw = wcnt[w * RS_BINS + d];
+                wcnt[w * RS_BINS + d] = run;
+                run += cw;
+            }
         }
     }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < RS_SLICE_ROUNDS; ++k) {
         if (slice + k * 32 + lane < count) {
-            const u32 p = wcnt[warp][(keys[k] >> shift) & RS_MASK] + rank[k];
+            const u32 p = wcnt[warp * RS_BINS + ((keys[k] >> shift) & RS_MASK)] + rank[k];
             skey[p] = keys[k];
             sval[p] = vals[k];
         }
@@ -263,7 +286,11 @@ __global__ void __launch_bounds__(RS_BLOCK) radix_scatter_kernel(
     }
     if (next_hist) {
         __syncthreads();
-        if (ncount[threadIdx.x]) atomicAdd(next_totals + threadIdx.x, ncount[threadIdx.x]);
+#pragma unroll
+        for (int j = 0; j < RS_DPT; ++j) {
+            const int d = threadIdx.x + RS_BLOCK * j;
+            if (ncount[d]) atomicAdd(next_totals + d, ncount[d]);
+        }
     }
 }
 
@@ -277,6 +304,17 @@ void morton_sort(const float* xyz, u32 n, const float smin[3], const float smax[
     for (int a = 0; a < 3; ++a) {
         const float ext = smax[a] - smin[a];
         inv[a] = ext > 0.0f ? 1.0f / ext : 0.0f;
+    }
+    {
+        // the scatter's shared memory is above the static limit: opt in once per device
+        static bool opted[64] = {};
+        int dev = 0;
+        DFSPH_CUDA(cudaGetDevice(&dev));
+        if (dev < 0 || dev >= 64 || !opted[dev]) {
+            DFSPH_CUDA(cudaFuncSetAttribute(radix_scatter_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            int(RS_SCATTER_SMEM)));
+            if (dev >= 0 && dev < 64) opted[dev] = true;
+        }
     }
     const int n_tiles = int((n + RS_TILE - 1) / RS_TILE);
     const size_t m = size_t(RS_BINS) * n_tiles;
@@ -302,8 +340,8 @@ void morton_sort(const float* xyz, u32 n, const float smin[3], const float smax[
         // the last pass writes the caller's arrays where given
         u32* ko = (last && sorted_codes) ? sorted_codes : kb;
         u32* vo = (last && sorted_idx) ? sorted_idx : vb;
-        radix_scatter_kernel<<<n_tiles, RS_BLOCK, 0, st>>>(ka, va, int(n), RS_BITS * pass, cur, n_tiles, ko, vo,
-                                                           nxt, last ? nullptr : totals + (pass + 1) * RS_BINS);
+        radix_scatter_kernel<<<n_tiles, RS_BLOCK, RS_SCATTER_SMEM, st>>>(
+            ka, va, int(n), RS_BITS * pass, cur, n_tiles, ko, vo, nxt, last ? nullptr : totals + (pass + 1) * RS_BINS);
         DFSPH_LAUNCHED();
         std::swap(ka, kb);
         std::swap(va, vb);
