@@ -401,28 +401,36 @@ def bench_frames(n_frames=24):
     return out
 
 
-def bench_precision(sc, steps=50):
+def bench_precision(sc, checkpoints=(50, 500)):
     """Field error of the FP32 step (plain and with Kahan density sums; both
     with FP64 convergence reductions) against the FP64 build of the same
-    kernels after `steps` steps from the same input."""
+    kernels, after each number of steps in `checkpoints` along one trajectory
+    from the same input."""
+    import time as _time
+
     from water_simulation_gb300 import _lib
     from water_simulation_gb300.solver import solver_for
 
-    out = {}
-    ref = None
+    fields = {}
     for name, prec in (("fp64", _lib.PRECISION_FP64), ("fp32", _lib.PRECISION_FP32),
                        ("fp32_kahan", _lib.PRECISION_FP32_KAHAN)):
         s = solver_for(sc, precision=prec)
-        s.step(sc.dt, steps)
-        f = {"x": s.field(_lib.FIELD_POSITION).astype(np.float64), "v": s.field(_lib.FIELD_VELOCITY).astype(np.float64),
-             "rho": s.field(_lib.FIELD_DENSITY).astype(np.float64)}
+        done = 0
+        fields[name] = {}
+        t0 = _time.perf_counter()
+        for c in checkpoints:
+            s.step(sc.dt, c - done)
+            done = c
+            fields[name][c] = {"x": s.field(_lib.FIELD_POSITION).astype(np.float64),
+                               "v": s.field(_lib.FIELD_VELOCITY).astype(np.float64),
+                               "rho": s.field(_lib.FIELD_DENSITY).astype(np.float64)}
+        fields[name]["wall_s"] = _time.perf_counter() - t0
         s.close()
-        if ref is None:
-            ref = f
-            continue
+
+    def errors(f, ref):
         vs = np.linalg.norm(ref["v"], axis=1).max()
         rel = np.abs(f["rho"] - ref["rho"]) / np.abs(ref["rho"])
-        out[name] = {
+        return {
             "density_max_rel": float(rel.max()),
             "density_rel_p50": float(np.percentile(rel, 50)),
             "density_rel_p99": float(np.percentile(rel, 99)),
@@ -431,7 +439,28 @@ def bench_precision(sc, steps=50):
             "position_max_abs_m": float(np.abs(f["x"] - ref["x"]).max()),
             "velocity_max_abs_rel_to_max_speed": float(np.abs(f["v"] - ref["v"]).max() / max(vs, 1e-30)),
         }
-    out["steps"] = steps
+
+    out = {}
+    first = checkpoints[0]
+    for name in ("fp32", "fp32_kahan"):
+        out[name] = errors(fields[name][first], fields["fp64"][first])  # at the first checkpoint
+        for c in checkpoints[1:]:
+            out[f"{name}_at_{c}_steps"] = errors(fields[name][c], fields["fp64"][c])
+    # the flow's own sensitivity: FP32 against FP32 from positions one ulp
+    # away, at the last checkpoint
+    import copy
+
+    moved = copy.copy(sc)
+    moved.fluid = np.nextafter(sc.fluid, np.float32(np.inf)).astype(np.float32)
+    s = solver_for(moved, precision=_lib.PRECISION_FP32)
+    s.step(sc.dt, checkpoints[-1])
+    g = {"x": s.field(_lib.FIELD_POSITION).astype(np.float64), "v": s.field(_lib.FIELD_VELOCITY).astype(np.float64),
+         "rho": s.field(_lib.FIELD_DENSITY).astype(np.float64)}
+    s.close()
+    out[f"fp32_vs_fp32_1ulp_input_at_{checkpoints[-1]}_steps"] = errors(g, fields["fp32"][checkpoints[-1]])
+    out["steps"] = first
+    out["checkpoints"] = list(checkpoints)
+    out["fp64_wall_s"] = fields["fp64"]["wall_s"]
     out["reference"] = "FP64 build of the same kernels"
     return out
 
@@ -736,7 +765,7 @@ def main():
             line["frames"] = {"unavailable": str(e)[:200]}
     if rank == 0 and not args.no_precision:
         try:
-            line["precision"] = bench_precision(sc, 50)
+            line["precision"] = bench_precision(sc)
         except Exception as e:
             line["precision"] = {"unavailable": str(e)[:200]}
     if rank == 0 and not args.no_adjoint:
