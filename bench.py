@@ -270,6 +270,7 @@ def bench_ours(args, rank, world):
            "dominant_timed_in": "warm-up steps (passes apart)" if adaptive else "timed steps",
            "nb_active": nb_active,
            "block_sizes": {k: tuned[k] for k in ("density_alpha", "pressure_rate", "pressure_apply", "forces_xsph")},
+           "warmup_raw": share,
            "warmup_share": {k: round(v[0] / max(sum(x[0] for x in share.values()), 1e-9), 4)
                             for k, v in share.items() if v[1]}}
     if not args.no_e2e:
@@ -734,6 +735,18 @@ def main():
                      "active_boundary_particles": res["nb_active"], "timed_in": res["dominant_timed_in"]},
         "kernel_share_warmup": res["warmup_share"],
     }
+    # every kernel class against the same peak (warm-up steps, per-launch
+    # events; the scan class is three launches per step, the apply class
+    # includes the fused last apply + integrator counted at the apply's bytes)
+    kr = {}
+    for k, (ms, cnt) in res["warmup_raw"].items():
+        alg = algorithmic_bytes(k, sc.n, res["nb_active"], cells)
+        if not alg or not cnt or ms <= 0:
+            continue
+        units = cnt / 3.0 if k == "grid_scan" else cnt
+        gbs = alg * units / (ms * 1e-3) / 1e9
+        kr[k] = {"GB/s": round(gbs, 1), "frac": round(gbs / hbm, 4)}
+    line["kernel_roofline_warmup"] = kr
     # the whole step against the same peak: compulsory bytes of one step
     # N (192 + 84 I) + 4 (C + 1) + 16 N_b,active (1 + 2 I), I = solver
     # iterations per step (x, v, rho, alpha, kappa and the grid arrays moved
