@@ -109,3 +109,33 @@ def test_reference_run_to_run_spread_with_xsph():
     diff = np.abs(gpu.velocities() - ref.field(1)).max()
     print(f"reference run-to-run velocity spread {spread:.3e}, GPU vs reference {diff:.3e}")
     assert diff < max(1e-2, 10 * spread)
+
+
+def test_reference_dam_break_1m_one_step():
+    """The largest configuration: the 1M-particle dam break (766,098 wall
+    particles, 8.0 M cells), one reference step. Cell keys, permutation and
+    cell_start of the fluid and wall grids bit for bit against the
+    reference's own kernels; neighbour counts bit for bit against the oracle;
+    density, positions and velocities within the one-step tolerances above."""
+    sc = scenes.dam_break(scale=2, reference_mode=True)
+    gpu = solver_for(sc, diagnostics=True)
+    inv = gpu.scalar(_lib.SCALAR_STENCIL_INV_CELL)
+    ocfg = O.config_from(sc.config(), stencil_inv_cell=inv)
+    ref = R.ReferenceRun(ocfg, sc.fluid, sc.velocity, sc.boundary)
+    assert np.array_equal(ref.field(14), gpu.field(_lib.FIELD_BOUNDARY_SORTED_INDEX))
+    assert np.array_equal(ref.field(13), gpu.field(_lib.FIELD_BOUNDARY_CELL_START))
+    ref.step(sc.dt)
+    gpu.step(sc.dt)
+    for fid_ref, fid_gpu in ((6, _lib.FIELD_CELL_KEY), (7, _lib.FIELD_SORTED_INDEX), (8, _lib.FIELD_CELL_START)):
+        assert np.array_equal(ref.field(fid_ref), gpu.field(fid_gpu)), fid_gpu
+    rho_ref = ref.field(2).astype(np.float64)
+    assert np.abs(gpu.field(_lib.FIELD_DENSITY) - rho_ref).max() / 1000.0 < 1e-5
+    assert np.abs(gpu.positions() - ref.field(0).astype(np.float64)).max() < 1e-6
+    assert np.abs(gpu.velocities() - ref.field(1).astype(np.float64)).max() < 2e-4
+    assert ref.last_density_iters() == gpu.last_density_iters() == sc.max_density_iters
+    ref.close()
+    # neighbour counts of the step just taken, against the oracle's
+    ora = O.Oracle(ocfg, sc.fluid, sc.velocity, sc.boundary, precision=32)
+    ora.step(sc.dt)
+    assert np.array_equal(ora.field(O.F_NBR_FLUID), gpu.field(_lib.FIELD_NBR_FLUID))
+    assert np.array_equal(ora.field(O.F_NBR_BOUNDARY), gpu.field(_lib.FIELD_NBR_BOUNDARY))
