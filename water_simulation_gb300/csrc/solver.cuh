@@ -150,6 +150,12 @@ public:
     ~Solver() override {
         drop_graph();
         drop_adjoint_graph();
+        if (replay_stream_) {
+            cudaStreamSynchronize(replay_stream_);
+            cudaStreamDestroy(replay_stream_);
+            for (cudaEvent_t e : {ev_start_, ev_replayed_[0], ev_replayed_[1], ev_reversed_[0], ev_reversed_[1]})
+                if (e) cudaEventDestroy(e);
+        }
         if (capture_stream_) cudaStreamDestroy(capture_stream_);
         if (loop_stream_) cudaStreamDestroy(loop_stream_);
         if (host_ctl_) cudaFreeHost(host_ctl_);
@@ -789,19 +795,14 @@ public:
         DFSPH_CUDA(cudaMemsetAsync(eps_acc_.p, 0, sizeof(double), stream_));
         DFSPH_CUDA(cudaMemsetAsync(eps_ctr_.p, 0, sizeof(u32), stream_));
         const u32 segs = (ad_steps_ + ad_every_ - 1) / ad_every_;
-        ensure_tape(std::min(ad_every_, ad_steps_));
-        for (u32 s = segs; s-- > 0;) {
-            const u32 s0 = s * ad_every_;
-            const u32 cnt = std::min(ad_every_, ad_steps_ - s0);
+        const u32 full = ad_steps_ / ad_every_;  // segments 0 .. full-1 have ad_every_ steps
+        const bool pipelined = full > 0 && profile_mask_ == 0;
+        ensure_tape(pipelined ? 2 * ad_every_ : std::min(ad_every_, ad_steps_));
+        // the segments run from the last; a shorter last segment, and every
+        // segment while the passes are profiled, run plainly
+        for (u32 s = segs; s-- > (pipelined ? full : 0u);) {
+            const u32 cnt = std::min(ad_every_, ad_steps_ - s * ad_every_);
             restore_checkpoint(s);
-            if (cnt == ad_every_ && profile_mask_ == 0) {
-                // a full segment: one launch of its captured graph
-                ensure_adjoint_graph(cnt);
-                DFSPH_CUDA(cudaGraphLaunch(adj_exec_, stream_));
-                launches_ += adj_kernels_;
-                counts_valid_ = true;  // the last replayed step counted the next one's cells
-                continue;
-            }
             {
                 const NvtxRange replay("adjoint segment replay");
                 for (u32 k = 0; k < cnt; ++k) {
@@ -811,6 +812,53 @@ public:
             }
             const NvtxRange reverse("adjoint segment reverse");
             for (u32 k = cnt; k-- > 0;) backward_step(tape_at(k));
+        }
+        if (pipelined) {
+            // Full segments: the replay of segment s - 1 (side stream, record
+            // buffer (s - 1) & 1) runs while the reverse of segment s (this
+            // stream, buffer s & 1) does; a buffer is rewritten only after
+            // the reverse that read it. The reverse kernels read only the
+            // records and the adjoint arrays, the replays write only the state
+            // and their records.
+            const NvtxRange pipe("adjoint segments, replay and reverse overlapped");
+            ensure_adjoint_graphs(ad_every_);
+            if (!replay_stream_) {
+                DFSPH_CUDA(cudaStreamCreateWithFlags(&replay_stream_, cudaStreamNonBlocking));
+                for (cudaEvent_t* e : {&ev_start_, &ev_replayed_[0], &ev_replayed_[1], &ev_reversed_[0],
+                                       &ev_reversed_[1]})
+                    DFSPH_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+            }
+            const cudaStream_t rev = stream_, side = replay_stream_;
+            DFSPH_CUDA(cudaEventRecord(ev_start_, rev));
+            DFSPH_CUDA(cudaStreamWaitEvent(side, ev_start_, 0));
+            auto replay = [&](u32 s) {
+                const u32 b = s & 1u;
+                stream_ = side;
+                try {
+                    restore_checkpoint(s);
+                } catch (...) {
+                    stream_ = rev;
+                    throw;
+                }
+                stream_ = rev;
+                DFSPH_CUDA(cudaGraphLaunch(adj_replay_[b].e, side));
+                launches_ += adj_replay_[b].kernels;
+                counts_valid_ = true;  // the last replayed step counted the next one's cells
+                DFSPH_CUDA(cudaEventRecord(ev_replayed_[b], side));
+            };
+            replay(full - 1);
+            for (u32 s = full; s-- > 0;) {
+                const u32 b = s & 1u;
+                DFSPH_CUDA(cudaStreamWaitEvent(rev, ev_replayed_[b], 0));
+                DFSPH_CUDA(cudaGraphLaunch(adj_reverse_[b].e, rev));
+                launches_ += adj_reverse_[b].kernels;
+                DFSPH_CUDA(cudaEventRecord(ev_reversed_[b], rev));
+                if (s > 0) {
+                    // buffer (s - 1) & 1 was last read by the reverse of segment s + 1
+                    if (s + 1 < full) DFSPH_CUDA(cudaStreamWaitEvent(side, ev_reversed_[(s - 1) & 1u], 0));
+                    replay(s - 1);
+                }
+            }
         }
         const size_t bytes = 3 * size_t(n) * sizeof(R);
         void* outs[2] = {x0bar, v0bar};
@@ -898,16 +946,20 @@ private:
         }
     }
 
-    // Graph of one full segment of the backward pass: the k replayed steps
-    // with their records, then the k reverse steps. Steps leave the buffer
-    // parity unchanged and the records sit at fixed addresses, so one capture
-    // serves every full segment (and every backward pass with the same k, n,
-    // dt and XSPH coefficient). The checkpoint restore before it runs outside.
-    void ensure_adjoint_graph(u32 cnt) {
-        if (adj_exec_ && adj_len_ == cnt && adj_n_ == n_ && adj_dt_ == ad_dt_ && adj_eps_ == ad_eps_ &&
-            cx_ == adj_cx_ && cv_ == adj_cv_ && ci_ == adj_ci_)
-            return;
-        drop_adjoint_graph();
+    // Graphs of the backward pass, per record buffer b (0, 1): the replay of
+    // a full segment (its k steps from the restored checkpoint, writing the
+    // records of buffer b) and its reverse (the k reverse steps reading them).
+    // Steps leave the buffer parity unchanged and the records sit at fixed
+    // addresses, so one capture serves every full segment (and every backward
+    // pass with the same k, n, dt and XSPH coefficient). Checkpoint restores
+    // run outside.
+    struct SegmentGraph {
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t e = nullptr;
+        unsigned long long kernels = 0;
+    };
+
+    template <class Body> void capture_segment_graph(SegmentGraph& sg, Body&& body) {
         if (!capture_stream_) DFSPH_CUDA(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking));
         const cudaStream_t caller = stream_;
         const unsigned long long k0 = graph_kernels_;
@@ -916,12 +968,9 @@ private:
         DFSPH_CUDA(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal));
         stream_ = capture_stream_;
         capturing_ = true;
+        counts_valid_ = false;  // a replay starts from a restored checkpoint
         try {
-            for (u32 k = 0; k < cnt; ++k) {
-                const StepTape<R> t = tape_at(k);
-                step_once(R(ad_dt_), true, &t);
-            }
-            for (u32 k = cnt; k-- > 0;) backward_step(tape_at(k));
+            body();
         } catch (...) {
             cudaGraph_t g = nullptr;
             cudaStreamEndCapture(capture_stream_, &g);
@@ -937,11 +986,29 @@ private:
         capturing_ = false;
         stream_ = caller;
         counts_valid_ = counted;
-        DFSPH_CUDA(cudaStreamEndCapture(capture_stream_, &adj_graph_));
+        DFSPH_CUDA(cudaStreamEndCapture(capture_stream_, &sg.g));
         if (cx_ != cx || cv_ != cv || ci_ != ci) throw Error(DFSPH_ERR_STATE, "a step changed buffer parity");
-        DFSPH_CUDA(cudaGraphInstantiate(&adj_exec_, adj_graph_, 0));
-        adj_kernels_ = graph_kernels_ - k0;
+        DFSPH_CUDA(cudaGraphInstantiate(&sg.e, sg.g, 0));
+        sg.kernels = graph_kernels_ - k0;
         graph_kernels_ = k0;
+    }
+
+    void ensure_adjoint_graphs(u32 cnt) {
+        if (adj_replay_[0].e && adj_len_ == cnt && adj_n_ == n_ && adj_dt_ == ad_dt_ && adj_eps_ == ad_eps_ &&
+            cx_ == adj_cx_ && cv_ == adj_cv_ && ci_ == adj_ci_)
+            return;
+        drop_adjoint_graph();
+        for (u32 b = 0; b < 2; ++b) {
+            capture_segment_graph(adj_replay_[b], [&] {
+                for (u32 k = 0; k < cnt; ++k) {
+                    const StepTape<R> t = tape_at(k, b);
+                    step_once(R(ad_dt_), true, &t);
+                }
+            });
+            capture_segment_graph(adj_reverse_[b], [&] {
+                for (u32 k = cnt; k-- > 0;) backward_step(tape_at(k, b));
+            });
+        }
         adj_len_ = cnt;
         adj_n_ = n_;
         adj_dt_ = ad_dt_;
@@ -950,15 +1017,19 @@ private:
     }
 
     void drop_adjoint_graph() {
-        if (adj_exec_) cudaGraphExecDestroy(adj_exec_);
-        if (adj_graph_) cudaGraphDestroy(adj_graph_);
-        adj_exec_ = nullptr;
-        adj_graph_ = nullptr;
+        for (SegmentGraph* sg : {&adj_replay_[0], &adj_replay_[1], &adj_reverse_[0], &adj_reverse_[1]}) {
+            if (sg->e) cudaGraphExecDestroy(sg->e);
+            if (sg->g) cudaGraphDestroy(sg->g);
+            sg->e = nullptr;
+            sg->g = nullptr;
+        }
     }
-    StepTape<R> tape_at(u32 k) {
+    // Records of step k of a segment in record buffer buf (buffers of
+    // ad_every_ steps each).
+    StepTape<R> tape_at(u32 k, u32 buf = 0) {
         const size_t np = tape_stride();
         const size_t kd = cfg_.max_divergence_iters, kr = cfg_.max_density_iters;
-        unsigned char* q = tape_.p + tape_step_bytes() * k;
+        unsigned char* q = tape_.p + tape_step_bytes() * (size_t(buf) * ad_every_ + k);
         auto take = [&](size_t bytes) {
             unsigned char* r = q;
             q += align256(bytes);
@@ -1654,12 +1725,12 @@ private:
     float ad_dt_ = 0.0f, ad_eps_ = 0.0f;
     DevBuf<V4> ck_;
     DevBuf<unsigned char> tape_, ad_staging_;
-    cudaGraph_t adj_graph_ = nullptr;
-    cudaGraphExec_t adj_exec_ = nullptr;
+    SegmentGraph adj_replay_[2], adj_reverse_[2];
     u32 adj_len_ = 0, adj_n_ = 0;
     float adj_dt_ = 0.0f, adj_eps_ = 0.0f;
     int adj_cx_ = 0, adj_cv_ = 0, adj_ci_ = 0;
-    unsigned long long adj_kernels_ = 0;
+    cudaStream_t replay_stream_ = nullptr;  // replays overlap the reverse of the segment after them
+    cudaEvent_t ev_start_ = nullptr, ev_replayed_[2] = {nullptr, nullptr}, ev_reversed_[2] = {nullptr, nullptr};
     DevBuf<V4> xg_, vg_, xbar_, vbar_[2], xr_, xq_, gq_;
     DevBuf<R> rhobar_, alphabar_;
     DevBuf<double> eps_part_, eps_acc_;
