@@ -241,8 +241,11 @@ int dfsph_adjoint_forward(dfsph_ctx* ctx, float dt, uint32_t n_steps, uint32_t c
  * dL/dv_0 (either output may be NULL) and *xsph_bar = dL/d(XSPH coefficient)
  * accumulated in FP64 (may be NULL). Each segment between checkpoints is
  * replayed once with its per-step records (neighbour structure included),
- * then differentiated step by step in reverse. The context is left at the
- * rollout's final state. */
+ * then differentiated step by step in reverse; the replay of the next segment
+ * runs beside the reverse of the current one, so the records of two segments
+ * are held at once (about 2 x checkpoint_every x 300 bytes per particle in
+ * FP32). Stream-ordered on the context's stream (plus a side stream of its
+ * own). The context is left at the rollout's final state. */
 int dfsph_adjoint_backward(dfsph_ctx* ctx, const void* pos_bar, const void* vel_bar, void* pos0_bar,
                            void* vel0_bar, double* xsph_bar, int mem);
 
