@@ -35,11 +35,19 @@ __device__ __forceinline__ int common_prefix(const u32* __restrict__ codes, int 
     return a != b ? __clz(a ^ b) : 32 + __clz(static_cast<u32>(i) ^ static_cast<u32>(j));
 }
 
+// empty_slots, when given, is the box array viewed as 8-byte words: node i's
+// box slot (3 words) is set to the all-ones pattern the box pass starts from.
 __global__ void __launch_bounds__(256) lbvh_internal_kernel(const u32* __restrict__ codes, int n,
                                                             u32* __restrict__ left, u32* __restrict__ right,
-                                                            u32* __restrict__ parent) {
+                                                            u32* __restrict__ parent,
+                                                            unsigned long long* __restrict__ empty_slots) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
+    if (empty_slots) {
+        empty_slots[3 * size_t(i)] = ~0ull;
+        empty_slots[3 * size_t(i) + 1] = ~0ull;
+        empty_slots[3 * size_t(i) + 2] = ~0ull;
+    }
     if (i == 0) parent[0] = 0xFFFFFFFFu;  // the root
     // the node's range extends towards the neighbour sharing the longer prefix
     const int d = common_prefix(codes, n, i, i + 1) > common_prefix(codes, n, i, i - 1) ? 1 : -1;
@@ -253,25 +261,16 @@ __global__ void __launch_bounds__(256) cohesion_kernel(const float* __restrict__
 
 }  // namespace
 
-void lbvh_build(const float* xyz, u32 n, const float smin[3], const float smax[3], float radius, u32* codes,
-                u32* sorted, u32* left, u32* right, u32* parent, float* boxes, u32* scratch, cudaStream_t st) {
-    if (n == 0) return;
-    morton_sort(xyz, n, smin, smax, codes, sorted, st);
-    if (n > 1) {
-        lbvh_internal_kernel<<<(n - 1 + 255) / 256, 256, 0, st>>>(codes, int(n), left, right, parent);
-        DFSPH_LAUNCHED();
-    } else {
-        DFSPH_CUDA(cudaMemsetAsync(parent, 0xFF, sizeof(u32), st));  // the single leaf is the root
-    }
-    lbvh_refit(xyz, n, radius, sorted, left, right, parent, boxes, scratch, st);
-}
+namespace {
+bool pair_aligned(const float* boxes) { return (reinterpret_cast<uintptr_t>(boxes) & 7u) == 0; }
 
-void lbvh_refit(const float* xyz, u32 n, float radius, const u32* sorted, const u32* left, const u32* right,
-                const u32* parent, float* boxes, u32* scratch, cudaStream_t st) {
+void refit_boxes(const float* xyz, u32 n, float radius, const u32* sorted, const u32* left, const u32* right,
+                 const u32* parent, float* boxes, u32* scratch, bool slots_empty, cudaStream_t st) {
     if (n == 0) return;
-    if ((reinterpret_cast<uintptr_t>(boxes) & 7u) == 0) {
+    if (pair_aligned(boxes)) {
         // 8-byte aligned boxes: the exchange walks (internal slots emptied first)
-        if (n > 1) DFSPH_CUDA(cudaMemsetAsync(boxes, 0xFF, size_t(n - 1) * 6 * sizeof(float), st));
+        if (n > 1 && !slots_empty)
+            DFSPH_CUDA(cudaMemsetAsync(boxes, 0xFF, size_t(n - 1) * 6 * sizeof(float), st));
         lbvh_refit_pairs_kernel<<<(n + REFIT_BLOCK - 1) / REFIT_BLOCK, REFIT_BLOCK, 0, st>>>(xyz, int(n), radius, sorted,
                                                                                             parent, boxes);
         DFSPH_LAUNCHED();
@@ -281,6 +280,28 @@ void lbvh_refit(const float* xyz, u32 n, float radius, const u32* sorted, const 
     lbvh_refit_kernel<<<(n + 255) / 256, 256, 0, st>>>(xyz, int(n), radius, sorted, left, right, parent, boxes,
                                                         scratch);
     DFSPH_LAUNCHED();
+}
+}  // namespace
+
+void lbvh_build(const float* xyz, u32 n, const float smin[3], const float smax[3], float radius, u32* codes,
+                u32* sorted, u32* left, u32* right, u32* parent, float* boxes, u32* scratch, cudaStream_t st) {
+    if (n == 0) return;
+    morton_sort(xyz, n, smin, smax, codes, sorted, st);
+    // the internal-node pass also empties the internal box slots for the box pass
+    const bool fill = pair_aligned(boxes);
+    if (n > 1) {
+        lbvh_internal_kernel<<<(n - 1 + 255) / 256, 256, 0, st>>>(
+            codes, int(n), left, right, parent, fill ? reinterpret_cast<unsigned long long*>(boxes) : nullptr);
+        DFSPH_LAUNCHED();
+    } else {
+        DFSPH_CUDA(cudaMemsetAsync(parent, 0xFF, sizeof(u32), st));  // the single leaf is the root
+    }
+    refit_boxes(xyz, n, radius, sorted, left, right, parent, boxes, scratch, fill, st);
+}
+
+void lbvh_refit(const float* xyz, u32 n, float radius, const u32* sorted, const u32* left, const u32* right,
+                const u32* parent, float* boxes, u32* scratch, cudaStream_t st) {
+    refit_boxes(xyz, n, radius, sorted, left, right, parent, boxes, scratch, false, st);
 }
 
 void cohesion(const float* r, u32 n, float l, float* out, cudaStream_t st) {
