@@ -1444,7 +1444,7 @@ private:
             launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R, false, 128>, pressure_apply_kernel<R, false, 256>, n, xout,
                    vr_[cv_].p, kap_it, cs, g_, phys_, bdev(), sd, ctl, it, (const V4*)nullptr, (const u32*)nullptr);
             launched = it + 1;
-            if (adaptive && it >= first_check) {
+            if (adaptive && it + 1 > first_check) {  // it >= first_check
                 // The reference reads the error back every iteration
                 // (dfsph.cu:296-299); the device already decided, the host
                 // only stops launching.
