@@ -29,6 +29,9 @@ frames     sim_cli's frame loop on the puddle block: substeps chosen on the
            device inside one graph launch per frame, against the host loop.
 adjoint    the differentiable drop (32,768 particles, 200 steps, checkpoint
            every 20): backward time over forward time.
+puddle_adaptive  the settled puddle with the reference's adaptive density
+           solve (its own CPU-runnable case), against the reference's kernels
+           over the same steps.
 lbvh       SpatialAccel::build on the workload's fluid positions: this
            build's dfsph_lbvh_build (+ boxes) and dfsph_lbvh_refit against the
            reference's own kernels under its restated orchestration, outputs
@@ -83,6 +86,7 @@ def parse():
     ap.add_argument("--no-frames", action="store_true", help="skip the device-stepped frame timing")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default 128-thread neighbour passes")
     ap.add_argument("--no-lbvh", action="store_true", help="skip the LBVH build/refit timing")
+    ap.add_argument("--no-puddle", action="store_true", help="skip the adaptive-puddle leg")
     return ap.parse_args()
 
 
@@ -540,6 +544,38 @@ def cpu_sample(sc, steps, threads=0):
             "ms_per_step": 1e3 * sec / steps}
 
 
+def bench_puddle_adaptive(steps=50, warmup=5):
+    """The settled puddle as the reference runs it (adaptive density solve at
+    0.01 %, at most 100 iterations, no divergence solver): steps
+    warmup+1 .. warmup+steps with CUDA events, and the reference's own kernels
+    over the same steps."""
+    import torch
+
+    from water_simulation_gb300.solver import solver_for
+
+    sc = make_scene("puddle_adaptive")
+    stream = torch.cuda.current_stream()
+    s = solver_for(sc, stream=stream.cuda_stream)
+    for _ in range(warmup):
+        s.step(sc.dt)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        s.step(sc.dt)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    s.close()
+    res = {"workload": sc.name, "particles": sc.n, "steps": f"{warmup + 1}-{warmup + steps}", "ms_per_step": ms,
+           "particle_steps_per_s": sc.n / (ms * 1e-3)}
+    ref = bench_ref_cuda(sc, steps, warmup)
+    res["ref_cuda"] = ref
+    if "ms_per_step" in ref:
+        res["speedup_vs_ref_cuda"] = ref["ms_per_step"] / ms
+    return res
+
+
 def bench_lbvh(sc, reps=20, warmup=3):
     """dfsph_lbvh_build / dfsph_lbvh_refit on the fluid positions of the
     workload (scene box = the domain), CUDA events over `reps` launches after
@@ -789,6 +825,11 @@ def main():
                                                             graphed["backward_over_forward"])}
         except Exception as e:
             line["adjoint"] = {"unavailable": str(e)[:200]}
+    if rank == 0 and not args.no_puddle:
+        try:
+            line["puddle_adaptive"] = bench_puddle_adaptive()
+        except Exception as e:
+            line["puddle_adaptive"] = {"unavailable": str(e)[:200]}
     if rank == 0 and not args.no_lbvh:
         try:
             line["lbvh"] = bench_lbvh(sc)
