@@ -73,6 +73,12 @@ template <class R> struct NbrSrc {
     const u32* rb = nullptr;
     const u32* re = nullptr;
     int stride = 0;
+    // the same for the wall runs (wrb/wre) and, when staged, the wall records
+    // of slots wlo .. (wx)
+    const u32* wrb = nullptr;
+    const u32* wre = nullptr;
+    const R4<R>* wx = nullptr;
+    u32 wlo = 0;
 };
 
 // The stencil's runs from NbrSrc's table when it has one, else from cell_start
@@ -799,15 +805,24 @@ __device__ __forceinline__ double rate_particle(int i, const R4<R>* __restrict__
     if (bd.has && boundary_near(c, g, bd.mask)) {
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
         R rb = 0;
-        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
-            for (u32 j = b; j < e; ++j) {
-                const R4<R> pj = ld(xb + j);
-                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-                R rinv;
-                const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
-                rb += pj.w * grad_factor(r, rinv, p) * (vi.x * rx + vi.y * ry + vi.z * rz);
+        auto wall = [&](const R4<R>& pj) {
+            const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+            R rinv;
+            const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
+            rb += pj.w * grad_factor(r, rinv, p) * (vi.x * rx + vi.y * ry + vi.z * rz);
+        };
+        if (COHERENT && src.wrb) {
+            // the wall runs from the per-launch table, records from shared memory when staged
+#pragma unroll 1
+            for (int k = 0; k < 9; ++k) {
+                const u32 b = src.wrb[k * src.stride], e = src.wre[k * src.stride];
+                for (u32 j = b; j < e; ++j) wall(src.wx ? src.wx[j - src.wlo] : ld(xb + j));
             }
-        });
+        } else {
+            for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+                for (u32 j = b; j < e; ++j) wall(ld(xb + j));
+            });
+        }
         rd += rb;
     }
     const R rho = vi.w;
@@ -915,16 +930,24 @@ __device__ __forceinline__ R4<R> apply_velocity(int i, const R4<R>* __restrict__
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
         const R kb = pi.w + kap[i] / rmax(p.rho0 * p.rho0, R(1e-9));
         R bx = 0, by = 0, bz = 0;
-        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
-            for (u32 j = b; j < e; ++j) {
-                const R4<R> pj = ld(xb + j);
-                const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-                R rinv;
-                const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
-                const R f = pj.w * grad_factor(r, rinv, p);
-                bx += f * rx; by += f * ry; bz += f * rz;
+        auto wall = [&](const R4<R>& pj) {
+            const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+            R rinv;
+            const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
+            const R f = pj.w * grad_factor(r, rinv, p);
+            bx += f * rx; by += f * ry; bz += f * rz;
+        };
+        if (COHERENT && src.wrb) {
+#pragma unroll 1
+            for (int k = 0; k < 9; ++k) {
+                const u32 b = src.wrb[k * src.stride], e = src.wre[k * src.stride];
+                for (u32 j = b; j < e; ++j) wall(src.wx ? src.wx[j - src.wlo] : ld(xb + j));
             }
-        });
+        } else {
+            for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+                for (u32 j = b; j < e; ++j) wall(ld(xb + j));
+            });
+        }
         const R sb = -dt * kb;
         ax += sb * bx; ay += sb * by; az += sb * bz;
     }
@@ -967,17 +990,21 @@ template <class R, bool DIV, int LB>
 __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
     int n, R4<R>* xa, R4<R>* xb, R4<R>* vr, const R* __restrict__ alpha, R* rho_adv, R* kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, double* partials,
-    IterCtl* ctl, u32 max_iters, u32 first_check, double inv_n, double threshold, u32 stage_cap) {
+    IterCtl* ctl, u32 max_iters, u32 first_check, double inv_n, double threshold, u32 stage_cap,
+    u32 wall_cap) {
     namespace cg = cooperative_groups;
     cg::grid_group grid = cg::this_grid();
     extern __shared__ __align__(16) unsigned char jacobi_stage[];
     R4<R>* sx = reinterpret_cast<R4<R>*>(jacobi_stage);
     R4<R>* sv = sx + stage_cap;
+    R4<R>* swx = sv + stage_cap;  // wall records, staged once per launch
     __shared__ double sh[LB / 32];
     __shared__ double part[JACOBI_SOLVE_MAX_BLOCKS];
     __shared__ int stop;
     __shared__ u32 span_lo, span_hi;
     __shared__ u32 run_b[9 * LB], run_e[9 * LB];
+    __shared__ u32 wrun_b[9 * LB], wrun_e[9 * LB];
+    __shared__ u32 wspan_lo, wspan_hi;
     const R dt = step_dt(sd);
     const int i = blockIdx.x * LB + threadIdx.x;
     // the slot range [lo, hi) that this block's stencils read (the grid does
@@ -985,12 +1012,16 @@ __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
     if (threadIdx.x == 0) {
         span_lo = 0xFFFFFFFFu;
         span_hi = 0u;
+        wspan_lo = 0xFFFFFFFFu;
+        wspan_hi = 0u;
     }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
         run_b[k * LB + threadIdx.x] = 0u;
         run_e[k * LB + threadIdx.x] = 0u;
+        wrun_b[k * LB + threadIdx.x] = 0u;
+        wrun_e[k * LB + threadIdx.x] = 0u;
     }
     if (i < n) {
         const R4<R> pi = ld_coh(xa + i);
@@ -1009,6 +1040,32 @@ __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
             atomicMin(&span_lo, lo);
             atomicMax(&span_hi, hi);
         }
+        // the wall runs of a particle near the walls (they never change)
+        const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
+        if (bd.has && boundary_near(c, g, bd.mask)) {
+            u32 wl = 0xFFFFFFFFu, wh = 0u;
+            int kw = 0;
+            for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+                if (b < e) {
+                    wrun_b[kw * LB + threadIdx.x] = b;
+                    wrun_e[kw * LB + threadIdx.x] = e;
+                    ++kw;
+                    wl = min(wl, b);
+                    wh = max(wh, e);
+                }
+            });
+            if (wh > wl) {
+                atomicMin(&wspan_lo, wl);
+                atomicMax(&wspan_hi, wh);
+            }
+        }
+    }
+    __syncthreads();
+    const u32 wlo = wspan_lo, whi = wspan_hi;
+    const bool wstaged = whi > wlo && whi - wlo <= wall_cap;
+    if (wstaged) {
+        const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
+        for (u32 k = threadIdx.x; k < whi - wlo; k += LB) swx[k] = ld(xb + wlo + k);
     }
     __syncthreads();
     const u32 lo = span_lo, hi = span_hi;
@@ -1022,6 +1079,10 @@ __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
         src.rb = run_b + threadIdx.x;
         src.re = run_e + threadIdx.x;
         src.stride = LB;
+        src.wrb = wrun_b + threadIdx.x;
+        src.wre = wrun_e + threadIdx.x;
+        src.wx = wstaged ? swx : nullptr;
+        src.wlo = wlo;
         if (staged) {
             for (u32 k = threadIdx.x; k < count; k += LB) {
                 sx[k] = ld_coh(xin + lo + k);

@@ -1481,9 +1481,11 @@ private:
         if (lb != 128 && lb != 256) return false;
         const int n = int(n_);
         const int blocks = blocks_for(n, lb);
-        // neighbour records staged per block: 2 x stage_cap of them
-        constexpr size_t kStageBytes = 96 * 1024;
-        const u32 stage_cap = static_cast<u32>(kStageBytes / (2 * sizeof(V4)));
+        // neighbour records staged per block: 2 x stage_cap fluid records
+        // (96 KB) and wall_cap wall records (32 KB)
+        constexpr size_t kStageBytes = 128 * 1024;
+        const u32 stage_cap = static_cast<u32>(96 * 1024 / (2 * sizeof(V4)));
+        const u32 wall_cap = static_cast<u32>(32 * 1024 / sizeof(V4));
         int& cap = coop_blocks_[DIV ? 1 : 0][lb == 256 ? 1 : 0];
         if (cap < 0) {
             int per_sm = 0, sms = 0;
@@ -1522,11 +1524,11 @@ private:
         if (lb == 128)
             e = cudaLaunchKernelEx(&lc, jacobi_solve_kernel<R, DIV, 128>, n, xa, xb, vr_[cv_].p, (const R*)alpha_.p,
                                    adv_out, kap_out, cs, g_, phys_, bdev(), sd, partials_.p, ctl, max_iters,
-                                   first_check, inv_n, thr, stage_cap);
+                                   first_check, inv_n, thr, stage_cap, wall_cap);
         else
             e = cudaLaunchKernelEx(&lc, jacobi_solve_kernel<R, DIV, 256>, n, xa, xb, vr_[cv_].p, (const R*)alpha_.p,
                                    adv_out, kap_out, cs, g_, phys_, bdev(), sd, partials_.p, ctl, max_iters,
-                                   first_check, inv_n, thr, stage_cap);
+                                   first_check, inv_n, thr, stage_cap, wall_cap);
         if (e == cudaErrorCooperativeLaunchTooLarge && !capturing_) {
             // fewer SMs than the device reports (a partitioned GPU): the
             // per-pass solve from now on
