@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <utility>
 #include <stdexcept>
 #include <string>
 
@@ -109,6 +110,23 @@ __device__ __forceinline__ u32 cell_key(R px, R py, R pz, const GridDev<R>& g) {
 // (griddepcontrol.wait; without the launch attribute it returns at once).
 // Every kernel of the step calls it before touching global memory.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+// A launch with programmatic stream serialization; the kernel must begin with
+// pdl_wait().
+template <class... P, class... A>
+inline void launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A&&... args) {
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = grid;
+    lc.blockDim = block;
+    lc.dynamicSmemBytes = smem;
+    lc.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    lc.attrs = at;
+    lc.numAttrs = 1;
+    DFSPH_CUDA(cudaLaunchKernelEx(&lc, kernel, std::forward<A>(args)...));
+}
 
 // Stencil-centre cell (dfsph_kernels.cu:15-17) clamped to [-2, dims+1]: any
 // value outside that range selects no cell on that axis, exactly as the

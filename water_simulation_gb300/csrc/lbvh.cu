@@ -41,6 +41,7 @@ __global__ void __launch_bounds__(256) lbvh_internal_kernel(const u32* __restric
                                                             u32* __restrict__ left, u32* __restrict__ right,
                                                             u32* __restrict__ parent,
                                                             unsigned long long* __restrict__ empty_slots) {
+    pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n - 1) return;
     if (empty_slots) {
@@ -93,6 +94,7 @@ __global__ void __launch_bounds__(256) lbvh_refit_kernel(const float* __restrict
                                                          const u32* __restrict__ sorted, const u32* __restrict__ left,
                                                          const u32* __restrict__ right, const u32* __restrict__ parent,
                                                          float* boxes, u32* arrivals) {
+    pdl_wait();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const u32 p = sorted[k];
@@ -152,6 +154,7 @@ __device__ __forceinline__ unsigned long long* pair_slot(float* boxes, u32 node,
 __global__ void __launch_bounds__(REFIT_BLOCK) lbvh_refit_pairs_kernel(const float* __restrict__ xyz, int n, float radius,
                                                                const u32* __restrict__ sorted,
                                                                const u32* __restrict__ parent, float* boxes) {
+    pdl_wait();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     bool active = k < n;
     float b[6] = {0, 0, 0, 0, 0, 0};
@@ -271,14 +274,14 @@ void refit_boxes(const float* xyz, u32 n, float radius, const u32* sorted, const
         // 8-byte aligned boxes: the exchange walks (internal slots emptied first)
         if (n > 1 && !slots_empty)
             DFSPH_CUDA(cudaMemsetAsync(boxes, 0xFF, size_t(n - 1) * 6 * sizeof(float), st));
-        lbvh_refit_pairs_kernel<<<(n + REFIT_BLOCK - 1) / REFIT_BLOCK, REFIT_BLOCK, 0, st>>>(xyz, int(n), radius, sorted,
-                                                                                            parent, boxes);
+        launch_pdl(lbvh_refit_pairs_kernel, (n + REFIT_BLOCK - 1) / REFIT_BLOCK, REFIT_BLOCK, 0, st, xyz, int(n),
+                   radius, sorted, parent, boxes);
         DFSPH_LAUNCHED();
         return;
     }
     if (n > 1) DFSPH_CUDA(cudaMemsetAsync(scratch, 0, size_t(n - 1) * sizeof(u32), st));
-    lbvh_refit_kernel<<<(n + 255) / 256, 256, 0, st>>>(xyz, int(n), radius, sorted, left, right, parent, boxes,
-                                                        scratch);
+    launch_pdl(lbvh_refit_kernel, (n + 255) / 256, 256, 0, st, xyz, int(n), radius, sorted, left, right, parent, boxes,
+               scratch);
     DFSPH_LAUNCHED();
 }
 }  // namespace
@@ -290,8 +293,8 @@ void lbvh_build(const float* xyz, u32 n, const float smin[3], const float smax[3
     // the internal-node pass also empties the internal box slots for the box pass
     const bool fill = pair_aligned(boxes);
     if (n > 1) {
-        lbvh_internal_kernel<<<(n - 1 + 255) / 256, 256, 0, st>>>(
-            codes, int(n), left, right, parent, fill ? reinterpret_cast<unsigned long long*>(boxes) : nullptr);
+        launch_pdl(lbvh_internal_kernel, (n - 1 + 255) / 256, 256, 0, st, (const u32*)codes, int(n), left, right, parent,
+                   fill ? reinterpret_cast<unsigned long long*>(boxes) : nullptr);
         DFSPH_LAUNCHED();
     } else {
         DFSPH_CUDA(cudaMemsetAsync(parent, 0xFF, sizeof(u32), st));  // the single leaf is the root

@@ -81,6 +81,7 @@ __global__ void __launch_bounds__(RS_BLOCK) morton_codes_kernel(int n, const flo
                                                                 u32* __restrict__ codes, u32* __restrict__ idx,
                                                                 u32* __restrict__ hist, int n_tiles,
                                                                 u32* __restrict__ totals) {
+    pdl_wait();
     __shared__ u32 h[RS_BINS];
 #pragma unroll
     for (int j = 0; j < RS_BINS / RS_BLOCK; ++j) h[threadIdx.x + RS_BLOCK * j] = 0u;
@@ -112,6 +113,7 @@ __global__ void __launch_bounds__(RS_BLOCK) morton_codes_kernel(int n, const flo
 __global__ void __launch_bounds__(256) radix_offsets_kernel(u32* __restrict__ hist, int n_tiles,
                                                             const u32* __restrict__ totals,
                                                             u32* __restrict__ next_hist) {
+    pdl_wait();
     __shared__ u32 tot[RS_BINS];
 #pragma unroll
     for (int j = 0; j < RS_BINS / 256; ++j) tot[threadIdx.x + 256 * j] = totals[threadIdx.x + 256 * j];
@@ -169,6 +171,7 @@ __global__ void __launch_bounds__(RS_BLOCK) radix_scatter_kernel(
     const u32* __restrict__ keys_in, const u32* __restrict__ vals_in, int n, int shift,
     const u32* __restrict__ offs, int n_tiles, u32* __restrict__ keys_out, u32* __restrict__ vals_out,
     u32* __restrict__ next_hist, u32* __restrict__ next_totals) {
+    pdl_wait();
     extern __shared__ u32 rs_smem[];
     u32* start = rs_smem;             // tile-local slot of the digit's first key
     u32* dst0 = start + RS_BINS;      // global slot of the digit's first key of this tile
@@ -328,20 +331,22 @@ void morton_sort(const float* xyz, u32 n, const float smin[3], const float smax[
     u32* hist[2] = {vb + n, vb + n + m};
     u32* totals = vb + n + 2 * m;
     DFSPH_CUDA(cudaMemsetAsync(totals, 0, RS_PASSES * RS_BINS * sizeof(u32), st));
-    morton_codes_kernel<<<n_tiles, RS_BLOCK, 0, st>>>(int(n), xyz, smin[0], smin[1], smin[2], inv[0], inv[1],
-                                                      inv[2], ka, va, hist[0], n_tiles, totals);
+    launch_pdl(morton_codes_kernel, n_tiles, RS_BLOCK, 0, st, int(n), xyz, smin[0], smin[1], smin[2], inv[0], inv[1],
+               inv[2], ka, va, hist[0], n_tiles, totals);
     DFSPH_LAUNCHED();
     for (int pass = 0; pass < RS_PASSES; ++pass) {
         const bool last = pass == RS_PASSES - 1;
         u32* cur = hist[pass & 1];
         u32* nxt = last ? nullptr : hist[(pass + 1) & 1];
-        radix_offsets_kernel<<<RS_BINS / 8, 256, 0, st>>>(cur, n_tiles, totals + pass * RS_BINS, nxt);
+        launch_pdl(radix_offsets_kernel, RS_BINS / 8, 256, 0, st, cur, n_tiles, (const u32*)(totals + pass * RS_BINS),
+                   nxt);
         DFSPH_LAUNCHED();
         // the last pass writes the caller's arrays where given
         u32* ko = (last && sorted_codes) ? sorted_codes : kb;
         u32* vo = (last && sorted_idx) ? sorted_idx : vb;
-        radix_scatter_kernel<<<n_tiles, RS_BLOCK, RS_SCATTER_SMEM, st>>>(
-            ka, va, int(n), RS_BITS * pass, cur, n_tiles, ko, vo, nxt, last ? nullptr : totals + (pass + 1) * RS_BINS);
+        launch_pdl(radix_scatter_kernel, n_tiles, RS_BLOCK, RS_SCATTER_SMEM, st, (const u32*)ka, (const u32*)va,
+                   int(n), RS_BITS * pass, (const u32*)cur, n_tiles, ko, vo, nxt,
+                   last ? nullptr : totals + (pass + 1) * RS_BINS);
         DFSPH_LAUNCHED();
         std::swap(ka, kb);
         std::swap(va, vb);
