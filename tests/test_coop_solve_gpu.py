@@ -71,3 +71,35 @@ def test_cooperative_solve_inside_device_frames():
     assert list(sd) == list(sh)
     assert np.array_equal(dev.positions(), host.positions())
     assert np.array_equal(dev.velocities(), host.velocities())
+
+
+def test_cooperative_solve_batched_scenes():
+    """A batched context (4 scenes of 1,000-6,000 particles) with adaptive
+    solves: one cooperative launch per solve over all scenes, equal bit for
+    bit to the per-pass solve."""
+    scs, eps = scenes.batched_blocks(n_scenes=4, n_min=1000, n_max=6000)
+
+    def run(profile):
+        cfg = scs[0].config(capacity=sum(s.n for s in scs))
+        cfg.n_scenes = 4
+        cfg.max_density_iters, cfg.max_divergence_iters = 100, 100
+        cfg.eta_density, cfg.eta_divergence = 1e-4, 1e-3
+        s = Solver(cfg)
+        s.set_boundary(scs[0].boundary)
+        s.set_fluid_batch([c.fluid for c in scs], [c.velocity for c in scs])
+        s.set_scene_viscosity(eps)
+        if profile:
+            s.profile_enable(ALL_CLASSES)
+        l0 = s.kernel_launches()
+        for _ in range(8):
+            s.step(scs[0].dt)
+        out = (s.positions(), s.velocities(), s.last_density_iters(), s.last_divergence_iters(),
+               s.kernel_launches() - l0)
+        s.close()
+        return out
+
+    x0, v0, d0, g0, l0 = run(False)
+    x1, v1, d1, g1, l1 = run(True)
+    assert (d0, g0) == (d1, g1) and d0 >= 2
+    assert np.array_equal(x0, x1) and np.array_equal(v0, v1)
+    assert l0 < l1
