@@ -976,29 +976,33 @@ __global__ void __launch_bounds__(LB) pressure_apply_kernel(
 // A whole adaptive Jacobi solve in one cooperative launch, every block
 // resident (small scenes, where a solve of many short passes is bound by
 // launches): per iteration the rate pass, a grid barrier, the stop decision,
-// the apply pass and a second barrier. Every block sums the block partials in
-// block order, as finish_reduction does, so all blocks take the same decision
-// and stop after the same iteration. Even iterations read positions from xa
+// the apply pass and a second barrier. Even iterations read positions from xa
 // and write (x, kappa / rho^2) to xb, odd ones the other way round, as the
-// graph-resident loop does. Launched with the rate pass's block size, so the
-// partial sums, and with them the iteration count, equal the per-launch
-// solve's. Records written inside the launch are read with ld_coh; a block
-// whose stencils read at most stage_cap consecutive slots copies them into
-// shared memory once per pass (dynamic shared memory: 2 x stage_cap records).
+// graph-resident loop does. Blocks of LB particles (as few as keep one block
+// per SM, so that a small scene spreads over many SMs) are independent of the
+// per-pass kernels' block size pass_block: every warp leaves the shuffle-tree
+// sum of its 32 particles' error terms in wsums, and after the barrier every
+// block rebuilds the per-pass partials from them (each the sum of its
+// pass_block / 32 warp sums in warp order, as block_sum_dyn adds them) and
+// sums those in block order (finish_reduction). The error sum, and with it the
+// iteration count, is therefore the per-pass solve's bit for bit, and all
+// blocks take the same decision. Records written inside the launch are read
+// with ld_coh; a block whose stencils read at most stage_cap consecutive slots
+// copies them into shared memory once per pass (dynamic shared memory:
+// 2 x stage_cap records).
 constexpr int JACOBI_SOLVE_MAX_BLOCKS = 256;
 template <class R, bool DIV, int LB>
 __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
     int n, R4<R>* xa, R4<R>* xb, R4<R>* vr, const R* __restrict__ alpha, R* rho_adv, R* kap,
-    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, double* partials,
+    const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, double* wsums,
     IterCtl* ctl, u32 max_iters, u32 first_check, double inv_n, double threshold, u32 stage_cap,
-    u32 wall_cap) {
+    u32 wall_cap, u32 pass_block) {
     namespace cg = cooperative_groups;
     cg::grid_group grid = cg::this_grid();
     extern __shared__ __align__(16) unsigned char jacobi_stage[];
     R4<R>* sx = reinterpret_cast<R4<R>*>(jacobi_stage);
     R4<R>* sv = sx + stage_cap;
     R4<R>* swx = sv + stage_cap;  // wall records, staged once per launch
-    __shared__ double sh[LB / 32];
     __shared__ double part[JACOBI_SOLVE_MAX_BLOCKS];
     __shared__ int stop;
     __shared__ u32 span_lo, span_hi;
@@ -1007,6 +1011,9 @@ __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
     __shared__ u32 wspan_lo, wspan_hi;
     const R dt = step_dt(sd);
     const int i = blockIdx.x * LB + threadIdx.x;
+    const u32 n_warps = (static_cast<u32>(n) + 31u) / 32u;
+    const u32 wpb = pass_block / 32u;                     // warps per per-pass block
+    const u32 n_pass = (n_warps + wpb - 1u) / wpb;        // per-pass blocks
     // the slot range [lo, hi) that this block's stencils read (the grid does
     // not change during the solve); staged in shared memory when it fits
     if (threadIdx.x == 0) {
@@ -1096,15 +1103,25 @@ __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
         double err = 0;
         if (i < n)
             err = rate_particle<R, DIV, true>(i, xin, xout, vr, alpha, rho_adv, kap, cs, g, p, bd, dt, nullptr, src);
-        const double t = block_sum_dyn(err, sh);
-        if (threadIdx.x == 0) partials[blockIdx.x] = t;
+        // the warp's share of block_sum_dyn: the same shuffle tree
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) err += __shfl_down_sync(0xffffffffu, err, o);
+        const u32 warp = (blockIdx.x * LB + threadIdx.x) >> 5;
+        if ((threadIdx.x & 31) == 0 && warp < n_warps) wsums[warp] = err;
         grid.sync();
-        // all partials in flight at once, then the sum in block order
-        for (u32 b = threadIdx.x; b < gridDim.x; b += LB) part[b] = __ldcg(partials + b);
+        // the per-pass partials, each from its warps' sums in warp order
+        // (warps past the last particle add +0 there), then their sum in
+        // block order
+        for (u32 b = threadIdx.x; b < n_pass; b += LB) {
+            const u32 w0 = b * wpb, w1 = min(w0 + wpb, n_warps);
+            double t = 0;
+            for (u32 w = w0; w < w1; ++w) t += __ldcg(wsums + w);
+            part[b] = t;
+        }
         __syncthreads();
         if (threadIdx.x == 0) {
             double s = 0;
-            for (u32 b = 0; b < gridDim.x; ++b) s += part[b];
+            for (u32 b = 0; b < n_pass; ++b) s += part[b];
             const bool done = it >= first_check && s * inv_n < threshold;
             stop = done ? 1 : 0;
             if (blockIdx.x == 0) {

@@ -111,7 +111,9 @@ public:
         cell_start_.alloc(keys_ + 1);  // closing entry = n
         n_tiles_ = static_cast<u32>((keys_ + SCAN_TILE - 1) / SCAN_TILE);
         tile_sums_.alloc(n_tiles_ + 1);
-        partials_.alloc(std::max<size_t>(1, (std::max(cap_, 1u) + 63) / 64));  // blocks of >= 64 threads
+        // block partials of the per-pass reductions (blocks of >= 64 threads)
+        // and the per-warp sums of the cooperative solve
+        partials_.alloc(std::max<size_t>(1, (std::max(cap_, 1u) + 31) / 32));
         ctl_.alloc(3);
         staging_.alloc(std::max<size_t>(size_t(std::max(cap_, bcap_)) * 6, 6));
         if (bcap_) {
@@ -1477,39 +1479,45 @@ private:
     bool solve_cooperative(const StepDt<R>& sd, u32 max_iters, double thr, u32 first_check, IterCtl* ctl,
                            R* kap_out, R* adv_out, const u32* cs) {
         if (max_iters == 0 || profile_mask_ != 0) return false;
-        const int lb = bs_[DFSPH_KERNEL_PRESSURE_RATE];
+        const int lb = bs_[DFSPH_KERNEL_PRESSURE_RATE];  // the per-pass reduction's block size
         if (lb != 128 && lb != 256) return false;
         const int n = int(n_);
-        const int blocks = blocks_for(n, lb);
+        if (blocks_for(n, lb) > JACOBI_SOLVE_MAX_BLOCKS) return false;
         // neighbour records staged per block: 2 x stage_cap fluid records
         // (96 KB) and wall_cap wall records (32 KB)
         constexpr size_t kStageBytes = 128 * 1024;
         const u32 stage_cap = static_cast<u32>(96 * 1024 / (2 * sizeof(V4)));
         const u32 wall_cap = static_cast<u32>(32 * 1024 / sizeof(V4));
-        int& cap = coop_blocks_[DIV ? 1 : 0][lb == 256 ? 1 : 0];
-        if (cap < 0) {
-            int per_sm = 0, sms = 0;
-            if (lb == 128) {
-                DFSPH_CUDA(cudaFuncSetAttribute(jacobi_solve_kernel<R, DIV, 128>,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize, int(kStageBytes)));
-                DFSPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_solve_kernel<R, DIV, 128>,
-                                                                         128, kStageBytes));
-            } else {
-                DFSPH_CUDA(cudaFuncSetAttribute(jacobi_solve_kernel<R, DIV, 256>,
-                                                cudaFuncAttributeMaxDynamicSharedMemorySize, int(kStageBytes)));
-                DFSPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, jacobi_solve_kernel<R, DIV, 256>,
-                                                                         256, kStageBytes));
+        // the smallest block (64, 128 or 256 particles) that needs at most
+        // one block per SM: the passes are latency-bound at this size, so
+        // spreading the particles over more SMs shortens them
+        static constexpr int kBlocks[3] = {64, 128, 256};
+        int pick = -1;
+        for (int k = 0; k < 3 && pick < 0; ++k) {
+            int& cap = coop_blocks_[DIV ? 1 : 0][k];
+            if (cap < 0) {
+                int per_sm = 0, sms = 0;
+                auto probe = [&](auto kernel, int threads) {
+                    DFSPH_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    int(kStageBytes)));
+                    DFSPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, kStageBytes));
+                };
+                if (k == 0) probe(jacobi_solve_kernel<R, DIV, 64>, 64);
+                else if (k == 1) probe(jacobi_solve_kernel<R, DIV, 128>, 128);
+                else probe(jacobi_solve_kernel<R, DIV, 256>, 256);
+                DFSPH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+                // at most one block per SM: beyond that the passes are long
+                // enough to hide their launches, and the per-pass kernels
+                // keep their neighbour gathers in L1
+                cap = std::min(per_sm, 1) * sms;
             }
-            DFSPH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
-            // at most one block per SM: beyond that the passes are long
-            // enough to hide their launches, and the per-pass kernels keep
-            // their neighbour gathers in L1
-            cap = std::min(std::min(per_sm, 1) * sms, JACOBI_SOLVE_MAX_BLOCKS);
+            if (blocks_for(n, kBlocks[k]) <= cap) pick = k;
         }
-        if (blocks > cap) return false;
+        if (pick < 0) return false;
+        const int cb = kBlocks[pick];
         cudaLaunchConfig_t lc = {};
-        lc.gridDim = dim3(unsigned(blocks));
-        lc.blockDim = dim3(unsigned(lb));
+        lc.gridDim = dim3(unsigned(blocks_for(n, cb)));
+        lc.blockDim = dim3(unsigned(cb));
         lc.dynamicSmemBytes = kStageBytes;
         lc.stream = stream_;
         cudaLaunchAttribute attr[1];
@@ -1520,20 +1528,20 @@ private:
         V4* xa = xk_[cx_].p;
         V4* xb = xk_[cx_ ^ 1].p;
         const double inv_n = 1.0 / double(n);
+        auto go = [&](auto kernel) {
+            return cudaLaunchKernelEx(&lc, kernel, n, xa, xb, vr_[cv_].p, (const R*)alpha_.p, adv_out, kap_out, cs,
+                                      g_, phys_, bdev(), sd, partials_.p, ctl, max_iters, first_check, inv_n, thr,
+                                      stage_cap, wall_cap, u32(lb));
+        };
         cudaError_t e;
-        if (lb == 128)
-            e = cudaLaunchKernelEx(&lc, jacobi_solve_kernel<R, DIV, 128>, n, xa, xb, vr_[cv_].p, (const R*)alpha_.p,
-                                   adv_out, kap_out, cs, g_, phys_, bdev(), sd, partials_.p, ctl, max_iters,
-                                   first_check, inv_n, thr, stage_cap, wall_cap);
-        else
-            e = cudaLaunchKernelEx(&lc, jacobi_solve_kernel<R, DIV, 256>, n, xa, xb, vr_[cv_].p, (const R*)alpha_.p,
-                                   adv_out, kap_out, cs, g_, phys_, bdev(), sd, partials_.p, ctl, max_iters,
-                                   first_check, inv_n, thr, stage_cap, wall_cap);
+        if (cb == 64) e = go(jacobi_solve_kernel<R, DIV, 64>);
+        else if (cb == 128) e = go(jacobi_solve_kernel<R, DIV, 128>);
+        else e = go(jacobi_solve_kernel<R, DIV, 256>);
         if (e == cudaErrorCooperativeLaunchTooLarge && !capturing_) {
             // fewer SMs than the device reports (a partitioned GPU): the
             // per-pass solve from now on
             cudaGetLastError();
-            cap = 0;
+            for (int k = 0; k < 3; ++k) coop_blocks_[DIV ? 1 : 0][k] = 0;
             return false;
         }
         DFSPH_CUDA(e);
@@ -1750,7 +1758,9 @@ private:
     int last_frame_graph_ = 0;
     cudaStream_t loop_stream_ = nullptr;
     bool iters_on_device_ = false;
-    int coop_blocks_[2][2] = {{-1, -1}, {-1, -1}};  // resident jacobi_solve_kernel blocks: [DIV][256 threads]  // the last step's iteration counts live in IterCtl::iters
+    // blocks of jacobi_solve_kernel one launch may hold, [DIV][64, 128, 256
+    // threads] (-1: not probed yet)
+    int coop_blocks_[2][3] = {{-1, -1, -1}, {-1, -1, -1}};
     bool fuse_advect_ = true;  // last density iteration carries the integrator when it can
     DevBuf<V4> tune_ck_;
     DevBuf<IterCtl> tune_ctl_;
