@@ -975,24 +975,27 @@ __global__ void __launch_bounds__(LB) pressure_apply_kernel(
 
 // A whole adaptive Jacobi solve in one cooperative launch, every block
 // resident (small scenes, where a solve of many short passes is bound by
-// launches): per iteration the rate pass, a grid barrier, the stop decision,
-// the apply pass and a second barrier. Even iterations read positions from xa
-// and write (x, kappa / rho^2) to xb, odd ones the other way round, as the
-// graph-resident loop does. Blocks of LB particles (as few as keep one block
-// per SM, so that a small scene spreads over many SMs) are independent of the
-// per-pass kernels' block size pass_block: every warp leaves the shuffle-tree
-// sum of its 32 particles' error terms in wsums, and after the barrier every
-// block rebuilds the per-pass partials from them (each the sum of its
-// pass_block / 32 warp sums in warp order, as block_sum_dyn adds them) and
-// sums those in block order (finish_reduction). The error sum, and with it the
-// iteration count, is therefore the per-pass solve's bit for bit, and all
-// blocks take the same decision. Records written inside the launch are read
-// with ld_coh; a block whose stencils read at most stage_cap consecutive slots
-// copies them into shared memory once per pass (dynamic shared memory:
-// 2 x stage_cap records).
+// launches): per iteration the rate pass, a grid barrier, the stop decision
+// and the apply pass, and a second barrier. Even iterations read positions
+// from xa and write (x, kappa / rho^2) to xb, odd ones the other way round, as
+// the graph-resident loop does. A block is LB particle threads (as few as keep
+// one block per SM, so that a small scene spreads over many SMs) plus one
+// warp that takes the stop decision while the particle threads run the apply
+// pass, which every iteration runs whatever the decision. The per-pass
+// kernels' block size pass_block fixes how the error terms are summed, and
+// the decision rebuilds that sum exactly: every particle warp leaves the
+// shuffle-tree sum of its 32 particles' error terms in wsums (the first stage
+// of block_sum_dyn); after the barrier the decision warp rebuilds the per-pass
+// partials from them (each the sum of its pass_block / 32 warp sums in warp
+// order) and sums those in block order (finish_reduction). The error sum, and
+// with it the iteration count, is therefore the per-pass solve's bit for bit,
+// and all blocks take the same decision. Records written inside the launch
+// are read with ld_coh; a block whose stencils read at most stage_cap
+// consecutive slots copies them into shared memory once per pass (dynamic
+// shared memory: 2 x stage_cap records).
 constexpr int JACOBI_SOLVE_MAX_BLOCKS = 256;
 template <class R, bool DIV, int LB>
-__global__ void __launch_bounds__(LB) jacobi_solve_kernel(
+__global__ void __launch_bounds__(LB + 32) jacobi_solve_kernel(
     int n, R4<R>* xa, R4<R>* xb, R4<R>* vr, const R* __restrict__ alpha, R* rho_adv, R* kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, double* wsums,
     IterCtl* ctl, u32 max_iters, u32 first_check, double inv_n, double threshold, u32 stage_cap,
@@ -1009,8 +1012,12 @@ __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
     __shared__ u32 run_b[9 * LB], run_e[9 * LB];
     __shared__ u32 wrun_b[9 * LB], wrun_e[9 * LB];
     __shared__ u32 wspan_lo, wspan_hi;
+    // threads LB .. LB + 31: the decision warp
+    const bool worker = threadIdx.x < LB;
+    // a barrier of the particle threads alone (named barrier 1)
+    auto workers_sync = [] { asm volatile("bar.sync 1, %0;" ::"r"(LB) : "memory"); };
     const R dt = step_dt(sd);
-    const int i = blockIdx.x * LB + threadIdx.x;
+    const int i = worker ? int(blockIdx.x * LB + threadIdx.x) : n;
     const u32 n_warps = (static_cast<u32>(n) + 31u) / 32u;
     const u32 wpb = pass_block / 32u;                     // warps per per-pass block
     const u32 n_pass = (n_warps + wpb - 1u) / wpb;        // per-pass blocks
@@ -1021,14 +1028,17 @@ __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
         span_hi = 0u;
         wspan_lo = 0xFFFFFFFFu;
         wspan_hi = 0u;
+        stop = 0;
     }
     __syncthreads();
+    if (worker) {
 #pragma unroll
-    for (int k = 0; k < 9; ++k) {
-        run_b[k * LB + threadIdx.x] = 0u;
-        run_e[k * LB + threadIdx.x] = 0u;
-        wrun_b[k * LB + threadIdx.x] = 0u;
-        wrun_e[k * LB + threadIdx.x] = 0u;
+        for (int k = 0; k < 9; ++k) {
+            run_b[k * LB + threadIdx.x] = 0u;
+            run_e[k * LB + threadIdx.x] = 0u;
+            wrun_b[k * LB + threadIdx.x] = 0u;
+            wrun_e[k * LB + threadIdx.x] = 0u;
+        }
     }
     if (i < n) {
         const R4<R> pi = ld_coh(xa + i);
@@ -1070,7 +1080,7 @@ __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
     __syncthreads();
     const u32 wlo = wspan_lo, whi = wspan_hi;
     const bool wstaged = whi > wlo && whi - wlo <= wall_cap;
-    if (wstaged) {
+    if (wstaged && worker) {
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
         for (u32 k = threadIdx.x; k < whi - wlo; k += LB) swx[k] = ld(xb + wlo + k);
     }
@@ -1078,11 +1088,8 @@ __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
     const u32 lo = span_lo, hi = span_hi;
     const bool staged = hi > lo && hi - lo <= stage_cap;
     const u32 count = staged ? hi - lo : 0u;
-    u32 it = 0;
-    while (it < max_iters) {
-        const R4<R>* xin = (it & 1u) ? xb : xa;
-        R4<R>* xout = (it & 1u) ? xa : xb;
-        NbrSrc<R> src;
+    NbrSrc<R> src;
+    if (worker) {
         src.rb = run_b + threadIdx.x;
         src.re = run_e + threadIdx.x;
         src.stride = LB;
@@ -1091,56 +1098,68 @@ __global__ void __launch_bounds__(LB) jacobi_solve_kernel(
         src.wx = wstaged ? swx : nullptr;
         src.wlo = wlo;
         if (staged) {
-            for (u32 k = threadIdx.x; k < count; k += LB) {
-                sx[k] = ld_coh(xin + lo + k);
-                sv[k] = ld_coh(vr + lo + k);
-            }
-            __syncthreads();
             src.x = sx;
             src.v = sv;
             src.lo = lo;
         }
-        double err = 0;
-        if (i < n)
-            err = rate_particle<R, DIV, true>(i, xin, xout, vr, alpha, rho_adv, kap, cs, g, p, bd, dt, nullptr, src);
-        // the warp's share of block_sum_dyn: the same shuffle tree
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) err += __shfl_down_sync(0xffffffffu, err, o);
-        const u32 warp = (blockIdx.x * LB + threadIdx.x) >> 5;
-        if ((threadIdx.x & 31) == 0 && warp < n_warps) wsums[warp] = err;
-        grid.sync();
-        // the per-pass partials, each from its warps' sums in warp order
-        // (warps past the last particle add +0 there), then their sum in
-        // block order
-        for (u32 b = threadIdx.x; b < n_pass; b += LB) {
-            const u32 w0 = b * wpb, w1 = min(w0 + wpb, n_warps);
-            double t = 0;
-            for (u32 w = w0; w < w1; ++w) t += __ldcg(wsums + w);
-            part[b] = t;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double s = 0;
-            for (u32 b = 0; b < n_pass; ++b) s += part[b];
-            const bool done = it >= first_check && s * inv_n < threshold;
-            stop = done ? 1 : 0;
-            if (blockIdx.x == 0) {
-                ctl->err_sum = s;
-                if (done) ctl->stop_iter = it;
-                if (!(s == s)) ctl->flags |= 1u;
+    }
+    u32 it = 0;
+    while (it < max_iters) {
+        const R4<R>* xin = (it & 1u) ? xb : xa;
+        R4<R>* xout = (it & 1u) ? xa : xb;
+        if (worker) {
+            if (staged) {
+                for (u32 k = threadIdx.x; k < count; k += LB) {
+                    sx[k] = ld_coh(xin + lo + k);
+                    sv[k] = ld_coh(vr + lo + k);
+                }
+                workers_sync();
             }
+            double err = 0;
+            if (i < n)
+                err = rate_particle<R, DIV, true>(i, xin, xout, vr, alpha, rho_adv, kap, cs, g, p, bd, dt, nullptr,
+                                                  src);
+            // the warp's share of block_sum_dyn: the same shuffle tree
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) err += __shfl_down_sync(0xffffffffu, err, o);
+            const u32 warp = (blockIdx.x * LB + threadIdx.x) >> 5;
+            if ((threadIdx.x & 31) == 0 && warp < n_warps) wsums[warp] = err;
         }
-        __syncthreads();
-        const bool done = stop != 0;
-        if (staged) {
-            // the block's rate pass finished reading sx, sv before the barrier
-            for (u32 k = threadIdx.x; k < count; k += LB) sx[k] = ld_coh(xout + lo + k);
-            __syncthreads();
+        grid.sync();
+        if (!worker) {
+            // the decision: the per-pass partials, each from its warps' sums
+            // in warp order (warps past the last particle add +0 there), then
+            // their sum in block order
+            const u32 lane = threadIdx.x - LB;
+            for (u32 b = lane; b < n_pass; b += 32) {
+                const u32 w0 = b * wpb, w1 = min(w0 + wpb, n_warps);
+                double t = 0;
+                for (u32 w = w0; w < w1; ++w) t += __ldcg(wsums + w);
+                part[b] = t;
+            }
+            __syncwarp();
+            if (lane == 0) {
+                double s = 0;
+                for (u32 b = 0; b < n_pass; ++b) s += part[b];
+                const bool done = it >= first_check && s * inv_n < threshold;
+                stop = done ? 1 : 0;
+                if (blockIdx.x == 0) {
+                    ctl->err_sum = s;
+                    if (done) ctl->stop_iter = it;
+                    if (!(s == s)) ctl->flags |= 1u;
+                }
+            }
+        } else {
+            if (staged) {
+                // the block's rate pass finished reading sx, sv before the barrier
+                for (u32 k = threadIdx.x; k < count; k += LB) sx[k] = ld_coh(xout + lo + k);
+                workers_sync();
+            }
+            if (i < n) vr[i] = apply_velocity<R, true>(i, xout, vr, kap, cs, g, p, bd, dt, src);
         }
-        if (i < n) vr[i] = apply_velocity<R, true>(i, xout, vr, kap, cs, g, p, bd, dt, src);
         ++it;
-        grid.sync();  // velocities complete before the next rate pass
-        if (done) break;
+        grid.sync();  // velocities complete before the next rate pass; stop visible
+        if (stop != 0) break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->iters = it;
 }

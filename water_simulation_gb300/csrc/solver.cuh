@@ -1502,9 +1502,10 @@ private:
                                                     int(kStageBytes)));
                     DFSPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, kStageBytes));
                 };
-                if (k == 0) probe(jacobi_solve_kernel<R, DIV, 64>, 64);
-                else if (k == 1) probe(jacobi_solve_kernel<R, DIV, 128>, 128);
-                else probe(jacobi_solve_kernel<R, DIV, 256>, 256);
+                // one more warp per block: the stop decision
+                if (k == 0) probe(jacobi_solve_kernel<R, DIV, 64>, 64 + 32);
+                else if (k == 1) probe(jacobi_solve_kernel<R, DIV, 128>, 128 + 32);
+                else probe(jacobi_solve_kernel<R, DIV, 256>, 256 + 32);
                 DFSPH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
                 // at most one block per SM: beyond that the passes are long
                 // enough to hide their launches, and the per-pass kernels
@@ -1517,7 +1518,7 @@ private:
         const int cb = kBlocks[pick];
         cudaLaunchConfig_t lc = {};
         lc.gridDim = dim3(unsigned(blocks_for(n, cb)));
-        lc.blockDim = dim3(unsigned(cb));
+        lc.blockDim = dim3(unsigned(cb + 32));
         lc.dynamicSmemBytes = kStageBytes;
         lc.stream = stream_;
         cudaLaunchAttribute attr[1];
