@@ -186,46 +186,6 @@ __device__ __forceinline__ void for_each_run(const Centre& c, const GridDev<R>& 
     }
 }
 
-// for_each_run for latency-bound launches (a persistent solve of a small
-// scene, few warps per SM): the next column's bounds are loaded before the
-// current run is walked. Same runs in the same order.
-template <class R, class F>
-__device__ __forceinline__ void for_each_run_ahead(const Centre& c, const GridDev<R>& g,
-                                                   const u32* __restrict__ cs, F&& f) {
-    const int z0 = max(c.z - 1, 0);
-    const int z1 = min(c.z + 1, g.nz - 1);
-    if (z0 > z1) return;
-#ifdef DFSPH_BOUNDS_CHECK
-    const u32 limit = __ldg(cs + g.cells1);
-#endif
-    auto column = [&](int k, u32& b, u32& e) {
-        const int nx = c.x + k / 3 - 1, ny = c.y + k % 3 - 1;
-        b = 0;
-        e = 0;
-        if (nx < 0 || nx >= g.nx || ny < 0 || ny >= g.ny) return;
-        const u32 base = (static_cast<u32>(nx) * static_cast<u32>(g.ny) + static_cast<u32>(ny)) *
-                         static_cast<u32>(g.nz);
-        b = __ldg(cs + base + z0);
-        e = __ldg(cs + base + z1 + 1);
-    };
-    u32 b, e;
-    column(0, b, e);
-#pragma unroll 1
-    for (int k = 0; k < 9; ++k) {
-        u32 nb = 0, ne = 0;
-        if (k < 8) column(k + 1, nb, ne);
-#ifdef DFSPH_BOUNDS_CHECK
-        if (b > e || e > limit) {
-            atomicAdd(&g_bounds_violations, 1u);
-            b = e;
-        }
-#endif
-        if (b < e) f(b, e);
-        b = nb;
-        e = ne;
-    }
-}
-
 #endif  // __CUDACC__
 
 }  // namespace dfsph

@@ -56,20 +56,17 @@ template <> __device__ __forceinline__ R4<double> ld_coh(const R4<double>* p) {
     const double2 a = __ldca(q), b = __ldca(q + 1);
     return {a.x, a.y, b.x, b.y};
 }
-template <class R, bool COHERENT> __device__ __forceinline__ R4<R> ld_rec(const R4<R>* p) {
-    if (COHERENT) return ld_coh(p);
-    return ld(p);
-}
 
-// Copies of a block's neighbour records in shared memory (slots lo ..): set by
-// a persistent solve for a block whose stencils read a short enough slot
-// range; x null means the records are read from global memory.
+// Where a persistent solve (jacobi_solve_kernel) finds a particle's
+// neighbours: copies of its block's neighbour records in shared memory (slots
+// lo ..; x null means the records are read from global memory), and the
+// particle's stencil runs, computed once per launch.
 template <class R> struct NbrSrc {
     const R4<R>* x = nullptr;
     const R4<R>* v = nullptr;
     u32 lo = 0;
-    // the thread's 9 stencil runs, computed once per launch: run k of the
-    // thread is [rb[k * stride], re[k * stride]) (null: look them up)
+    // run k of the particle is [rb[k * stride], re[k * stride]); runs past
+    // its last one are empty
     const u32* rb = nullptr;
     const u32* re = nullptr;
     int stride = 0;
@@ -80,22 +77,6 @@ template <class R> struct NbrSrc {
     const R4<R>* wx = nullptr;
     u32 wlo = 0;
 };
-
-// The stencil's runs from NbrSrc's table when it has one, else from cell_start
-// (for_each_run_ahead); the same runs in the same order either way.
-template <class R, class F>
-__device__ __forceinline__ void for_each_run_src(const NbrSrc<R>& src, const Centre& c, const GridDev<R>& g,
-                                                 const u32* __restrict__ cs, F&& f) {
-    if (!src.rb) {
-        for_each_run_ahead(c, g, cs, f);
-        return;
-    }
-#pragma unroll 1
-    for (int k = 0; k < 9; ++k) {
-        const u32 b = src.rb[k * src.stride], e = src.re[k * src.stride];
-        if (b < e) f(b, e);
-    }
-}
 
 // ---------------------------------------------------------------------------
 // Pair terms. With r = |x_i - x_j| the cubic spline and its gradient factor
@@ -132,6 +113,65 @@ template <class R> __device__ __forceinline__ R kernel_w(R r, const Phys<R>& p) 
     return r < p.l ? inner : outer;
 }
 
+
+// The pair terms of the Jacobi passes. Their dot products are written out as
+// explicit roundings (no contraction left to the compiler, whose choice of
+// which product to fuse can depend on the code around an inlined call), and
+// each term is added to its sum with an explicit fused multiply-add, so that
+// a pass that evaluates a particle's candidates on several lanes and adds them
+// on one (jacobi_solve_kernel) gets the same bits as the one-lane passes.
+__device__ __forceinline__ float fma_r(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fma_r(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float mul_r(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_r(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float sub_r(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_r(double a, double b) { return __dsub_rn(a, b); }
+// a.x b.x + a.y b.y + a.z b.z as fma(az, bz, fma(ay, by, ax bx))
+template <class R> __device__ __forceinline__ R dot3(R ax, R ay, R az, R bx, R by, R bz) {
+    return fma_r(az, bz, fma_r(ay, by, mul_r(ax, bx)));
+}
+// pair_r and grad_factor with every rounding explicit
+template <class R> __device__ __forceinline__ R pair_r_x(R r2, R& rinv) {
+    rinv = rsqrt_r(rmax(r2, R(1e-24)));
+    return mul_r(r2, rinv);
+}
+template <class R> __device__ __forceinline__ R grad_factor_x(R r, R rinv, const Phys<R>& p) {
+    const R t = rmax(sub_r(p.two_l, r), R(0));
+    const R outer = mul_r(mul_r(mul_r(p.gC, t), t), rinv);
+    const R inner = fma_r(p.gA, r, p.gB);
+    return r < p.l ? inner : outer;
+}
+
+// rate pass, fluid candidate j: rd = fma(f, d, rd)
+template <class R>
+__device__ __forceinline__ void rate_fluid_terms(const R4<R>& pi, const R4<R>& vi, const R4<R>& pj,
+                                                 const R4<R>& vj, const Phys<R>& p, R& f, R& d) {
+    const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+    R rinv;
+    const R r = pair_r_x(dot3(rx, ry, rz, rx, ry, rz), rinv);
+    f = grad_factor_x(r, rinv, p);
+    d = dot3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, rx, ry, rz);
+}
+// rate pass, wall candidate j (wall velocity 0): rb = fma(f, d, rb)
+template <class R>
+__device__ __forceinline__ void rate_wall_terms(const R4<R>& pi, const R4<R>& vi, const R4<R>& pj,
+                                                const Phys<R>& p, R& f, R& d) {
+    const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+    R rinv;
+    const R r = pair_r_x(dot3(rx, ry, rz, rx, ry, rz), rinv);
+    f = mul_r(pj.w, grad_factor_x(r, rinv, p));
+    d = dot3(vi.x, vi.y, vi.z, rx, ry, rz);
+}
+// apply pass, candidate j with the pair weight w = kfac_i + kfac_j (fluid)
+// or m_b (wall): a = fma(f, r_ij, a) per component
+template <class R>
+__device__ __forceinline__ void apply_terms(const R4<R>& pi, const R4<R>& pj, R w, const Phys<R>& p, R& f, R& rx,
+                                            R& ry, R& rz) {
+    rx = pi.x - pj.x; ry = pi.y - pj.y; rz = pi.z - pj.z;
+    R rinv;
+    const R r = pair_r_x(dot3(rx, ry, rz, rx, ry, rz), rinv);
+    f = mul_r(w, grad_factor_x(r, rinv, p));
+}
 
 // ---------------------------------------------------------------------------
 // Reductions: FP64 block partial sums with a deterministic last-block finish.
@@ -754,81 +794,45 @@ __global__ void __launch_bounds__(LB) forces_xsph_kernel(
 
 // One particle of the rate pass: rho_adv, kappa and (x, kappa / rho^2) of
 // particle i; returns its error term (the reduction's input).
-template <class R, bool DIVERGENCE, bool COHERENT = false>
+template <class R, bool DIVERGENCE>
 __device__ __forceinline__ double rate_particle(int i, const R4<R>* __restrict__ xk_in, R4<R>* __restrict__ xk_out,
                                                 const R4<R>* __restrict__ vr, const R* __restrict__ alpha,
                                                 R* __restrict__ rho_adv, R* __restrict__ kap,
                                                 const u32* __restrict__ cs, const GridDev<R>& g, const Phys<R>& p,
-                                                const BoundaryDev& bd, R dt, R4<R>* __restrict__ tape_v,
-                                                const NbrSrc<R>& src = NbrSrc<R>()) {
+                                                const BoundaryDev& bd, R dt, R4<R>* __restrict__ tape_v) {
     double err = 0;
-    const R4<R> pi = ld_rec<R, COHERENT>(xk_in + i);
-    const R4<R> vi = ld_rec<R, COHERENT>(vr + i);
+    const R4<R> pi = ld(xk_in + i);
+    const R4<R> vi = ld(vr + i);
     if (tape_v) tape_v[i] = vi;
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
     R rd = 0;
     auto pair = [&](const R4<R>& pj, const R4<R>& vj) {
-        const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-        R rinv;
-        const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
-        const R f = grad_factor(r, rinv, p);
-        rd += f * ((vi.x - vj.x) * rx + (vi.y - vj.y) * ry + (vi.z - vj.z) * rz);
+        R f, d;
+        rate_fluid_terms(pi, vi, pj, vj, p, f, d);
+        rd = fma_r(f, d, rd);
     };
-    if (COHERENT) {
-        // latency-bound: a column's records four at a time, summed in order
-        for_each_run_src(src, c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
-            for (u32 j0 = b; j0 < e; j0 += 4) {
-                R4<R> pj[4], vj[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const u32 j = min(j0 + u, e - 1);
-                    if (src.x) {
-                        pj[u] = src.x[j - src.lo];
-                        vj[u] = src.v[j - src.lo];
-                    } else {
-                        pj[u] = ld_coh(xk_in + j);
-                        vj[u] = ld_coh(vr + j);
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    if (j0 + u < e) pair(pj[u], vj[u]);
-            }
-        });
-    } else {
-        for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+    for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
 #pragma unroll 2
-            for (u32 j = b; j < e; ++j) pair(ld(xk_in + j), ld(vr + j));
-        });
-    }
+        for (u32 j = b; j < e; ++j) pair(ld(xk_in + j), ld(vr + j));
+    });
     rd *= p.mass;
     if (bd.has && boundary_near(c, g, bd.mask)) {
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
         R rb = 0;
         auto wall = [&](const R4<R>& pj) {
-            const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-            R rinv;
-            const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
-            rb += pj.w * grad_factor(r, rinv, p) * (vi.x * rx + vi.y * ry + vi.z * rz);
+            R f, d;
+            rate_wall_terms(pi, vi, pj, p, f, d);
+            rb = fma_r(f, d, rb);
         };
-        if (COHERENT && src.wrb) {
-            // the wall runs from the per-launch table, records from shared memory when staged
-#pragma unroll 1
-            for (int k = 0; k < 9; ++k) {
-                const u32 b = src.wrb[k * src.stride], e = src.wre[k * src.stride];
-                for (u32 j = b; j < e; ++j) wall(src.wx ? src.wx[j - src.wlo] : ld(xb + j));
-            }
-        } else {
-            for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
-                for (u32 j = b; j < e; ++j) wall(ld(xb + j));
-            });
-        }
+        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+            for (u32 j = b; j < e; ++j) wall(ld(xb + j));
+        });
         rd += rb;
     }
     const R rho = vi.w;
     R k;
     if (!DIVERGENCE) {
-        const R rp = rho + dt * rd;
+        const R rp = fma_r(dt, rd, rho);
         rho_adv[i] = rp;
         const R over = rmax(rp - p.rho0, R(0));
         k = over * alpha[i] / (dt * dt);
@@ -889,41 +893,21 @@ __global__ void __launch_bounds__(LB) pressure_rate_kernel(
 // v_i -= dt sum_j m (kfac_i + kfac_j) gradW over fluid and
 // dt sum_b m_b (kfac_i + kappa_i / max(rho0^2, 1e-9)) gradW over the boundary.
 // One particle of the apply pass: its velocity after the pressure update.
-template <class R, bool COHERENT = false>
+template <class R>
 __device__ __forceinline__ R4<R> apply_velocity(int i, const R4<R>* __restrict__ xk, const R4<R>* __restrict__ vr,
                                                 const R* __restrict__ kap, const u32* __restrict__ cs,
-                                                const GridDev<R>& g, const Phys<R>& p, const BoundaryDev& bd, R dt,
-                                                const NbrSrc<R>& src = NbrSrc<R>()) {
-    const R4<R> pi = ld_rec<R, COHERENT>(xk + i);
+                                                const GridDev<R>& g, const Phys<R>& p, const BoundaryDev& bd, R dt) {
+    const R4<R> pi = ld(xk + i);
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
     R ax = 0, ay = 0, az = 0;
     auto pair = [&](const R4<R>& pj) {
-        const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-        R rinv;
-        const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
-        const R f = (pi.w + pj.w) * grad_factor(r, rinv, p);
-        ax += f * rx; ay += f * ry; az += f * rz;
+        R f, rx, ry, rz;
+        apply_terms(pi, pj, pi.w + pj.w, p, f, rx, ry, rz);
+        ax = fma_r(f, rx, ax); ay = fma_r(f, ry, ay); az = fma_r(f, rz, az);
     };
-    if (COHERENT) {
-        // latency-bound: a column's records four at a time, summed in order
-        for_each_run_src(src, c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
-            for (u32 j0 = b; j0 < e; j0 += 4) {
-                R4<R> pj[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const u32 j = min(j0 + u, e - 1);
-                    pj[u] = src.x ? src.x[j - src.lo] : ld_coh(xk + j);
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-                    if (j0 + u < e) pair(pj[u]);
-            }
-        });
-    } else {
-        for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
-            for (u32 j = b; j < e; ++j) pair(ld(xk + j));
-        });
-    }
+    for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+        for (u32 j = b; j < e; ++j) pair(ld(xk + j));
+    });
     const R sf = -dt * p.mass;
     ax *= sf; ay *= sf; az *= sf;
     if (bd.has && boundary_near(c, g, bd.mask)) {
@@ -931,25 +915,15 @@ __device__ __forceinline__ R4<R> apply_velocity(int i, const R4<R>* __restrict__
         const R kb = pi.w + kap[i] / rmax(p.rho0 * p.rho0, R(1e-9));
         R bx = 0, by = 0, bz = 0;
         auto wall = [&](const R4<R>& pj) {
-            const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
-            R rinv;
-            const R r = pair_r(rx * rx + ry * ry + rz * rz, rinv);
-            const R f = pj.w * grad_factor(r, rinv, p);
-            bx += f * rx; by += f * ry; bz += f * rz;
+            R f, rx, ry, rz;
+            apply_terms(pi, pj, pj.w, p, f, rx, ry, rz);
+            bx = fma_r(f, rx, bx); by = fma_r(f, ry, by); bz = fma_r(f, rz, bz);
         };
-        if (COHERENT && src.wrb) {
-#pragma unroll 1
-            for (int k = 0; k < 9; ++k) {
-                const u32 b = src.wrb[k * src.stride], e = src.wre[k * src.stride];
-                for (u32 j = b; j < e; ++j) wall(src.wx ? src.wx[j - src.wlo] : ld(xb + j));
-            }
-        } else {
-            for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
-                for (u32 j = b; j < e; ++j) wall(ld(xb + j));
-            });
-        }
+        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+            for (u32 j = b; j < e; ++j) wall(ld(xb + j));
+        });
         const R sb = -dt * kb;
-        ax += sb * bx; ay += sb * by; az += sb * bz;
+        ax = fma_r(sb, bx, ax); ay = fma_r(sb, by, ay); az = fma_r(sb, bz, az);
     }
     R4<R> v = vr[i];
     v.x += ax; v.y += ay; v.z += az;
@@ -973,33 +947,180 @@ __global__ void __launch_bounds__(LB) pressure_apply_kernel(
     vr[i] = apply_velocity(i, xk, vr, kap, cs, g, p, bd, dt);
 }
 
+// The rate and apply passes of jacobi_solve_kernel with one particle per quad
+// of lanes (lanes 4k .. 4k + 3 of a warp, q = lane % 4). The candidates come
+// from the launch's run tables (src), in the one-lane order: for every run,
+// groups of four consecutive slots, lane q evaluating slot j0 + q. The group's
+// terms are exchanged within the quad and every lane adds them, in slot order,
+// with the one-lane pass's fused multiply-adds, so each lane ends with the
+// one-lane sum bit for bit while a particle's dependent chain of pair terms is
+// a quarter as long. Records come from shared memory when staged, else through
+// ld_coh.
+template <class R>
+__device__ __forceinline__ R quad_get(unsigned qmask, R v, int src_lane) {
+    return __shfl_sync(qmask, v, src_lane);
+}
+
+template <class R, bool DIVERGENCE>
+__device__ __forceinline__ double rate_particle_quad(int i, int q, unsigned qmask, const R4<R>* xk_in,
+                                                     R4<R>* xk_out, const R4<R>* vr, const R* __restrict__ alpha,
+                                                     R* rho_adv, R* kap, const GridDev<R>& g, const Phys<R>& p,
+                                                     const BoundaryDev& bd, R dt, const NbrSrc<R>& src) {
+    const R4<R> pi = ld_coh(xk_in + i);
+    const R4<R> vi = ld_coh(vr + i);
+    const int base = int(threadIdx.x & 31u) & ~3;
+    R rd = 0;
+#pragma unroll 1
+    for (int k = 0; k < 9; ++k) {
+        const u32 b = src.rb[k * src.stride], e = src.re[k * src.stride];
+        for (u32 j0 = b; j0 < e; j0 += 4) {
+            const u32 j = j0 + u32(q);
+            R f = 0, d = 0;
+            if (j < e) {
+                const R4<R> pj = src.x ? src.x[j - src.lo] : ld_coh(xk_in + j);
+                const R4<R> vj = src.x ? src.v[j - src.lo] : ld_coh(vr + j);
+                rate_fluid_terms(pi, vi, pj, vj, p, f, d);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const R fu = quad_get(qmask, f, base + u), du = quad_get(qmask, d, base + u);
+                if (j0 + u < e) rd = fma_r(fu, du, rd);
+            }
+        }
+    }
+    rd *= p.mass;
+    const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
+    if (bd.has && boundary_near(c, g, bd.mask)) {
+        const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
+        R rb = 0;
+#pragma unroll 1
+        for (int k = 0; k < 9; ++k) {
+            const u32 b = src.wrb[k * src.stride], e = src.wre[k * src.stride];
+            for (u32 j0 = b; j0 < e; j0 += 4) {
+                const u32 j = j0 + u32(q);
+                R f = 0, d = 0;
+                if (j < e) rate_wall_terms(pi, vi, src.wx ? src.wx[j - src.wlo] : ld(xb + j), p, f, d);
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const R fu = quad_get(qmask, f, base + u), du = quad_get(qmask, d, base + u);
+                    if (j0 + u < e) rb = fma_r(fu, du, rb);
+                }
+            }
+        }
+        rd += rb;
+    }
+    if (q != 0) return 0.0;
+    const R rho = vi.w;
+    R kk;
+    double err;
+    if (!DIVERGENCE) {
+        const R rp = fma_r(dt, rd, rho);
+        rho_adv[i] = rp;
+        const R over = rmax(rp - p.rho0, R(0));
+        kk = over * alpha[i] / (dt * dt);
+        err = double(over);
+    } else {
+        const R sv = rmax(rd, R(0));
+        rho_adv[i] = rd;
+        kk = sv * alpha[i] / dt;
+        err = double(sv);
+    }
+    kap[i] = kk;
+    xk_out[i] = {pi.x, pi.y, pi.z, kk / rmax(rho * rho, R(1e-9))};
+    return err;
+}
+
+template <class R>
+__device__ __forceinline__ R4<R> apply_velocity_quad(int i, int q, unsigned qmask, const R4<R>* xk,
+                                                     const R4<R>* vr, const R* kap, const GridDev<R>& g,
+                                                     const Phys<R>& p, const BoundaryDev& bd, R dt,
+                                                     const NbrSrc<R>& src) {
+    const R4<R> pi = ld_coh(xk + i);
+    const int base = int(threadIdx.x & 31u) & ~3;
+    R ax = 0, ay = 0, az = 0;
+#pragma unroll 1
+    for (int k = 0; k < 9; ++k) {
+        const u32 b = src.rb[k * src.stride], e = src.re[k * src.stride];
+        for (u32 j0 = b; j0 < e; j0 += 4) {
+            const u32 j = j0 + u32(q);
+            R f = 0, rx = 0, ry = 0, rz = 0;
+            if (j < e) {
+                const R4<R> pj = src.x ? src.x[j - src.lo] : ld_coh(xk + j);
+                apply_terms(pi, pj, pi.w + pj.w, p, f, rx, ry, rz);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int l = base + u;
+                const R fu = quad_get(qmask, f, l), xu = quad_get(qmask, rx, l), yu = quad_get(qmask, ry, l),
+                        zu = quad_get(qmask, rz, l);
+                if (j0 + u < e) { ax = fma_r(fu, xu, ax); ay = fma_r(fu, yu, ay); az = fma_r(fu, zu, az); }
+            }
+        }
+    }
+    const R sf = -dt * p.mass;
+    ax *= sf; ay *= sf; az *= sf;
+    const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
+    if (bd.has && boundary_near(c, g, bd.mask)) {
+        const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
+        const R kb = pi.w + kap[i] / rmax(p.rho0 * p.rho0, R(1e-9));
+        R bx = 0, by = 0, bz = 0;
+#pragma unroll 1
+        for (int k = 0; k < 9; ++k) {
+            const u32 b = src.wrb[k * src.stride], e = src.wre[k * src.stride];
+            for (u32 j0 = b; j0 < e; j0 += 4) {
+                const u32 j = j0 + u32(q);
+                R f = 0, rx = 0, ry = 0, rz = 0;
+                if (j < e) {
+                    const R4<R> pj = src.wx ? src.wx[j - src.wlo] : ld(xb + j);
+                    apply_terms(pi, pj, pj.w, p, f, rx, ry, rz);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int l = base + u;
+                    const R fu = quad_get(qmask, f, l), xu = quad_get(qmask, rx, l), yu = quad_get(qmask, ry, l),
+                            zu = quad_get(qmask, rz, l);
+                    if (j0 + u < e) { bx = fma_r(fu, xu, bx); by = fma_r(fu, yu, by); bz = fma_r(fu, zu, bz); }
+                }
+            }
+        }
+        const R sb = -dt * kb;
+        ax = fma_r(sb, bx, ax); ay = fma_r(sb, by, ay); az = fma_r(sb, bz, az);
+    }
+    R4<R> v = vr[i];
+    v.x += ax; v.y += ay; v.z += az;
+    return v;
+}
+
 // A whole adaptive Jacobi solve in one cooperative launch, every block
 // resident (small scenes, where a solve of many short passes is bound by
 // launches): per iteration the rate pass, a grid barrier, the stop decision
 // and the apply pass, and a second barrier. Even iterations read positions
 // from xa and write (x, kappa / rho^2) to xb, odd ones the other way round, as
-// the graph-resident loop does. A block is LB particle threads (as few as keep
-// one block per SM, so that a small scene spreads over many SMs) plus one
-// warp that takes the stop decision while the particle threads run the apply
-// pass, which every iteration runs whatever the decision. The per-pass
-// kernels' block size pass_block fixes how the error terms are summed, and
-// the decision rebuilds that sum exactly: every particle warp leaves the
-// shuffle-tree sum of its 32 particles' error terms in wsums (the first stage
-// of block_sum_dyn); after the barrier the decision warp rebuilds the per-pass
-// partials from them (each the sum of its pass_block / 32 warp sums in warp
-// order) and sums those in block order (finish_reduction). The error sum, and
-// with it the iteration count, is therefore the per-pass solve's bit for bit,
-// and all blocks take the same decision. Records written inside the launch
-// are read with ld_coh; a block whose stencils read at most stage_cap
-// consecutive slots copies them into shared memory once per pass (dynamic
-// shared memory: 2 x stage_cap records).
+// the graph-resident loop does. A block holds P particles, one per quad of
+// lanes (rate_particle_quad, apply_velocity_quad), P as small as keeps one
+// block per SM so that a small scene spreads over many SMs, plus one warp
+// that takes the stop decision while the particle lanes run the apply pass,
+// which every iteration runs whatever the decision. The per-pass kernels'
+// block size pass_block fixes how the error terms are summed, and the
+// decision rebuilds that sum exactly: the error terms of every 32 consecutive
+// particles are summed with block_sum_dyn's warp shuffle tree into wsums;
+// after the barrier the decision warp rebuilds the per-pass partials from them
+// (each the sum of its pass_block / 32 warp sums in warp order) and sums those
+// in block order (finish_reduction). The error sum, and with it the iteration
+// count, is therefore the per-pass solve's bit for bit, and all blocks take the
+// same decision. Records written inside the launch are read with ld_coh; a
+// block whose stencils read at most stage_cap consecutive slots copies them
+// into shared memory once per pass (dynamic shared memory: 2 x stage_cap
+// records).
 constexpr int JACOBI_SOLVE_MAX_BLOCKS = 256;
-template <class R, bool DIV, int LB>
-__global__ void __launch_bounds__(LB + 32) jacobi_solve_kernel(
+template <class R, bool DIV, int P>
+__global__ void __launch_bounds__(4 * P + 32) jacobi_solve_kernel(
     int n, R4<R>* xa, R4<R>* xb, R4<R>* vr, const R* __restrict__ alpha, R* rho_adv, R* kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, double* wsums,
     IterCtl* ctl, u32 max_iters, u32 first_check, double inv_n, double threshold, u32 stage_cap,
     u32 wall_cap, u32 pass_block) {
+    static_assert(P % 32 == 0, "whole warps of particles");
+    constexpr int W = 4 * P;  // particle lanes
     namespace cg = cooperative_groups;
     cg::grid_group grid = cg::this_grid();
     extern __shared__ __align__(16) unsigned char jacobi_stage[];
@@ -1007,17 +1128,21 @@ __global__ void __launch_bounds__(LB + 32) jacobi_solve_kernel(
     R4<R>* sv = sx + stage_cap;
     R4<R>* swx = sv + stage_cap;  // wall records, staged once per launch
     __shared__ double part[JACOBI_SOLVE_MAX_BLOCKS];
+    __shared__ double errs[P];
     __shared__ int stop;
     __shared__ u32 span_lo, span_hi;
-    __shared__ u32 run_b[9 * LB], run_e[9 * LB];
-    __shared__ u32 wrun_b[9 * LB], wrun_e[9 * LB];
+    __shared__ u32 run_b[9 * P], run_e[9 * P];
+    __shared__ u32 wrun_b[9 * P], wrun_e[9 * P];
     __shared__ u32 wspan_lo, wspan_hi;
-    // threads LB .. LB + 31: the decision warp
-    const bool worker = threadIdx.x < LB;
-    // a barrier of the particle threads alone (named barrier 1)
-    auto workers_sync = [] { asm volatile("bar.sync 1, %0;" ::"r"(LB) : "memory"); };
+    // threads W .. W + 31: the decision warp
+    const bool worker = threadIdx.x < W;
+    // a barrier of the particle lanes alone (named barrier 1)
+    auto workers_sync = [] { asm volatile("bar.sync 1, %0;" ::"r"(W) : "memory"); };
     const R dt = step_dt(sd);
-    const int i = worker ? int(blockIdx.x * LB + threadIdx.x) : n;
+    const int pl = int(threadIdx.x >> 2);  // particle of the block (workers)
+    const int q = int(threadIdx.x & 3u);
+    const unsigned qmask = 0xFu << (threadIdx.x & 28u);
+    const int i = worker ? int(blockIdx.x) * P + pl : n;
     const u32 n_warps = (static_cast<u32>(n) + 31u) / 32u;
     const u32 wpb = pass_block / 32u;                     // warps per per-pass block
     const u32 n_pass = (n_warps + wpb - 1u) / wpb;        // per-pass blocks
@@ -1031,23 +1156,23 @@ __global__ void __launch_bounds__(LB + 32) jacobi_solve_kernel(
         stop = 0;
     }
     __syncthreads();
-    if (worker) {
+    if (worker && q == 0) {
 #pragma unroll
         for (int k = 0; k < 9; ++k) {
-            run_b[k * LB + threadIdx.x] = 0u;
-            run_e[k * LB + threadIdx.x] = 0u;
-            wrun_b[k * LB + threadIdx.x] = 0u;
-            wrun_e[k * LB + threadIdx.x] = 0u;
+            run_b[k * P + pl] = 0u;
+            run_e[k * P + pl] = 0u;
+            wrun_b[k * P + pl] = 0u;
+            wrun_e[k * P + pl] = 0u;
         }
     }
-    if (i < n) {
+    if (q == 0 && i < n) {
         const R4<R> pi = ld_coh(xa + i);
         u32 lo = 0xFFFFFFFFu, hi = 0u;
         int k = 0;  // runs come in column order; empty and off-grid ones are skipped
         for_each_run(stencil_centre(pi.x, pi.y, pi.z, g), g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
             if (b < e) {
-                run_b[k * LB + threadIdx.x] = b;
-                run_e[k * LB + threadIdx.x] = e;
+                run_b[k * P + pl] = b;
+                run_e[k * P + pl] = e;
                 ++k;
                 lo = min(lo, b);
                 hi = max(hi, e);
@@ -1064,8 +1189,8 @@ __global__ void __launch_bounds__(LB + 32) jacobi_solve_kernel(
             int kw = 0;
             for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
                 if (b < e) {
-                    wrun_b[kw * LB + threadIdx.x] = b;
-                    wrun_e[kw * LB + threadIdx.x] = e;
+                    wrun_b[kw * P + pl] = b;
+                    wrun_e[kw * P + pl] = e;
                     ++kw;
                     wl = min(wl, b);
                     wh = max(wh, e);
@@ -1082,7 +1207,7 @@ __global__ void __launch_bounds__(LB + 32) jacobi_solve_kernel(
     const bool wstaged = whi > wlo && whi - wlo <= wall_cap;
     if (wstaged && worker) {
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
-        for (u32 k = threadIdx.x; k < whi - wlo; k += LB) swx[k] = ld(xb + wlo + k);
+        for (u32 k = threadIdx.x; k < whi - wlo; k += W) swx[k] = ld(xb + wlo + k);
     }
     __syncthreads();
     const u32 lo = span_lo, hi = span_hi;
@@ -1090,11 +1215,11 @@ __global__ void __launch_bounds__(LB + 32) jacobi_solve_kernel(
     const u32 count = staged ? hi - lo : 0u;
     NbrSrc<R> src;
     if (worker) {
-        src.rb = run_b + threadIdx.x;
-        src.re = run_e + threadIdx.x;
-        src.stride = LB;
-        src.wrb = wrun_b + threadIdx.x;
-        src.wre = wrun_e + threadIdx.x;
+        src.rb = run_b + pl;
+        src.re = run_e + pl;
+        src.stride = P;
+        src.wrb = wrun_b + pl;
+        src.wre = wrun_e + pl;
         src.wx = wstaged ? swx : nullptr;
         src.wlo = wlo;
         if (staged) {
@@ -1109,7 +1234,7 @@ __global__ void __launch_bounds__(LB + 32) jacobi_solve_kernel(
         R4<R>* xout = (it & 1u) ? xa : xb;
         if (worker) {
             if (staged) {
-                for (u32 k = threadIdx.x; k < count; k += LB) {
+                for (u32 k = threadIdx.x; k < count; k += W) {
                     sx[k] = ld_coh(xin + lo + k);
                     sv[k] = ld_coh(vr + lo + k);
                 }
@@ -1117,20 +1242,26 @@ __global__ void __launch_bounds__(LB + 32) jacobi_solve_kernel(
             }
             double err = 0;
             if (i < n)
-                err = rate_particle<R, DIV, true>(i, xin, xout, vr, alpha, rho_adv, kap, cs, g, p, bd, dt, nullptr,
-                                                  src);
-            // the warp's share of block_sum_dyn: the same shuffle tree
+                err = rate_particle_quad<R, DIV>(i, q, qmask, xin, xout, vr, alpha, rho_adv, kap, g, p, bd, dt,
+                                                 src);
+            if (q == 0) errs[pl] = err;
+            workers_sync();
+            if (threadIdx.x < P) {
+                // the warp's share of block_sum_dyn over 32 consecutive
+                // particles: the same shuffle tree
+                double e = errs[threadIdx.x];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) err += __shfl_down_sync(0xffffffffu, err, o);
-            const u32 warp = (blockIdx.x * LB + threadIdx.x) >> 5;
-            if ((threadIdx.x & 31) == 0 && warp < n_warps) wsums[warp] = err;
+                for (int o = 16; o > 0; o >>= 1) e += __shfl_down_sync(0xffffffffu, e, o);
+                const u32 warp = (blockIdx.x * P + threadIdx.x) >> 5;
+                if ((threadIdx.x & 31) == 0 && warp < n_warps) wsums[warp] = e;
+            }
         }
         grid.sync();
         if (!worker) {
             // the decision: the per-pass partials, each from its warps' sums
             // in warp order (warps past the last particle add +0 there), then
             // their sum in block order
-            const u32 lane = threadIdx.x - LB;
+            const u32 lane = threadIdx.x - W;
             for (u32 b = lane; b < n_pass; b += 32) {
                 const u32 w0 = b * wpb, w1 = min(w0 + wpb, n_warps);
                 double t = 0;
@@ -1152,10 +1283,13 @@ __global__ void __launch_bounds__(LB + 32) jacobi_solve_kernel(
         } else {
             if (staged) {
                 // the block's rate pass finished reading sx, sv before the barrier
-                for (u32 k = threadIdx.x; k < count; k += LB) sx[k] = ld_coh(xout + lo + k);
+                for (u32 k = threadIdx.x; k < count; k += W) sx[k] = ld_coh(xout + lo + k);
                 workers_sync();
             }
-            if (i < n) vr[i] = apply_velocity<R, true>(i, xout, vr, kap, cs, g, p, bd, dt, src);
+            if (i < n) {
+                const R4<R> v = apply_velocity_quad(i, q, qmask, xout, vr, kap, g, p, bd, dt, src);
+                if (q == 0) vr[i] = v;
+            }
         }
         ++it;
         grid.sync();  // velocities complete before the next rate pass; stop visible

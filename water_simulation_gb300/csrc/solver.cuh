@@ -1488,10 +1488,10 @@ private:
         constexpr size_t kStageBytes = 128 * 1024;
         const u32 stage_cap = static_cast<u32>(96 * 1024 / (2 * sizeof(V4)));
         const u32 wall_cap = static_cast<u32>(32 * 1024 / sizeof(V4));
-        // the smallest block (64, 128 or 256 particles) that needs at most
-        // one block per SM: the passes are latency-bound at this size, so
-        // spreading the particles over more SMs shortens them
-        static constexpr int kBlocks[3] = {64, 128, 256};
+        // the smallest block (32, 64 or 128 particles, four lanes each) that
+        // needs at most one block per SM: the passes are latency-bound at
+        // this size, so spreading the particles over more SMs shortens them
+        static constexpr int kBlocks[3] = {32, 64, 128};
         int pick = -1;
         for (int k = 0; k < 3 && pick < 0; ++k) {
             int& cap = coop_blocks_[DIV ? 1 : 0][k];
@@ -1502,10 +1502,10 @@ private:
                                                     int(kStageBytes)));
                     DFSPH_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, kStageBytes));
                 };
-                // one more warp per block: the stop decision
-                if (k == 0) probe(jacobi_solve_kernel<R, DIV, 64>, 64 + 32);
-                else if (k == 1) probe(jacobi_solve_kernel<R, DIV, 128>, 128 + 32);
-                else probe(jacobi_solve_kernel<R, DIV, 256>, 256 + 32);
+                // four lanes per particle and one more warp: the stop decision
+                if (k == 0) probe(jacobi_solve_kernel<R, DIV, 32>, 4 * 32 + 32);
+                else if (k == 1) probe(jacobi_solve_kernel<R, DIV, 64>, 4 * 64 + 32);
+                else probe(jacobi_solve_kernel<R, DIV, 128>, 4 * 128 + 32);
                 DFSPH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
                 // at most one block per SM: beyond that the passes are long
                 // enough to hide their launches, and the per-pass kernels
@@ -1518,7 +1518,7 @@ private:
         const int cb = kBlocks[pick];
         cudaLaunchConfig_t lc = {};
         lc.gridDim = dim3(unsigned(blocks_for(n, cb)));
-        lc.blockDim = dim3(unsigned(cb + 32));
+        lc.blockDim = dim3(unsigned(4 * cb + 32));
         lc.dynamicSmemBytes = kStageBytes;
         lc.stream = stream_;
         cudaLaunchAttribute attr[1];
@@ -1535,9 +1535,9 @@ private:
                                       stage_cap, wall_cap, u32(lb));
         };
         cudaError_t e;
-        if (cb == 64) e = go(jacobi_solve_kernel<R, DIV, 64>);
-        else if (cb == 128) e = go(jacobi_solve_kernel<R, DIV, 128>);
-        else e = go(jacobi_solve_kernel<R, DIV, 256>);
+        if (cb == 32) e = go(jacobi_solve_kernel<R, DIV, 32>);
+        else if (cb == 64) e = go(jacobi_solve_kernel<R, DIV, 64>);
+        else e = go(jacobi_solve_kernel<R, DIV, 128>);
         if (e == cudaErrorCooperativeLaunchTooLarge && !capturing_) {
             // fewer SMs than the device reports (a partitioned GPU): the
             // per-pass solve from now on
