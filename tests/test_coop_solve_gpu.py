@@ -103,3 +103,16 @@ def test_cooperative_solve_batched_scenes():
     assert (d0, g0) == (d1, g1) and d0 >= 2
     assert np.array_equal(x0, x1) and np.array_equal(v0, v1)
     assert l0 < l1
+
+
+def test_cooperative_solve_largest_blocks():
+    """27,000 particles: blocks of 224 particles (121 blocks), the largest
+    cooperative shape, equal bit for bit to the per-pass solve."""
+    sc = scenes.falling_block(n_side=(30, 30, 30), corner=(0.2, 0.2, 0.2), velocity_sigma=0.3)
+    sc.max_density_iters, sc.max_divergence_iters = 100, 100
+    sc.eta_density, sc.eta_divergence = 1e-4, 1e-3
+    x0, v0, r0, it0, l0 = _run(sc, False, 6)
+    x1, v1, r1, it1, l1 = _run(sc, True, 6)
+    assert it0 == it1 and sum(a + b for a, b in it0) > 2 * 6
+    assert np.array_equal(x0, x1) and np.array_equal(v0, v1) and np.array_equal(r0, r1)
+    assert l0 < l1

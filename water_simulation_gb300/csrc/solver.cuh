@@ -1488,12 +1488,12 @@ private:
         constexpr size_t kStageBytes = 128 * 1024;
         const u32 stage_cap = static_cast<u32>(96 * 1024 / (2 * sizeof(V4)));
         const u32 wall_cap = static_cast<u32>(32 * 1024 / sizeof(V4));
-        // the smallest block (32, 64 or 128 particles, four lanes each) that
-        // needs at most one block per SM: the passes are latency-bound at
-        // this size, so spreading the particles over more SMs shortens them
-        static constexpr int kBlocks[3] = {32, 64, 128};
+        // the smallest block (32, 64, 128 or 224 particles, four lanes each)
+        // that needs at most one block per SM: the passes are latency-bound
+        // at this size, so spreading the particles over more SMs shortens them
+        static constexpr int kBlocks[4] = {32, 64, 128, 224};
         int pick = -1;
-        for (int k = 0; k < 3 && pick < 0; ++k) {
+        for (int k = 0; k < 4 && pick < 0; ++k) {
             int& cap = coop_blocks_[DIV ? 1 : 0][k];
             if (cap < 0) {
                 int per_sm = 0, sms = 0;
@@ -1505,7 +1505,8 @@ private:
                 // four lanes per particle and one more warp: the stop decision
                 if (k == 0) probe(jacobi_solve_kernel<R, DIV, 32>, 4 * 32 + 32);
                 else if (k == 1) probe(jacobi_solve_kernel<R, DIV, 64>, 4 * 64 + 32);
-                else probe(jacobi_solve_kernel<R, DIV, 128>, 4 * 128 + 32);
+                else if (k == 2) probe(jacobi_solve_kernel<R, DIV, 128>, 4 * 128 + 32);
+                else probe(jacobi_solve_kernel<R, DIV, 224>, 4 * 224 + 32);
                 DFSPH_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
                 // at most one block per SM: beyond that the passes are long
                 // enough to hide their launches, and the per-pass kernels
@@ -1537,12 +1538,13 @@ private:
         cudaError_t e;
         if (cb == 32) e = go(jacobi_solve_kernel<R, DIV, 32>);
         else if (cb == 64) e = go(jacobi_solve_kernel<R, DIV, 64>);
-        else e = go(jacobi_solve_kernel<R, DIV, 128>);
+        else if (cb == 128) e = go(jacobi_solve_kernel<R, DIV, 128>);
+        else e = go(jacobi_solve_kernel<R, DIV, 224>);
         if (e == cudaErrorCooperativeLaunchTooLarge && !capturing_) {
             // fewer SMs than the device reports (a partitioned GPU): the
             // per-pass solve from now on
             cudaGetLastError();
-            for (int k = 0; k < 3; ++k) coop_blocks_[DIV ? 1 : 0][k] = 0;
+            for (int k = 0; k < 4; ++k) coop_blocks_[DIV ? 1 : 0][k] = 0;
             return false;
         }
         DFSPH_CUDA(e);
@@ -1759,9 +1761,9 @@ private:
     int last_frame_graph_ = 0;
     cudaStream_t loop_stream_ = nullptr;
     bool iters_on_device_ = false;
-    // blocks of jacobi_solve_kernel one launch may hold, [DIV][64, 128, 256
-    // threads] (-1: not probed yet)
-    int coop_blocks_[2][3] = {{-1, -1, -1}, {-1, -1, -1}};
+    // blocks of jacobi_solve_kernel one launch may hold, [DIV][32, 64, 128,
+    // 224 particles] (-1: not probed yet)
+    int coop_blocks_[2][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}};
     bool fuse_advect_ = true;  // last density iteration carries the integrator when it can
     DevBuf<V4> tune_ck_;
     DevBuf<IterCtl> tune_ctl_;
