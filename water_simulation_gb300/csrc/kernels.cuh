@@ -953,9 +953,9 @@ __global__ void __launch_bounds__(LB) pressure_apply_kernel(
 // groups of four consecutive slots, lane q evaluating slot j0 + q. The group's
 // terms are exchanged within the quad and every lane adds them, in slot order,
 // with the one-lane pass's fused multiply-adds, so each lane ends with the
-// one-lane sum bit for bit while a particle's dependent chain of pair terms is
-// a quarter as long. Records come from shared memory when staged, else through
-// ld_coh.
+// one-lane sum bit for bit while it evaluates only a quarter of the
+// particle's pair terms. Records come from shared memory when staged, else
+// through ld_coh.
 template <class R>
 __device__ __forceinline__ R quad_get(unsigned qmask, R v, int src_lane) {
     return __shfl_sync(qmask, v, src_lane);
