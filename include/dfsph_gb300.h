@@ -152,7 +152,10 @@ int dfsph_set_boundary(dfsph_ctx* ctx, const float* xyz, uint32_t n, int mem);
 /* Fluid state: ParticleStore::resize + the position/velocity uploads of
  * sim_cli (apps/sim_cli/main.cpp:180-184). `vel` may be NULL (zero velocity,
  * as a freshly registered attribute). n > capacity => DFSPH_ERR_OUT_OF_RANGE
- * (ParticleStore::resize, core/src/particle_store.cu:11-17). */
+ * (ParticleStore::resize, core/src/particle_store.cu:11-17). With mem =
+ * DFSPH_MEM_HOST, page-locked 16-byte-aligned arrays are read in place by a
+ * kernel, other host memory through a staging copy; either way the arrays may
+ * be freed when the call returns. */
 int dfsph_set_fluid(dfsph_ctx* ctx, const float* xyz, const float* vel, uint32_t n, int mem);
 
 /* Scene batching (no counterpart in the reference: it steps one scene per
@@ -207,7 +210,10 @@ int dfsph_frame_config_init(dfsph_frame_config* fc);
 int dfsph_step_frames(dfsph_ctx* ctx, const dfsph_frame_config* fc, uint32_t n_frames, uint32_t* substeps);
 
 /* Field readback (density_at/alpha_at/boundary_mass_at, dfsph.cu:330-353, as
- * whole arrays). dst_bytes is checked against the field's size. */
+ * whole arrays). dst_bytes is checked against the field's size. Float particle
+ * fields bound for page-locked 16-byte-aligned host memory are written there
+ * in place by a kernel; other host memory receives a copy. Returns when the
+ * data is in dst. */
 int dfsph_get_field(dfsph_ctx* ctx, int field, void* dst, size_t dst_bytes, int mem);
 int dfsph_get_scalar(dfsph_ctx* ctx, int which, double* out);
 

@@ -548,6 +548,87 @@ __global__ void __launch_bounds__(256) export_kernel(int n, const u32* __restric
     if (rho_adv_out) rho_adv_out[i] = float(rho_adv[s]);
 }
 
+// Import from, and export to, caller memory that the GPU reads and writes in
+// place (page-locked host memory): the xyz triples of a block's 256
+// particles move as 16-byte accesses through shared memory, the few floats
+// past the block's last whole 16 bytes (the tail of the last block) as single
+// words. Base pointers are 16-byte aligned (checked by the host).
+__device__ __forceinline__ void load_triples(const float* __restrict__ src, int base, int cnt, float* tile) {
+    const int nf = 3 * cnt, n4 = nf / 4, t = threadIdx.x;
+    const float4* s4 = reinterpret_cast<const float4*>(src + 3 * size_t(base));
+    if (t < n4) reinterpret_cast<float4*>(tile)[t] = s4[t];
+    if (t < nf - 4 * n4) tile[4 * n4 + t] = src[3 * size_t(base) + 4 * n4 + t];
+}
+__device__ __forceinline__ void store_triples(float* __restrict__ dst, int base, int cnt, const float* tile) {
+    const int nf = 3 * cnt, n4 = nf / 4, t = threadIdx.x;
+    float4* d4 = reinterpret_cast<float4*>(dst + 3 * size_t(base));
+    if (t < n4) d4[t] = reinterpret_cast<const float4*>(tile)[t];
+    if (t < nf - 4 * n4) dst[3 * size_t(base) + 4 * n4 + t] = tile[4 * n4 + t];
+}
+
+// import_kernel on caller memory read in place (vel null: zero velocities)
+template <class R>
+__global__ void __launch_bounds__(256) import_mapped_kernel(int n, const float* __restrict__ pos,
+                                                            const float* __restrict__ vel,
+                                                            R4<R>* __restrict__ xk, R4<R>* __restrict__ vr,
+                                                            u32* __restrict__ id) {
+    __shared__ __align__(16) float tp[3 * 256];
+    __shared__ __align__(16) float tv[3 * 256];
+    const int base = blockIdx.x * 256;
+    const int cnt = min(256, n - base);
+    load_triples(pos, base, cnt, tp);
+    if (vel) load_triples(vel, base, cnt, tv);
+    __syncthreads();
+    const int t = threadIdx.x;
+    if (t >= cnt) return;
+    const int i = base + t;
+    xk[i] = {R(tp[3 * t]), R(tp[3 * t + 1]), R(tp[3 * t + 2]), R(0)};
+    if (vel)
+        vr[i] = {R(tv[3 * t]), R(tv[3 * t + 1]), R(tv[3 * t + 2]), R(0)};
+    else
+        vr[i] = {R(0), R(0), R(0), R(0)};
+    id[i] = static_cast<u32>(i);
+}
+
+// slot of every original index: inv[id[s]] = s
+static __global__ void __launch_bounds__(256) invert_kernel(int n, const u32* __restrict__ id,
+                                                            u32* __restrict__ inv) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) inv[id[s]] = static_cast<u32>(s);
+}
+
+// A per-slot field in original order, written in place to caller memory:
+// lane < 0 the xyz triple of in, lane 0..3 one lane of in, or (in null) the
+// scalar array sc. Thread t of the block takes original index base + t.
+template <class R>
+__global__ void __launch_bounds__(256) export_mapped_kernel(int n, const u32* __restrict__ inv,
+                                                            const R4<R>* __restrict__ in, int lane,
+                                                            const R* __restrict__ sc, float* __restrict__ out) {
+    __shared__ __align__(16) float tile[3 * 256];
+    const int base = blockIdx.x * 256;
+    const int cnt = min(256, n - base);
+    const int t = threadIdx.x;
+    if (!in) {
+        if (t < cnt) out[base + t] = float(sc[inv[base + t]]);
+        return;
+    }
+    if (lane >= 0) {
+        if (t < cnt) {
+            const R4<R> v = in[inv[base + t]];
+            out[base + t] = float(lane == 0 ? v.x : lane == 1 ? v.y : lane == 2 ? v.z : v.w);
+        }
+        return;
+    }
+    if (t < cnt) {
+        const R4<R> v = in[inv[base + t]];
+        tile[3 * t] = float(v.x);
+        tile[3 * t + 1] = float(v.y);
+        tile[3 * t + 2] = float(v.z);
+    }
+    __syncthreads();
+    store_triples(out, base, cnt, tile);
+}
+
 // Scatter a per-slot array to original order (double output for FP64 reads).
 template <class T, class O>
 __global__ void __launch_bounds__(256) unsort_kernel(int n, const u32* __restrict__ id,

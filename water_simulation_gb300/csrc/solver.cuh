@@ -210,14 +210,46 @@ public:
 
     void set_fluid_batch(u32 n_scenes, const u32* counts, const float* xyz, const float* vel, int mem) override {
         const u32 n = check_counts(n_scenes, counts);
-        const float* pos = upload(xyz, vel, n, mem);
-        const float* v = vel ? pos + 3 * size_t(n) : nullptr;
+        // page-locked host arrays are read in place by the import kernel;
+        // other host memory goes through the staging buffer
+        const float* mp = nullptr;
+        const float* mv = nullptr;
+        if (mem == DFSPH_MEM_HOST && n) {
+            mp = mapped_host(xyz);
+            mv = vel ? mapped_host(vel) : nullptr;
+            if (vel && !mv) mp = nullptr;
+        }
+        const float* pos = mp ? nullptr : upload(xyz, vel, n, mem);
+        const float* v = vel && pos ? pos + 3 * size_t(n) : nullptr;
         if (mem == DFSPH_MEM_DEVICE) { pos = xyz; v = vel; }
         install_counts(n_scenes, counts, n);
         if (n == 0) return;
-        launch_import(n, pos, v, xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
+        if (mp) {
+            launch(DFSPH_KERNEL_IO, import_mapped_kernel<R>, blocks_for(n, 256), 256, int(n), mp, mv, xk_[cx_].p,
+                   vr_[cv_].p, id_[ci_].p);
+            // the caller may free its arrays after return
+            DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        } else {
+            launch_import(n, pos, v, xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
+        }
         counts_valid_ = false;
         have_state_ = true;
+    }
+
+    // The device address of caller memory passed as host memory when the GPU
+    // can use it in place: page-locked (registered or cudaHostAlloc) and
+    // 16-byte aligned. Null for pageable or unaligned memory.
+    static const float* mapped_host(const void* p) {
+        if (!p || (reinterpret_cast<uintptr_t>(p) & 15u)) return nullptr;
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        if (a.type != cudaMemoryTypeHost || !a.devicePointer ||
+            (reinterpret_cast<uintptr_t>(a.devicePointer) & 15u))
+            return nullptr;
+        return static_cast<const float*>(a.devicePointer);
     }
 
     u32 check_counts(u32 n_scenes, const u32* counts) const {
@@ -341,6 +373,7 @@ public:
         if ((field == DFSPH_FIELD_NBR_FLUID || field == DFSPH_FIELD_NBR_BOUNDARY) && !cfg_.record_diagnostics)
             throw Error(DFSPH_ERR_STATE, "neighbour counts need record_diagnostics = 1");
         if (need == 0) return;
+        if (mem == DFSPH_MEM_HOST && export_mapped(field, dst)) return;
         // Produce the field in device scratch (original order), then copy out.
         void* out = (mem == DFSPH_MEM_DEVICE) ? dst : scratch_bytes(need);
         const int nb = blocks_for(std::max<size_t>(n, 1), 256);
@@ -386,6 +419,34 @@ public:
             DFSPH_CUDA(cudaMemcpyAsync(dst, out, need, cudaMemcpyDeviceToHost, stream_));
             DFSPH_CUDA(cudaStreamSynchronize(stream_));
         }
+    }
+
+    // The float particle fields written in place to page-locked host memory
+    // (export_mapped_kernel, in original order); false for other fields or
+    // memory, which take the staging copy.
+    bool export_mapped(int field, void* dst) {
+        const V4* in = nullptr;
+        const R* sc = nullptr;
+        int lane = -1;
+        switch (field) {
+            case DFSPH_FIELD_POSITION: in = xk_[cx_].p; break;
+            case DFSPH_FIELD_VELOCITY: in = vr_[cv_].p; break;
+            case DFSPH_FIELD_DENSITY: in = vr_[cv_].p; lane = 3; break;
+            case DFSPH_FIELD_ALPHA: sc = alpha_.p; break;
+            case DFSPH_FIELD_KAPPA: sc = kap_.p; break;
+            case DFSPH_FIELD_DENSITY_ADV: sc = rho_adv_.p; break;
+            case DFSPH_FIELD_KAPPA_V: sc = kap_v_.p; break;
+            default: return false;
+        }
+        float* out = const_cast<float*>(mapped_host(dst));
+        if (!out) return false;
+        const size_t n = n_;
+        u32* inv = static_cast<u32*>(scratch_bytes(n * sizeof(u32)));
+        launch(DFSPH_KERNEL_IO, invert_kernel, blocks_for(n, 256), 256, int(n), (const u32*)id_[ci_].p, inv);
+        launch(DFSPH_KERNEL_IO, export_mapped_kernel<R>, blocks_for(n, 256), 256, int(n), (const u32*)inv, in, lane,
+               sc, out);
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        return true;
     }
 
     double get_scalar(int which) override {
