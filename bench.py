@@ -241,12 +241,12 @@ def bench_ours(args, rank, world):
         share[_lib.KERNEL_NAMES[k]] = s.profile_read(k)
     dominant = max(share, key=lambda k: share[k][0])
     dom_id = _lib.KERNEL_NAMES.index(dominant)
-    # adaptive solves of a small scene run as one cooperative launch, which a
-    # profiled pass would split: their timed steps run unprofiled and the
-    # dominant pass's launch time comes from the profiled warm-up
-    adaptive = (sc.eta_density > 0 and sc.max_density_iters > 0) or (
-        sc.eta_divergence > 0 and sc.max_divergence_iters > 0)
-    s.profile_enable(0 if adaptive else 1 << dom_id)
+    # the solves of a small scene (at most 224 particles per SM) run as one
+    # cooperative launch each, which a profiled pass would split: their timed
+    # steps run unprofiled and the dominant pass's launch time comes from the
+    # profiled warm-up
+    coop = sc.n <= 224 * torch.cuda.get_device_properties(local).multi_processor_count
+    s.profile_enable(0 if coop else 1 << dom_id)
     nb_active = s.active_boundary()
     l0 = s.kernel_launches()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -264,14 +264,14 @@ def bench_ours(args, rank, world):
     barrier(world)
     launches = s.kernel_launches() - l0
     ms = sum(a.elapsed_time(b) for a, b in ev)
-    dom_ms, dom_launches = share[dominant] if adaptive else s.profile_read(dom_id)
+    dom_ms, dom_launches = share[dominant] if coop else s.profile_read(dom_id)
     s.profile_enable(0)
     from water_simulation_gb300 import replicas
 
     ms_max, work = replicas.aggregate(ms, float(sc.n) * args.steps, world)
     res = {"ms_total": ms_max, "work": work, "wall_s": wall, "launches": launches, "clocks": clk.summary(),
            "dominant": dominant, "dominant_ms": dom_ms, "dominant_launches": dom_launches,
-           "dominant_timed_in": "warm-up steps (passes apart)" if adaptive else "timed steps",
+           "dominant_timed_in": "warm-up steps (passes apart)" if coop else "timed steps",
            "nb_active": nb_active,
            "block_sizes": {k: tuned[k] for k in ("density_alpha", "pressure_rate", "pressure_apply", "forces_xsph")},
            "warmup_raw": share,

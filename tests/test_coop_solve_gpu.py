@@ -116,3 +116,17 @@ def test_cooperative_solve_largest_blocks():
     assert it0 == it1 and sum(a + b for a, b in it0) > 2 * 6
     assert np.array_equal(x0, x1) and np.array_equal(v0, v1) and np.array_equal(r0, r1)
     assert l0 < l1
+
+
+def test_cooperative_solve_fixed_iterations():
+    """Fixed iteration counts (eta = 0, the reference's step): the solves of a
+    small scene are cooperative launches too, equal bit for bit to the
+    per-pass solve, which fuses its last apply pass with the integrator."""
+    sc = scenes.puddle()
+    sc.velocity = np.random.default_rng(5).normal(0, 0.3, size=sc.fluid.shape).astype(np.float32)
+    sc.max_density_iters, sc.max_divergence_iters, sc.eta_density, sc.eta_divergence = 4, 2, 0.0, 0.0
+    x0, v0, r0, it0, l0 = _run(sc, False, 10)
+    x1, v1, r1, it1, l1 = _run(sc, True, 10)
+    assert it0 == it1 == [(2, 4)] * 10
+    assert np.array_equal(x0, x1) and np.array_equal(v0, v1) and np.array_equal(r0, r1)
+    assert l0 < l1

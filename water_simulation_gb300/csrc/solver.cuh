@@ -1461,10 +1461,12 @@ private:
         const bool adaptive = eta > 0.0f;
         const double thr = double(eta) * double(cfg_.rest_density);
         const u32 first_check = DIV ? 0u : 1u;  // density: from the 2nd iteration (dfsph.cu:255)
-        if (adaptive && !tp) {
-            // small scenes: the whole solve in one cooperative launch
+        if (!tp) {
+            // small scenes: the whole solve in one cooperative launch (with
+            // eta = 0 its stop decision never fires: max_iters iterations)
             if (solve_cooperative<DIV>(sd, max_iters, thr, first_check, ctl, kap_out, adv_out, cs)) return max_iters;
-            if (capturing_) return solve_on_device<DIV>(sd, max_iters, thr, first_check, ctl, kap_out, adv_out, cs);
+            if (adaptive && capturing_)
+                return solve_on_device<DIV>(sd, max_iters, thr, first_check, ctl, kap_out, adv_out, cs);
         }
         const int w = DIV ? 0 : 1;
         u32 launched = 0;
