@@ -90,16 +90,19 @@ def parse():
     return ap.parse_args()
 
 
-def make_scene(name):
+def make_scene(name, sampler=None):
+    """The named workload; `sampler` samples the walls (default: the library's
+    sample_aabb_boundary; the reference arm passes the oracle's, so that it
+    never loads the library)."""
     from water_simulation_gb300 import scenes
 
     if name == "dam1m":
-        return scenes.dam_break(scale=2, reference_mode=True)
+        return scenes.dam_break(scale=2, reference_mode=True, sampler=sampler)
     if name == "dam128k":
-        return scenes.dam_break(scale=1, reference_mode=True)
+        return scenes.dam_break(scale=1, reference_mode=True, sampler=sampler)
     if name == "dam128k_div":  # with 2 divergence-solver iterations (the reference has none)
-        return scenes.dam_break(scale=1, reference_mode=False)
-    sc = scenes.puddle()
+        return scenes.dam_break(scale=1, reference_mode=False, sampler=sampler)
+    sc = scenes.puddle(sampler=sampler)
     if name == "puddle_adaptive":  # the settled puddle as the reference runs it: adaptive density solve
         sc.max_divergence_iters, sc.eta_divergence = 0, 0.0  # (0.01 %, <= 100 iterations), no divergence solver
         sc.name = "puddle_4913_adaptive"
@@ -230,6 +233,11 @@ def bench_ours(args, rank, world):
     # launch shapes of the neighbour passes, measured on this workload (the
     # state is restored afterwards)
     tuned = s.autotune(sc.dt, 3) if not args.no_autotune else s.block_sizes()
+    # the solves of a small scene run as one cooperative launch each, which a
+    # profiled pass would split: one plain step tells (the library counts them)
+    c0 = s.scalar(_lib.SCALAR_COOP_SOLVES)
+    s.step(sc.dt)
+    coop = s.scalar(_lib.SCALAR_COOP_SOLVES) > c0
     # warm-up, with every kernel class profiled to find the dominant one
     s.profile_enable((1 << _lib.KERNEL_CLASSES) - 1)
     for _ in range(args.warmup):
@@ -241,11 +249,8 @@ def bench_ours(args, rank, world):
         share[_lib.KERNEL_NAMES[k]] = s.profile_read(k)
     dominant = max(share, key=lambda k: share[k][0])
     dom_id = _lib.KERNEL_NAMES.index(dominant)
-    # the solves of a small scene (at most 224 particles per SM) run as one
-    # cooperative launch each, which a profiled pass would split: their timed
-    # steps run unprofiled and the dominant pass's launch time comes from the
-    # profiled warm-up
-    coop = sc.n <= 224 * torch.cuda.get_device_properties(local).multi_processor_count
+    # cooperative solves: the timed steps run unprofiled and the dominant
+    # pass's launch time comes from the profiled warm-up
     s.profile_enable(0 if coop else 1 << dom_id)
     nb_active = s.active_boundary()
     l0 = s.kernel_launches()
@@ -379,12 +384,15 @@ def bench_frames(n_frames=24):
     device and both solves run as device-resident loops, one graph launch per
     frame, against the reference's host loop (max |v| read back before every
     substep, the mean error after every iteration). Wall time of n_frames
-    frames from rest; both runs take the same substeps and iterations."""
+    frames from rest. Both paths take e^{-d dt} from the same device function,
+    so they take the same substeps and iterations and end in the same state
+    (checked: same_substeps, same_state)."""
     from water_simulation_gb300 import scenes
     from water_simulation_gb300.solver import Solver
 
     sc = scenes.puddle()
     out = {"workload": "puddle_4913, adaptive solvers, 24 fps", "frames": n_frames}
+    final = {}
     for name, graph in (("device", True), ("host_loop", False)):
         cfg = sc.config()
         cfg.use_cuda_graph = 1 if graph else 0
@@ -398,44 +406,46 @@ def bench_frames(n_frames=24):
         s.synchronize()
         t1 = time.perf_counter()
         x = s.positions()
+        final[name] = (list(subs), x, s.velocities())
         out[name] = {"ms_per_frame": 1e3 * (t1 - t0) / n_frames, "substeps": int(subs.sum()),
                      "ms_per_substep": 1e3 * (t1 - t0) / max(int(subs.sum()), 1),
                      "on_device": s.frames_on_device(), "min_y_m": float(x[:, 1].min())}
         s.close()
     out["speedup"] = out["host_loop"]["ms_per_frame"] / out["device"]["ms_per_frame"]
+    a, b = final["device"], final["host_loop"]
+    out["same_substeps"] = a[0] == b[0]
+    out["same_state"] = bool(np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2]))
     return out
 
 
 def bench_precision(sc, checkpoints=(50, 500)):
     """Field error of the FP32 step (plain and with Kahan density sums; both
     with FP64 convergence reductions) against the FP64 build of the same
-    kernels, after each number of steps in `checkpoints` along one trajectory
-    from the same input."""
+    kernels. Every build bins and centres the stencil with the same float
+    arithmetic, so from identical inputs the builds visit identical neighbour
+    sets and differ by rounding only ("one_step_from_same_input"). Along one
+    trajectory (the checkpoints) the positions drift apart by rounding, and a
+    particle near a cell face can then see a different candidate set in the
+    two builds (the stencil is truncated at one cell of length l against a
+    support of 2l, so such a pair enters one sum with a jump). The FP32 and
+    FP64 runs are stepped in lockstep for the first checkpoint and compare
+    their candidate-set signatures after every step: "flipped" particles saw
+    a different set at some step, "near_flip" ones shared a cell
+    neighbourhood (27 cells) with a flipped particle at the end."""
     import time as _time
 
     from water_simulation_gb300 import _lib
-    from water_simulation_gb300.solver import solver_for
+    from water_simulation_gb300.solver import Solver, solver_for
 
-    fields = {}
-    for name, prec in (("fp64", _lib.PRECISION_FP64), ("fp32", _lib.PRECISION_FP32),
-                       ("fp32_kahan", _lib.PRECISION_FP32_KAHAN)):
-        s = solver_for(sc, precision=prec)
-        done = 0
-        fields[name] = {}
-        t0 = _time.perf_counter()
-        for c in checkpoints:
-            s.step(sc.dt, c - done)
-            done = c
-            fields[name][c] = {"x": s.field(_lib.FIELD_POSITION).astype(np.float64),
-                               "v": s.field(_lib.FIELD_VELOCITY).astype(np.float64),
-                               "rho": s.field(_lib.FIELD_DENSITY).astype(np.float64)}
-        fields[name]["wall_s"] = _time.perf_counter() - t0
-        s.close()
+    def snap(s):
+        return {"x": s.field(_lib.FIELD_POSITION).astype(np.float64),
+                "v": s.field(_lib.FIELD_VELOCITY).astype(np.float64),
+                "rho": s.field(_lib.FIELD_DENSITY).astype(np.float64)}
 
-    def errors(f, ref):
+    def errors(f, ref, mask=None):
         vs = np.linalg.norm(ref["v"], axis=1).max()
         rel = np.abs(f["rho"] - ref["rho"]) / np.abs(ref["rho"])
-        return {
+        out = {
             "density_max_rel": float(rel.max()),
             "density_rel_p50": float(np.percentile(rel, 50)),
             "density_rel_p99": float(np.percentile(rel, 99)),
@@ -444,13 +454,79 @@ def bench_precision(sc, checkpoints=(50, 500)):
             "position_max_abs_m": float(np.abs(f["x"] - ref["x"]).max()),
             "velocity_max_abs_rel_to_max_speed": float(np.abs(f["v"] - ref["v"]).max() / max(vs, 1e-30)),
         }
+        if mask is not None:
+            out["density_max_rel_without_flips"] = float(rel[~mask].max()) if (~mask).any() else 0.0
+        return out, rel
 
-    out = {}
+    ctxs = {name: solver_for(sc, precision=prec, diagnostics=(name != "fp32_kahan"))
+            for name, prec in (("fp64", _lib.PRECISION_FP64), ("fp32", _lib.PRECISION_FP32),
+                               ("fp32_kahan", _lib.PRECISION_FP32_KAHAN))}
+    # lockstep to the first checkpoint, candidate-set signatures compared every step
     first = checkpoints[0]
+    flipped = np.zeros(sc.n, bool)
+    flips_per_step = []
+    t0 = _time.perf_counter()
+    for _ in range(first):
+        for s in ctxs.values():
+            s.step(sc.dt)
+        d = ctxs["fp32"].field(_lib.FIELD_NBR_SIGNATURE) != ctxs["fp64"].field(_lib.FIELD_NBR_SIGNATURE)
+        flips_per_step.append(int(d.sum()))
+        flipped |= d
+    lockstep_s = _time.perf_counter() - t0
+    # particles within one cell (27-cell neighbourhood) of a flipped particle
+    s64 = ctxs["fp64"]
+    dims = s64.dims
+    keys = s64.field(_lib.FIELD_CELL_KEY).astype(np.int64)
+    total = int(dims[0]) * int(dims[1]) * int(dims[2])
+    grid = np.zeros(total + 1, bool)
+    grid[keys[flipped]] = True
+    g3 = grid[:total].reshape(dims)
+    for ax in range(3):
+        a = g3.copy()
+        sl = [slice(None)] * 3
+        sl[ax] = slice(1, None)
+        src = [slice(None)] * 3
+        src[ax] = slice(None, -1)
+        a[tuple(sl)] |= g3[tuple(src)]
+        a[tuple(src)] |= g3[tuple(sl)]
+        g3 = a
+    grid[:total] = g3.ravel()
+    near = grid[keys] | flipped
+    f = {name: snap(s) for name, s in ctxs.items()}
+    out = {}
     for name in ("fp32", "fp32_kahan"):
-        out[name] = errors(fields[name][first], fields["fp64"][first])  # at the first checkpoint
-        for c in checkpoints[1:]:
-            out[f"{name}_at_{c}_steps"] = errors(fields[name][c], fields["fp64"][c])
+        e, rel = errors(f[name], f["fp64"], flipped)
+        e["density_max_rel_away_from_flips"] = float(rel[~near].max()) if (~near).any() else 0.0
+        e["over_1e-4"] = int((rel > 1e-4).sum())
+        e["over_1e-4_flipped"] = int((rel[flipped] > 1e-4).sum())
+        e["over_1e-4_near_flip"] = int((rel[near] > 1e-4).sum())
+        out[name] = e
+    out["flipped_particles"] = int(flipped.sum())
+    out["near_flip_particles"] = int(near.sum())
+    out["flips_per_step_max"] = int(max(flips_per_step)) if flips_per_step else 0
+    out["flips_first_step"] = next((k for k, c in enumerate(flips_per_step) if c), None)
+    # one step of each build from the same (FP32) state: rounding only
+    x32, v32 = f["fp32"]["x"].astype(np.float32), f["fp32"]["v"].astype(np.float32)
+    probe = {}
+    for name, prec in (("fp64", _lib.PRECISION_FP64), ("fp32", _lib.PRECISION_FP32)):
+        s = solver_for(sc, precision=prec, diagnostics=True)
+        s.set_fluid(x32, v32)
+        s.step(sc.dt)
+        probe[name] = snap(s)
+        probe[name]["sig"] = s.field(_lib.FIELD_NBR_SIGNATURE)
+        s.close()
+    e1, _ = errors(probe["fp32"], probe["fp64"])
+    e1["candidate_sets_differ"] = int((probe["fp32"]["sig"] != probe["fp64"]["sig"]).sum())
+    out[f"one_step_from_same_input_at_step_{first}"] = e1
+    # the rest of the trajectory
+    for c in checkpoints[1:]:
+        for s in ctxs.values():
+            s.step(sc.dt, c - first)
+        g = {name: snap(s) for name, s in ctxs.items()}
+        for name in ("fp32", "fp32_kahan"):
+            out[f"{name}_at_{c}_steps"] = errors(g[name], g["fp64"])[0]
+    for s in ctxs.values():
+        s.close()
     # the flow's own sensitivity: FP32 against FP32 from positions one ulp
     # away, at the last checkpoint
     import copy
@@ -459,14 +535,14 @@ def bench_precision(sc, checkpoints=(50, 500)):
     moved.fluid = np.nextafter(sc.fluid, np.float32(np.inf)).astype(np.float32)
     s = solver_for(moved, precision=_lib.PRECISION_FP32)
     s.step(sc.dt, checkpoints[-1])
-    g = {"x": s.field(_lib.FIELD_POSITION).astype(np.float64), "v": s.field(_lib.FIELD_VELOCITY).astype(np.float64),
-         "rho": s.field(_lib.FIELD_DENSITY).astype(np.float64)}
+    gm = snap(s)
     s.close()
-    out[f"fp32_vs_fp32_1ulp_input_at_{checkpoints[-1]}_steps"] = errors(g, fields["fp32"][checkpoints[-1]])
+    out[f"fp32_vs_fp32_1ulp_input_at_{checkpoints[-1]}_steps"] = errors(gm, g["fp32"])[0] if len(checkpoints) > 1 \
+        else None
     out["steps"] = first
     out["checkpoints"] = list(checkpoints)
-    out["fp64_wall_s"] = fields["fp64"]["wall_s"]
-    out["reference"] = "FP64 build of the same kernels"
+    out["lockstep_wall_s"] = lockstep_s
+    out["reference"] = "FP64 build of the same kernels (float cell arithmetic, as the FP32 build)"
     return out
 
 
@@ -679,15 +755,41 @@ def bench_ref_cuda(sc, steps, warmup=1):
             "steps": steps, "kind": "reference kernels from its sources, sm_103a, same GPU"}
 
 
+def oracle_config(sc):
+    """The oracle's configuration of a scene, built without the library (the
+    values Scene.config() gives the library's dfsph_config). The stencil is
+    centred with the IEEE reciprocal of the cell length, which changes no
+    timing."""
+    from oracle import oracle as O
+
+    c = O.OracleConfig()
+    c.rest_density = 1000.0
+    c.particle_radius = sc.radius
+    c.smoothing_length = np.float32(2.0 * np.float32(sc.radius))
+    c.viscosity = sc.viscosity
+    c.damping = sc.damping
+    c.surface_tension = 0.0
+    c.gravity[0], c.gravity[1], c.gravity[2] = 0.0, -9.81, 0.0
+    c.max_density_iters = sc.max_density_iters
+    c.max_divergence_iters = sc.max_divergence_iters
+    c.eta_density = sc.eta_density
+    c.eta_divergence = sc.eta_divergence
+    for a in range(3):
+        c.domain_min[a] = sc.domain_min[a]
+        c.domain_max[a] = sc.domain_max[a]
+    c.stencil_inv_cell = 0.0
+    return c
+
+
 def reference_arm(args, rank, world):
     """The reference arm: the reference step has no CPU implementation, so the
     arm times the FP32 restatement (oracle/) on all host cores, rank 0 only."""
     if rank != 0:
         return None
-    sc = make_scene(args.workload)
     from oracle import oracle as O
 
-    c = O.config_from(sc.config())
+    sc = make_scene(args.workload, sampler=O.sample_aabb_boundary)
+    c = oracle_config(sc)
     L = O.load()
     cores = L.oracle_max_threads()
     o = O.Oracle(c, sc.fluid, sc.velocity, sc.boundary, precision=32)

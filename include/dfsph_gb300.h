@@ -93,6 +93,10 @@ typedef struct dfsph_ctx dfsph_ctx;
 #define DFSPH_FIELD_KAPPA_V          12  /* float[n]    divergence-solver kappa                    */
 #define DFSPH_FIELD_BOUNDARY_CELL_START   13  /* uint32[C+1] boundary CellGrid::cell_start()      */
 #define DFSPH_FIELD_BOUNDARY_SORTED_INDEX 14  /* uint32[nb] boundary CellGrid::sorted_indices()   */
+#define DFSPH_FIELD_NBR_SIGNATURE    15  /* uint32[n]   signature of the candidate set visited at the last
+                                            density pass: sum of mixed ids (needs record_diagnostics);
+                                            equal sets give equal signatures, so comparing two runs
+                                            finds the particles whose stencil membership differs */
 
 /* Scalars readable with dfsph_get_scalar(). */
 #define DFSPH_SCALAR_MAX_VELOCITY          0  /* DFSPHSolver::max_velocity() (dfsph.h:40) */
@@ -113,6 +117,9 @@ typedef struct dfsph_ctx dfsph_ctx;
                                                  2h of them (counted on demand, last grid) */
 #define DFSPH_SCALAR_FRAME_GRAPH          13  /* 1: the last dfsph_step_frames ran as device-stepped
                                                  graphs; 0: as the host loop */
+#define DFSPH_SCALAR_COOP_SOLVES          15  /* Jacobi solves this context ran as one cooperative launch
+                                                 (a small scene's solve; counted at launch, or once at
+                                                 capture for a graph) */
 #define DFSPH_SCALAR_BOUNDS_VIOLATIONS    14  /* neighbour runs outside their cell_start range seen
                                                  by the bounds-checked build (-DDFSPH_BOUNDS_CHECK),
                                                  all contexts of the library; -1 in the normal build */
@@ -274,8 +281,26 @@ int dfsph_load_state(dfsph_ctx* ctx, const char* path);
 int dfsph_autotune(dfsph_ctx* ctx, float dt, uint32_t steps, int32_t* block_sizes);
 int dfsph_get_block_sizes(dfsph_ctx* ctx, int32_t* block_sizes);
 
-/* Wait for the context's stream; returns a pending device error if any. */
+/* Wait for the context's stream; returns a pending device error if any,
+ * DFSPH_ERR_DEVICE_TIMEOUT when a bounded device wait gave up (below). */
 int dfsph_synchronize(dfsph_ctx* ctx);
+
+/* Bounded device waits. Replaces the host synchronisation of the reference's
+ * density solve, which reads the error back after every iteration
+ * (solvers/dfsph/src/dfsph.cu:296-299): a small scene's Jacobi solve runs as
+ * one cooperative launch whose blocks meet at a grid barrier twice per
+ * iteration. Every such wait gives up after limit_ns nanoseconds (default
+ * 1e9), sets the context's device error word and returns; the next
+ * dfsph_synchronize, dfsph_get_field or dfsph_step_frames returns
+ * DFSPH_ERR_DEVICE_TIMEOUT and clears the word. The state of the step that
+ * timed out is not valid; set it again (dfsph_set_fluid, dfsph_load_state) to
+ * continue. No trap, fault or endless wait is left on the device. */
+int dfsph_set_wait_limit(dfsph_ctx* ctx, uint64_t limit_ns);
+/* Test hook (no use outside tests): the grid barrier also waits for
+ * missing_blocks blocks that do not exist, so every wait runs out after the
+ * limit and the timeout path runs without a GPU fault. 0 restores the normal
+ * barrier. */
+int dfsph_test_stall_waits(dfsph_ctx* ctx, uint32_t missing_blocks);
 
 const char* dfsph_last_error(const dfsph_ctx* ctx);
 const char* dfsph_status_string(int status);
@@ -346,7 +371,13 @@ int dfsph_cohesion_kernel(const float* r_dev, uint32_t n, float support, float* 
  * dims.x*dims.y*dims.z <= DFSPH_STATIC_GRID_MAX_CELLS, else
  * DFSPH_ERR_OUT_OF_RANGE. All calls share the scratch: calls that overlap on
  * the GPU race. The first call on a device looks the scratch address up (a
- * runtime query); make it before any stream capture. */
+ * runtime query); make it before any stream capture. The address is kept for
+ * the life of the process: after cudaDeviceReset on that device (which
+ * unloads the library's device memory) this entry point must not be called
+ * again. As in dfsph_build_cell_grid, ordering the particles of one cell takes
+ * time proportional to the square of that cell's occupancy (out-of-grid
+ * particles all share one key), so inputs that pile many particles into one
+ * cell make a slow call. */
 #define DFSPH_STATIC_GRID_MAX_PARTICLES 131072u
 #define DFSPH_STATIC_GRID_MAX_CELLS     1048576u
 #define DFSPH_STATIC_GRID_SCRATCH_BYTES (7u * 1024u * 1024u)

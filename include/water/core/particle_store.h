@@ -1,18 +1,25 @@
-// ParticleStore: fixed-capacity particle arrays with named attributes, each a
-// zero-filled stream-ordered device buffer; position and velocity are AoS Vec3f.
-// Same interface and error behaviour as the reference
-// (core/include/water/core/particle_store.h:15-127, core/src/particle_store.cu):
-// resize beyond capacity throws std::out_of_range, registering a name twice
-// throws std::runtime_error.
+// ParticleStore: particle arrays of a fixed capacity with named, typed
+// attributes; position and velocity are AoS Vec3f. The public interface and
+// error behaviour are the reference's (core/include/water/core/particle_store.h
+// :15-127, core/src/particle_store.cu): resize beyond the capacity throws
+// std::out_of_range, a handle that names no attribute throws
+// std::out_of_range, registering a name twice throws std::runtime_error, and
+// every attribute starts zero-filled.
+//
+// Storage is pooled: attributes are carved, 256-byte aligned, out of arena
+// blocks of device memory (stream ordered on the store's stream), so the
+// position, velocity and the solver's four scalar attributes of a store live
+// in one allocation instead of six. An attribute that does not fit the free
+// tail of the current block opens a new block (existing attributes never
+// move: their pointers stay valid for the store's lifetime).
 #pragma once
 
 #include <cuda_runtime.h>
 
-#include <memory>
+#include <cstddef>
 #include <stdexcept>
 #include <string>
 #include <string_view>
-#include <unordered_map>
 #include <vector>
 
 #include "water/core/device_buffer.h"
@@ -22,21 +29,10 @@ namespace water {
 
 enum class AttribType { F32, F32x3, U32 };
 
+// Bytes per particle of an attribute type.
 inline std::size_t attrib_element_size(AttribType t) {
-    switch (t) {
-        case AttribType::F32: return sizeof(float);
-        case AttribType::F32x3: return 3 * sizeof(float);
-        case AttribType::U32: return sizeof(unsigned);
-    }
-    return 0;
+    return t == AttribType::F32x3 ? 3 * sizeof(float) : sizeof(float);  // F32 and U32 are both 4 bytes
 }
-
-struct AttribStorage {
-    std::string name;
-    AttribType type;
-    std::size_t element_size;
-    std::unique_ptr<DeviceBuffer<unsigned char>> buffer;
-};
 
 template <typename T>
 class AttribHandle {
@@ -47,13 +43,17 @@ public:
     bool valid() const noexcept { return index_ != npos; }
 
 private:
-    static constexpr std::size_t npos = static_cast<std::size_t>(-1);
+    static constexpr std::size_t npos = ~std::size_t(0);
     std::size_t index_ = npos;
 };
 
 class ParticleStore {
 public:
-    explicit ParticleStore(std::size_t capacity, cudaStream_t stream = 0) : capacity_(capacity), stream_(stream) {
+    // The first arena block is sized for position, velocity and four scalar
+    // attributes per particle (the solver's density, alpha, kappa, rho*).
+    explicit ParticleStore(std::size_t capacity, cudaStream_t stream = 0)
+        : capacity_(capacity), stream_(stream) {
+        reserve_block(2 * padded(capacity * sizeof(Vec3f)) + 4 * padded(capacity * sizeof(float)));
         position_ = register_attribute<Vec3f>("position", AttribType::F32x3);
         velocity_ = register_attribute<Vec3f>("velocity", AttribType::F32x3);
     }
@@ -66,38 +66,37 @@ public:
     AttribHandle<Vec3f> position_handle() const noexcept { return position_; }
     AttribHandle<Vec3f> velocity_handle() const noexcept { return velocity_; }
 
-    Vec3f* positions() { return typed<Vec3f>(position_); }
-    Vec3f* velocities() { return typed<Vec3f>(velocity_); }
-    const Vec3f* positions() const { return typed_const<Vec3f>(position_); }
-    const Vec3f* velocities() const { return typed_const<Vec3f>(velocity_); }
+    Vec3f* positions() { return attribute_data(position_); }
+    Vec3f* velocities() { return attribute_data(velocity_); }
+    const Vec3f* positions() const { return attribute_data(position_); }
+    const Vec3f* velocities() const { return attribute_data(velocity_); }
 
     template <typename T>
     AttribHandle<T> register_attribute(std::string_view name, AttribType type) {
-        std::string key{name};
-        if (name_to_index_.count(key)) throw std::runtime_error("ParticleStore: attribute already registered: " + key);
-        AttribStorage st;
-        st.name = key;
-        st.type = type;
-        st.element_size = attrib_element_size(type);
-        st.buffer = std::make_unique<DeviceBuffer<unsigned char>>(capacity_ * st.element_size, stream_);
-        st.buffer->fill_zero();
-        const std::size_t idx = attribs_.size();
-        attribs_.push_back(std::move(st));
-        name_to_index_[key] = idx;
-        return AttribHandle<T>(idx);
+        if (find(name) != attribs_.size())
+            throw std::runtime_error("ParticleStore: the attribute '" + std::string(name) + "' exists already");
+        const std::size_t bytes = capacity_ * attrib_element_size(type);
+        unsigned char* at = carve(bytes);
+        if (bytes) WATER_CUDA_CHECK(cudaMemsetAsync(at, 0, bytes, stream_));
+        attribs_.push_back(Attrib{std::string(name), type, at});
+        return AttribHandle<T>(attribs_.size() - 1);
     }
 
     template <typename T>
-    T* attribute_data(AttribHandle<T> h) { return typed<T>(h); }
+    T* attribute_data(AttribHandle<T> h) {
+        return reinterpret_cast<T*>(slot(h.index()).data);
+    }
     template <typename T>
-    const T* attribute_data(AttribHandle<T> h) const { return typed_const<T>(h); }
+    const T* attribute_data(AttribHandle<T> h) const {
+        return reinterpret_cast<const T*>(slot(h.index()).data);
+    }
 
-    bool has_attribute(std::string_view name) const { return name_to_index_.count(std::string{name}) != 0; }
+    bool has_attribute(std::string_view name) const { return find(name) != attribs_.size(); }
 
     void resize(std::size_t count) {
         if (count > capacity_)
-            throw std::out_of_range("ParticleStore::resize: count " + std::to_string(count) + " exceeds capacity " +
-                                    std::to_string(capacity_));
+            throw std::out_of_range("ParticleStore::resize: " + std::to_string(count) + " particles requested, " +
+                                    std::to_string(capacity_) + " is the capacity");
         count_ = count;
     }
     std::size_t count() const noexcept { return count_; }
@@ -105,22 +104,44 @@ public:
     cudaStream_t stream() const noexcept { return stream_; }
 
 private:
-    template <typename T>
-    T* typed(AttribHandle<T> h) {
-        if (!h.valid() || h.index() >= attribs_.size()) throw std::out_of_range("ParticleStore: invalid handle");
-        return reinterpret_cast<T*>(attribs_[h.index()].buffer->data());
+    static constexpr std::size_t kAlign = 256;
+    static constexpr std::size_t padded(std::size_t b) noexcept { return (b + kAlign - 1) / kAlign * kAlign; }
+
+    struct Attrib {
+        std::string name;
+        AttribType type;
+        unsigned char* data;  // inside one of blocks_
+    };
+
+    // index of the attribute called `name`, or attribs_.size()
+    std::size_t find(std::string_view name) const {
+        std::size_t k = 0;
+        while (k < attribs_.size() && attribs_[k].name != name) ++k;
+        return k;
     }
-    template <typename T>
-    const T* typed_const(AttribHandle<T> h) const {
-        if (!h.valid() || h.index() >= attribs_.size()) throw std::out_of_range("ParticleStore: invalid handle");
-        return reinterpret_cast<const T*>(attribs_[h.index()].buffer->data());
+    const Attrib& slot(std::size_t index) const {
+        if (index >= attribs_.size()) throw std::out_of_range("ParticleStore: no attribute behind this handle");
+        return attribs_[index];
+    }
+    void reserve_block(std::size_t bytes) {
+        blocks_.emplace_back(bytes, stream_);
+        used_ = 0;
+    }
+    // `bytes` of the current block's free tail, or of a new block
+    unsigned char* carve(std::size_t bytes) {
+        const std::size_t need = padded(bytes);
+        if (blocks_.empty() || used_ + need > blocks_.back().size()) reserve_block(need);
+        unsigned char* p = blocks_.back().data() + used_;
+        used_ += need;
+        return p;
     }
 
     std::size_t capacity_;
     std::size_t count_ = 0;
     cudaStream_t stream_;
-    std::vector<AttribStorage> attribs_;
-    std::unordered_map<std::string, std::size_t> name_to_index_;
+    std::vector<DeviceBuffer<unsigned char>> blocks_;
+    std::size_t used_ = 0;  // bytes taken from blocks_.back()
+    std::vector<Attrib> attribs_;
     AttribHandle<Vec3f> position_;
     AttribHandle<Vec3f> velocity_;
 };

@@ -118,6 +118,12 @@ inline Dual exp(const Dual& a) {
     return {e, e * a.d};
 }
 inline double floor(const Dual& a) { return std::floor(a.v); }
+// A coordinate as the cell arithmetic sees it: rounded to float in every
+// instance (the FP64 and dual instances keep the FP32 instance's neighbour
+// structure for the same positions; a dual's derivative plays no part).
+inline float cell_coord(float p) { return p; }
+inline float cell_coord(double p) { return static_cast<float>(p); }
+inline float cell_coord(const Dual& p) { return static_cast<float>(p.v); }
 using std::exp;
 using std::floor;
 using std::sqrt;
@@ -163,11 +169,12 @@ static inline u32 linear_cell(long long cx, long long cy, long long cz, const Gr
 
 // hash_cell (core/src/cell_grid.cu:10-22); `inv` is the host reciprocal
 // 1.0f / cell_length computed in CellGrid::build (core/src/cell_grid.cu:81).
+// The arithmetic is float in every instance (cell_coord).
 template <class R>
-static inline u32 hash_cell(const V3<R>& p, const Grid& g, R inv) {
-    const long long cx = f2i_sat(floor((p.x - R(g.origin[0])) * inv));
-    const long long cy = f2i_sat(floor((p.y - R(g.origin[1])) * inv));
-    const long long cz = f2i_sat(floor((p.z - R(g.origin[2])) * inv));
+static inline u32 hash_cell(const V3<R>& p, const Grid& g, float inv) {
+    const long long cx = f2i_sat(std::floor((cell_coord(p.x) - g.origin[0]) * inv));
+    const long long cy = f2i_sat(std::floor((cell_coord(p.y) - g.origin[1]) * inv));
+    const long long cz = f2i_sat(std::floor((cell_coord(p.z) - g.origin[2]) * inv));
     if (cx < 0 || cx >= g.dims[0] || cy < 0 || cy >= g.dims[1] || cz < 0 || cz >= g.dims[2])
         return g.total;
     return linear_cell(cx, cy, cz, g);
@@ -194,7 +201,7 @@ static void build_grid(const V3<R>* pos, std::size_t n, const Grid& g, GridArray
         if (out.cell_start.size() != std::size_t(g.total) + 1) out.cell_start.assign(std::size_t(g.total) + 1, 0u);
         return;
     }
-    const R inv = R(1) / R(g.cell_length);
+    const float inv = 1.0f / g.cell_length;
     out.keys.resize(n);
 #pragma omp parallel for schedule(static)
     for (long long i = 0; i < (long long)n; ++i) out.keys[i] = hash_cell(pos[i], g, inv);
@@ -216,11 +223,11 @@ static void build_grid(const V3<R>* pos, std::size_t n, const Grid& g, GridArray
 // cell of p (centred with the device reciprocal), dz outer, dx inner, bounds-
 // checked, iterating sorted slots [cell_start[c], cell_start[c+1]).
 template <class R, class F>
-static inline void for_neighbors(const V3<R>& p, const Grid& g, R inv_stencil,
+static inline void for_neighbors(const V3<R>& p, const Grid& g, float inv_stencil,
                                  const GridArrays& ga, F&& f) {
-    const long long cx = f2i_sat(floor((p.x - R(g.origin[0])) * inv_stencil));
-    const long long cy = f2i_sat(floor((p.y - R(g.origin[1])) * inv_stencil));
-    const long long cz = f2i_sat(floor((p.z - R(g.origin[2])) * inv_stencil));
+    const long long cx = f2i_sat(std::floor((cell_coord(p.x) - g.origin[0]) * inv_stencil));
+    const long long cy = f2i_sat(std::floor((cell_coord(p.y) - g.origin[1]) * inv_stencil));
+    const long long cz = f2i_sat(std::floor((cell_coord(p.z) - g.origin[2]) * inv_stencil));
     for (int dz = -1; dz <= 1; ++dz)
         for (int dy = -1; dy <= 1; ++dy)
             for (int dx = -1; dx <= 1; ++dx) {
@@ -272,7 +279,7 @@ template <class R>
 struct Solver {
     Config cfg;
     Grid grid;
-    R inv_stencil;
+    float inv_stencil;
     R mass;
     R l;
     std::vector<V3<R>> x, v, xb;
@@ -290,11 +297,10 @@ struct Solver {
         grid = make_grid(c);
         xsph = R(c.viscosity);
         l = R(c.smoothing_length);
-        // The stencil reciprocal: the device value when given (the FP32 instance
-        // must match the device's stencil centring bit for bit), else IEEE.
-        inv_stencil = (c.stencil_inv_cell != 0.0f && sizeof(R) == sizeof(float))
-                          ? R(c.stencil_inv_cell)
-                          : R(1) / R(c.smoothing_length);
+        // The stencil reciprocal: the device value when given (every instance
+        // centres its stencil with the device's float arithmetic), else the
+        // IEEE float reciprocal.
+        inv_stencil = c.stencil_inv_cell != 0.0f ? c.stencil_inv_cell : 1.0f / c.smoothing_length;
         // mass = rho0 * (2r)^3 (dfsph.cu:76-78), evaluated in float as there.
         const float spacing = 2.0f * c.particle_radius;
         const float v0 = spacing * spacing * spacing;

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <memory>
 #include <vector>
 
@@ -60,6 +61,61 @@ TEST_CASE("ParticleStore: host round trips") {
     WATER_CUDA_CHECK(cudaMemcpy(store.attribute_data(h), t.data(), 32, cudaMemcpyHostToDevice));
     WATER_CUDA_CHECK(cudaMemcpy(tb.data(), store.attribute_data(h), 32, cudaMemcpyDeviceToHost));
     CHECK(t == tb);
+}
+
+TEST_CASE("ParticleStore: attributes are zero-filled, disjoint and keep their address") {
+    ParticleStore store(1000);
+    Vec3f* pos = store.positions();
+    std::vector<AttribHandle<float>> hs;
+    const char* names[] = {"a", "b", "c", "d", "e", "f", "g"};  // more than the first arena block holds
+    for (const char* n : names) hs.push_back(store.register_attribute<float>(n, AttribType::F32));
+    auto u = store.register_attribute<unsigned>("flags", AttribType::U32);
+    CHECK(store.positions() == pos);  // no attribute moved
+    std::vector<const unsigned char*> lo, hi;
+    for (auto h : hs) {
+        lo.push_back(reinterpret_cast<const unsigned char*>(store.attribute_data(h)));
+        hi.push_back(lo.back() + 1000 * sizeof(float));
+        CHECK(reinterpret_cast<std::uintptr_t>(lo.back()) % 256 == 0);
+    }
+    lo.push_back(reinterpret_cast<const unsigned char*>(store.positions()));
+    hi.push_back(lo.back() + 1000 * sizeof(Vec3f));
+    lo.push_back(reinterpret_cast<const unsigned char*>(store.velocities()));
+    hi.push_back(lo.back() + 1000 * sizeof(Vec3f));
+    lo.push_back(reinterpret_cast<const unsigned char*>(store.attribute_data(u)));
+    hi.push_back(lo.back() + 1000 * sizeof(unsigned));
+    for (std::size_t a = 0; a < lo.size(); ++a)
+        for (std::size_t b = a + 1; b < lo.size(); ++b) CHECK(hi[a] <= lo[b] || hi[b] <= lo[a]);
+    WATER_CUDA_CHECK(cudaStreamSynchronize(store.stream()));
+    std::vector<float> back(1000, 1.0f);
+    WATER_CUDA_CHECK(cudaMemcpy(back.data(), store.attribute_data(hs.back()), 4000, cudaMemcpyDeviceToHost));
+    CHECK(std::all_of(back.begin(), back.end(), [](float v) { return v == 0.0f; }));
+}
+
+TEST_CASE("ParticleStore: a handle that names no attribute throws out_of_range") {
+    ParticleStore store(16);
+    AttribHandle<float> none;
+    CHECK(!none.valid());
+    CHECK_THROWS_AS(store.attribute_data(none), std::out_of_range);
+    CHECK_THROWS_AS(store.attribute_data(AttribHandle<float>(99)), std::out_of_range);
+}
+
+TEST_CASE("DeviceBuffer: move leaves the source empty; copies round trip") {
+    DeviceBuffer<int> a(64);
+    std::vector<int> in(64), out(64, -1);
+    for (int i = 0; i < 64; ++i) in[i] = i * 3;
+    a.copy_from_host(in.data(), 64);
+    DeviceBuffer<int> b(std::move(a));
+    CHECK(a.empty() && a.data() == nullptr && b.size() == 64);
+    DeviceBuffer<int> c;
+    c = std::move(b);
+    CHECK(b.empty() && c.size() == 64);
+    c.copy_to_host(out.data(), 64);
+    WATER_CUDA_CHECK(cudaStreamSynchronize(c.stream()));
+    CHECK(in == out);
+    c.fill_zero();
+    c.copy_to_host(out.data(), 64);
+    WATER_CUDA_CHECK(cudaStreamSynchronize(c.stream()));
+    CHECK(std::all_of(out.begin(), out.end(), [](int v) { return v == 0; }));
 }
 
 TEST_CASE("CellGrid: 8 grid-aligned points map to 8 distinct cells") {

@@ -37,3 +37,43 @@ def test_reference_arm_line_has_the_contract_keys():
     assert line["config"]["workload"] == "puddle_4913"
     # other ranks print nothing and do no work
     assert bench.reference_arm(args, rank=1, world=2) is None
+
+
+def test_reference_arm_never_loads_the_library():
+    """The reference arm times the oracle alone: its scene (walls sampled by
+    the oracle) and its configuration are built without libdfsph_gb300.so,
+    which must not even be mapped into the process."""
+    import os
+    import subprocess
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import argparse, json, bench\n"
+            "a = argparse.Namespace(workload='puddle', steps=1, warmup=3, gpus=1, impl='reference')\n"
+            "line = bench.reference_arm(a, rank=0, world=1)\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print(json.dumps({'lib': 'libdfsph_gb300' in maps, 'oracle': 'liboracle' in maps,\n"
+            "                  'value': line['value'], 'nb': line['config']['boundary_particles']}))\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    import json
+
+    out = json.loads(r.stdout.strip().splitlines()[-1])
+    assert out["oracle"] and not out["lib"]
+    assert out["value"] > 0 and out["nb"] == 46818
+
+
+def test_reference_arm_scene_is_the_benchmark_scene():
+    """The oracle's wall sampler gives the library's walls bit for bit, so the
+    arm steps the same input as the library's arm."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    a = bench.make_scene("puddle")
+    b = bench.make_scene("puddle", sampler=O.sample_aabb_boundary)
+    assert np.array_equal(a.boundary, b.boundary) and np.array_equal(a.fluid, b.fluid)
+    c = bench.oracle_config(b)
+    d = O.config_from(a.config())
+    for name, _ in O.OracleConfig._fields_:
+        x, y = getattr(c, name), getattr(d, name)
+        assert (list(x) == list(y)) if hasattr(x, "__len__") else x == y, name

@@ -130,3 +130,49 @@ def test_cooperative_solve_fixed_iterations():
     assert it0 == it1 == [(2, 4)] * 10
     assert np.array_equal(x0, x1) and np.array_equal(v0, v1) and np.array_equal(r0, r1)
     assert l0 < l1
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_grid_barrier_wait_runs_out_and_reports_a_timeout(graph):
+    """The cooperative solve's grid barrier waits a bounded time. With the test
+    hook the barrier waits for two blocks that never arrive, so every wait
+    runs out after the limit (20 ms here): the kernel returns, the next
+    synchronising call reports DFSPH_ERR_DEVICE_TIMEOUT and the context keeps
+    working once a valid state is set again. No fault, trap or endless wait."""
+    import time
+
+    sc = scenes.puddle()
+    sc.max_divergence_iters, sc.eta_divergence = 4, 0.0
+    sc.max_density_iters, sc.eta_density = 4, 0.0
+    s = _solver(sc, graph=graph)
+    ref = _solver(sc, graph=graph)
+    s.set_wait_limit(0.02)
+    s.test_stall_waits(2)
+    t0 = time.perf_counter()
+    s.step(sc.dt)
+    with pytest.raises(_lib.DfsphError) as e:
+        s.synchronize()
+    waited = time.perf_counter() - t0
+    assert e.value.status == _lib.ERR_DEVICE_TIMEOUT
+    assert waited < 5.0  # two solves, each gives up after about 20 ms
+    # the word was cleared: the next call is clean
+    s.synchronize()
+    # back to normal waits: the same steps as an untouched context, bit for bit
+    s.test_stall_waits(0)
+    s.set_wait_limit(1.0)
+    s.set_fluid(sc.fluid, sc.velocity)
+    for _ in range(3):
+        s.step(sc.dt)
+        ref.step(sc.dt)
+    s.synchronize()
+    assert np.array_equal(s.positions(), ref.positions())
+    assert np.array_equal(s.velocities(), ref.velocities())
+    s.close()
+    ref.close()
+
+
+def test_wait_limit_rejects_zero():
+    sc = scenes.falling_block((4, 4, 4))
+    s = _solver(sc)
+    with pytest.raises(_lib.DfsphError):
+        s.set_wait_limit(0.0)

@@ -5,9 +5,9 @@ substep, until the frame's remaining time is <= 1e-6 or 64 substeps.
 The device path (use_cuda_graph = 1, fixed iterations) chooses each substep in
 a one-thread kernel from the max |v| the integrator left on the device and
 repeats the substep with a CUDA graph WHILE node; the host path reads max |v|
-back before every substep. With damping 0 (e^0 = 1 on both sides) the two must
-agree bit for bit; with damping the device evaluates e^{-d dt} itself, so
-positions agree to rounding.
+back before every substep. Both paths take e^{-d dt} from the same device
+function (the reference's fast-math expf, dfsph_kernels.cu:347-355), so the two
+agree bit for bit with and without damping, fixed or adaptive iterations.
 """
 import numpy as np
 import pytest
@@ -53,7 +53,9 @@ def test_device_frames_with_damping(block):
     sd = dev.step_frames(3)
     sh = host.step_frames(3)
     assert list(sd) == list(sh)
-    assert np.abs(dev.positions() - host.positions()).max() < 1e-5
+    assert np.array_equal(dev.positions(), host.positions())
+    assert np.array_equal(dev.velocities(), host.velocities())
+    assert dev.max_velocity() == host.max_velocity()
 
 
 def test_frames_continue_across_calls_and_respect_the_cap(block):
@@ -115,10 +117,12 @@ def test_adaptive_solves_in_graphs_match_the_host_loop():
     assert np.array_equal(dev.velocities(), host.velocities())
 
 
-def test_adaptive_device_frames_match_the_host_loop():
-    dev, host = _adaptive(True, 0.0), _adaptive(False, 0.0)
+@pytest.mark.parametrize("damping", [0.0, 0.5])
+def test_adaptive_device_frames_match_the_host_loop(damping):
+    dev, host = _adaptive(True, damping), _adaptive(False, damping)
     sd = dev.step_frames(3)
     sh = host.step_frames(3)
     assert dev.frames_on_device() and not host.frames_on_device()
     assert list(sd) == list(sh)
     assert np.array_equal(dev.positions(), host.positions())
+    assert np.array_equal(dev.velocities(), host.velocities())

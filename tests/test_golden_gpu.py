@@ -1,10 +1,13 @@
 """This project's CUDA step against the reference goldens (tests/golden/),
 through the C ABI: structure bit-exact per step, fields with the tolerances of
-tests/test_golden.py."""
+tests/test_golden.py, and the pressure fields of the last Jacobi iteration
+(kappa, rho*) with the tolerances of tests/tolerances.py: rho* within 2e-5 of
+rho0, as the density (the oracle meets the goldens to 1e-6)."""
 import numpy as np
 import pytest
 
 from test_golden import GOLDEN, load_case
+from tolerances import assert_pressure_fields_close
 from water_simulation_gb300 import _lib
 from water_simulation_gb300.solver import Solver
 
@@ -35,6 +38,8 @@ def test_cuda_step_matches_reference_goldens(path):
         assert np.abs(s.field(_lib.FIELD_BOUNDARY_MASS) - mb).max() / mb.max() < 1e-5
     s.set_fluid(d["fluid"], d["velocity0"])
     vtol = 2e-3 if float(d["cfg_viscosity"]) > 0 else 5e-4
+    ptol = 2e-5
+    worst = [0.0, 0.0]
     for k in range(d["position"].shape[0]):
         s.step(float(d["dt"]))
         assert np.array_equal(s.field(_lib.FIELD_CELL_KEY), d["cell_key"][k]), k
@@ -44,3 +49,7 @@ def test_cuda_step_matches_reference_goldens(path):
         assert np.abs(s.field(_lib.FIELD_DENSITY) - d["density"][k]).max() / 1000.0 < 2e-5, k
         assert np.abs(s.positions() - d["position"][k]).max() < 2e-6, k
         assert np.abs(s.velocities() - d["velocity"][k]).max() < vtol, k
+        e = assert_pressure_fields_close(s.field(_lib.FIELD_KAPPA), s.field(_lib.FIELD_DENSITY_ADV), d["kappa"][k],
+                                         d["density_adv"][k], d["alpha"][k], float(d["dt"]), ptol, f"step {k}")
+        worst = [max(worst[0], e[0]), max(worst[1], e[1])]
+    print(f"{path.rsplit('/', 1)[-1]}: rho* {worst[0]:.2e}, kappa {worst[1]:.2e} (of rho0, alpha rho0 / dt^2)")

@@ -13,6 +13,7 @@ import pytest
 
 from oracle import oracle as O
 from oracle import reference as R
+from tolerances import assert_pressure_fields_close
 from water_simulation_gb300 import _lib, scenes
 from water_simulation_gb300.solver import solver_for
 
@@ -61,6 +62,9 @@ def test_reference_structure_and_fields_one_step(dims, seed, visc):
     assert np.abs(gpu.velocities() - v_ref).max() < 2e-4
     assert gpu.max_velocity() == pytest.approx(ref.max_velocity(), rel=1e-4)
     assert ref.last_density_iters() == gpu.last_density_iters() == sc.max_density_iters
+    # the last Jacobi iteration's kappa and rho* (dfsph_kernels.cu:226-231)
+    assert_pressure_fields_close(gpu.field(_lib.FIELD_KAPPA), gpu.field(_lib.FIELD_DENSITY_ADV), ref.field(4),
+                                 ref.field(5), a_ref, sc.dt, 2e-5)
 
 
 def test_reference_structure_every_step_20_steps():
@@ -139,3 +143,37 @@ def test_reference_dam_break_1m_one_step():
     ora.step(sc.dt)
     assert np.array_equal(ora.field(O.F_NBR_FLUID), gpu.field(_lib.FIELD_NBR_FLUID))
     assert np.array_equal(ora.field(O.F_NBR_BOUNDARY), gpu.field(_lib.FIELD_NBR_BOUNDARY))
+
+
+def test_reference_dam_break_128k_every_step_50_steps():
+    """The dam-break configuration at 128,000 particles (193,458 wall
+    particles, 4 fixed density iterations, no divergence solver: the
+    reference's step), 50 steps. Before every step the GPU state is handed to
+    a fresh run of the reference's own kernels, and both take the step: cell
+    keys, permutation and cell_start bit for bit; density, kappa and rho* within
+    2e-5 of rho0 (kappa times alpha / dt^2), positions within 2e-6 m, velocities
+    within 2e-3 m/s (the reference's XSPH races), every step."""
+    sc = scenes.dam_break(scale=1, reference_mode=True)
+    gpu = solver_for(sc, diagnostics=True)
+    inv = gpu.scalar(_lib.SCALAR_STENCIL_INV_CELL)
+    ocfg = O.config_from(sc.config(), stencil_inv_cell=inv)
+    worst = np.zeros(5)
+    for k in range(50):
+        x, v = gpu.positions(), gpu.velocities()
+        ref = R.ReferenceRun(ocfg, x, v, sc.boundary)
+        ref.step(sc.dt)
+        gpu.step(sc.dt)
+        for fid_ref, fid_gpu in ((6, _lib.FIELD_CELL_KEY), (7, _lib.FIELD_SORTED_INDEX), (8, _lib.FIELD_CELL_START)):
+            assert np.array_equal(ref.field(fid_ref), gpu.field(fid_gpu)), (k, fid_gpu)
+        assert ref.last_density_iters() == gpu.last_density_iters() == 4
+        e_rho = np.abs(gpu.field(_lib.FIELD_DENSITY) - ref.field(2).astype(np.float64)).max() / 1000.0
+        e_x = np.abs(gpu.positions() - ref.field(0).astype(np.float64)).max()
+        e_v = np.abs(gpu.velocities() - ref.field(1).astype(np.float64)).max()
+        e_adv, e_kap = assert_pressure_fields_close(gpu.field(_lib.FIELD_KAPPA), gpu.field(_lib.FIELD_DENSITY_ADV),
+                                                    ref.field(4), ref.field(5), ref.field(3), sc.dt, 2e-5,
+                                                    f"step {k}")
+        assert e_rho < 2e-5 and e_x < 2e-6 and e_v < 2e-3, (k, e_rho, e_x, e_v)
+        worst = np.maximum(worst, [e_rho, e_adv, e_kap, e_x, e_v])
+        ref.close()
+    print("dam 128k, 50 re-fed steps against the reference's kernels: max |drho|/rho0 %.2e, rho* %.2e, "
+          "kappa %.2e, |dx| %.2e m, |dv| %.2e m/s" % tuple(worst))

@@ -43,6 +43,7 @@ FIELD_BOUNDARY_MASS = 11
 FIELD_KAPPA_V = 12
 FIELD_BOUNDARY_CELL_START = 13
 FIELD_BOUNDARY_SORTED_INDEX = 14
+FIELD_NBR_SIGNATURE = 15
 
 SCALAR_MAX_VELOCITY = 0
 SCALAR_PARTICLE_MASS = 1
@@ -59,6 +60,7 @@ SCALAR_FLAGS = 11
 SCALAR_ACTIVE_BOUNDARY = 12
 SCALAR_FRAME_GRAPH = 13
 SCALAR_BOUNDS_VIOLATIONS = 14
+SCALAR_COOP_SOLVES = 15
 
 KERNEL_GRID_COUNT = 0
 KERNEL_GRID_SCAN = 1
@@ -135,6 +137,8 @@ _SIGNATURES = [
     ("dfsph_get_field", ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_int]),
     ("dfsph_get_scalar", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("dfsph_synchronize", ctypes.c_int, [_P]),
+    ("dfsph_set_wait_limit", ctypes.c_int, [_P, ctypes.c_uint64]),
+    ("dfsph_test_stall_waits", ctypes.c_int, [_P, ctypes.c_uint32]),
     ("dfsph_profile_enable", ctypes.c_int, [_P, ctypes.c_uint32]),
     ("dfsph_profile_read", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_uint64)]),

@@ -286,10 +286,11 @@ static __device__ __forceinline__ void accumulate_partial(double partial, double
 template <class R>
 __global__ void __launch_bounds__(128) adjoint_xsph_kernel(
     int n, const R4<R>* __restrict__ tx, const R4<R>* __restrict__ vx, const R4<R>* __restrict__ vbar_in,
-    R4<R>* __restrict__ vbar_out, const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, R decay, R eps,
+    R4<R>* __restrict__ vbar_out, const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, R damping, R dt, R eps,
     R4<R>* __restrict__ xbar, R* __restrict__ rhobar, double* __restrict__ partials, u32* counter,
     double* eps_acc) {
     pdl_wait();
+    const R decay = damping_decay(damping, dt);  // the forward pass's factor
     __shared__ double sh[4];
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double part = 0;

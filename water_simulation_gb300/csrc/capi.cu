@@ -15,6 +15,8 @@ struct dfsph_ctx {
     dfsph_config cfg;
     int device = 0;
     std::string last_error;
+    unsigned long long wait_ns = 1000000000ull;  // bounded device waits (dfsph_set_wait_limit)
+    uint32_t wait_missing = 0;                   // dfsph_test_stall_waits
 };
 
 namespace {
@@ -228,6 +230,7 @@ int dfsph_get_field(dfsph_ctx* ctx, int field, void* dst, size_t dst_bytes, int 
     return guarded(ctx, [&] {
         cudaSetDevice(ctx->device);
         ctx->solver->get_field(field, dst, dst_bytes, mem);
+        ctx->solver->check_device_status();
     });
 }
 
@@ -252,6 +255,19 @@ int dfsph_profile_read(dfsph_ctx* ctx, int kernel_class, double* total_ms, uint6
         unsigned long long c = 0;
         ctx->solver->profile_read(kernel_class, total_ms, &c);
         *launches = c;
+    });
+}
+
+int dfsph_set_wait_limit(dfsph_ctx* ctx, uint64_t limit_ns) {
+    if (!ctx || limit_ns == 0) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] { ctx->solver->set_wait_limit(limit_ns, ctx->wait_missing); ctx->wait_ns = limit_ns; });
+}
+
+int dfsph_test_stall_waits(dfsph_ctx* ctx, uint32_t missing_blocks) {
+    if (!ctx) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        ctx->solver->set_wait_limit(ctx->wait_ns, missing_blocks);
+        ctx->wait_missing = missing_blocks;
     });
 }
 
@@ -322,6 +338,7 @@ int dfsph_step_frames(dfsph_ctx* ctx, const dfsph_frame_config* fc, uint32_t n_f
     return guarded(ctx, [&] {
         cudaSetDevice(ctx->device);
         ctx->solver->step_frames(*fc, n_frames, substeps);
+        ctx->solver->check_device_status();
     });
 }
 

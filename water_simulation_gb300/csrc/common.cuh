@@ -50,13 +50,18 @@ struct GridGeom {
 
 GridGeom make_grid_geom(const float dmin[3], const float dmax[3], float smoothing_length);
 
-// Device-side copy of the grid with the working real type.
+// Device-side copy of the grid. The cell arithmetic is FP32 in every build:
+// positions are rounded to float and binned and centred with the float
+// origin and the two float reciprocals, exactly as the reference's FP32
+// kernels do, so the FP64 build (the GPU oracle) visits the neighbour sets
+// the FP32 build visits for the same positions instead of switching a
+// particle's cell wherever the exact reciprocal 1/l differs from the float one.
 template <class R> struct GridDev {
-    R ox, oy, oz;
+    float ox, oy, oz;
     int nx, ny, nz;
     u32 total;
-    R inv_bin;
-    R inv_stencil;
+    float inv_bin;
+    float inv_stencil;
     // Scenes stepped together share the geometry; scene s owns the keys
     // [s * cells1, (s + 1) * cells1), cells1 = total + 1 (its out-of-grid key
     // last). slot_scene[s] is the scene of sorted slot s (null: one scene).
@@ -66,18 +71,13 @@ template <class R> struct GridDev {
 
 template <class R> inline GridDev<R> to_dev(const GridGeom& g) {
     GridDev<R> d;
-    d.ox = R(g.origin[0]); d.oy = R(g.origin[1]); d.oz = R(g.origin[2]);
+    d.ox = g.origin[0]; d.oy = g.origin[1]; d.oz = g.origin[2];
     d.nx = g.dims[0]; d.ny = g.dims[1]; d.nz = g.dims[2];
     d.total = g.total;
     d.cells1 = g.total + 1;
     d.slot_scene = nullptr;
-    if (sizeof(R) == sizeof(float)) {
-        d.inv_bin = R(g.inv_bin);
-        d.inv_stencil = R(g.inv_stencil);
-    } else {
-        d.inv_bin = R(1) / R(g.cell_length);
-        d.inv_stencil = R(1) / R(g.cell_length);
-    }
+    d.inv_bin = g.inv_bin;
+    d.inv_stencil = g.inv_stencil;
     return d;
 }
 
@@ -85,9 +85,6 @@ template <class R> inline GridDev<R> to_dev(const GridGeom& g) {
 // floor + float->int with the GPU's saturating conversion (NaN -> 0), as the
 // reference's static_cast<int>(floorf(...)) compiles on the device.
 __device__ __forceinline__ int floor_to_int(float v) { return static_cast<int>(floorf(v)); }
-__device__ __forceinline__ int floor_to_int(double v) {
-    return static_cast<int>(floor(v));
-}
 
 template <class R> __device__ __forceinline__ u32 scene_of(const GridDev<R>& g, int slot) {
     return g.slot_scene ? static_cast<u32>(g.slot_scene[slot]) : 0u;
@@ -96,9 +93,9 @@ template <class R> __device__ __forceinline__ u32 scene_of(const GridDev<R>& g, 
 // hash_cell (core/src/cell_grid.cu:10-22): x-major id, out of grid -> total.
 template <class R>
 __device__ __forceinline__ u32 cell_key(R px, R py, R pz, const GridDev<R>& g) {
-    const int cx = floor_to_int((px - g.ox) * g.inv_bin);
-    const int cy = floor_to_int((py - g.oy) * g.inv_bin);
-    const int cz = floor_to_int((pz - g.oz) * g.inv_bin);
+    const int cx = floor_to_int(__fmul_rn(__fsub_rn(float(px), g.ox), g.inv_bin));
+    const int cy = floor_to_int(__fmul_rn(__fsub_rn(float(py), g.oy), g.inv_bin));
+    const int cz = floor_to_int(__fmul_rn(__fsub_rn(float(pz), g.oz), g.inv_bin));
     if (cx < 0 || cx >= g.nx || cy < 0 || cy >= g.ny || cz < 0 || cz >= g.nz) return g.total;
     return (static_cast<u32>(cx) * static_cast<u32>(g.ny) + static_cast<u32>(cy)) *
                static_cast<u32>(g.nz) + static_cast<u32>(cz);
@@ -136,9 +133,9 @@ struct Centre { int x, y, z; };
 template <class R>
 __device__ __forceinline__ Centre stencil_centre(R px, R py, R pz, const GridDev<R>& g) {
     Centre c;
-    c.x = min(max(floor_to_int((px - g.ox) * g.inv_stencil), -2), g.nx + 1);
-    c.y = min(max(floor_to_int((py - g.oy) * g.inv_stencil), -2), g.ny + 1);
-    c.z = min(max(floor_to_int((pz - g.oz) * g.inv_stencil), -2), g.nz + 1);
+    c.x = min(max(floor_to_int(__fmul_rn(__fsub_rn(float(px), g.ox), g.inv_stencil)), -2), g.nx + 1);
+    c.y = min(max(floor_to_int(__fmul_rn(__fsub_rn(float(py), g.oy), g.inv_stencil)), -2), g.ny + 1);
+    c.z = min(max(floor_to_int(__fmul_rn(__fsub_rn(float(pz), g.oz), g.inv_stencil)), -2), g.nz + 1);
     return c;
 }
 

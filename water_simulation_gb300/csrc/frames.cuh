@@ -41,8 +41,8 @@ __device__ __forceinline__ float read_max_velocity(const IterCtl* ctl) {
 __device__ __forceinline__ void choose_substep(FrameCtl* f, float max_velocity) {
     const float dt = cfl_next_dt(*f, std_max(max_velocity, f->v_floor), f->remaining);
     f->dt = dt;
-    f->decay_f = expf(-f->damping * dt);
-    f->decay_d = exp(-double(f->damping) * double(dt));
+    f->decay_f = damping_decay(f->damping, dt);
+    f->decay_d = damping_decay(double(f->damping), double(dt));
 }
 
 static __global__ void frame_begin_kernel(FrameCtl* f, const IterCtl* ctl) {

@@ -12,8 +12,6 @@
 // consecutive 16-byte records that the warp's other particles share in L1.
 #pragma once
 
-#include <cooperative_groups.h>
-
 #include "common.cuh"
 
 namespace dfsph {
@@ -187,7 +185,61 @@ struct IterCtl {
                           // ints), spread over MAXV_SLOTS words; the max of the
                           // words is the step's max |v|
     u32 flags;            // bit0: non-finite seen; bit1: sentinel order not canonical
+    u32 bar_arrive;       // arrivals at the cooperative solve's grid barrier (cleared every step)
 };
+
+// ---------------------------------------------------------------------------
+// Bounded device waits. The only kernel that waits on other blocks is the
+// cooperative Jacobi solve (jacobi_solve_kernel), whose blocks are all
+// resident (cooperative launch). Its grid barrier gives up after a time limit
+// instead of spinning forever: the block that gives up sets the context's
+// device error word, every other waiting block sees the word and returns too,
+// and the host reports DFSPH_ERR_DEVICE_TIMEOUT at its next synchronising
+// call. No wait, fault or trap is left behind, so the context stays usable.
+// ---------------------------------------------------------------------------
+constexpr u32 DEV_ERR_BARRIER_TIMEOUT = 1u;
+
+struct WaitCfg {
+    unsigned long long limit_ns;  // give up a wait after this many nanoseconds
+    u32 missing;                  // blocks the barrier also waits for (0; tests set more to make every wait run out)
+    u32* err;                     // the context's device error word (sticky until the host clears it)
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Barrier number k (0, 1, 2, ...) of a cooperative launch, called by every
+// thread of every block. Thread 0 of a block releases the block's writes,
+// counts its arrival on a counter that only grows (barrier k is complete at
+// (k + 1) x (blocks + missing) arrivals) and polls the counter until then, the
+// time limit, or another block's give-up. Returns false, the same in every
+// thread of the block, when the wait gave up; the caller returns then.
+__device__ __forceinline__ bool grid_barrier(u32* arrive, u32 k, const WaitCfg& w, int* sh_ok) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        __threadfence();
+        atomicAdd(arrive, 1u);
+        const u32 target = (k + 1u) * (gridDim.x + w.missing);
+        const unsigned long long t0 = global_ns();
+        while (*((volatile const u32*)arrive) < target) {
+            if (*((volatile const u32*)w.err) & DEV_ERR_BARRIER_TIMEOUT) { ok = 0; break; }
+            if (global_ns() - t0 > w.limit_ns) {
+                atomicOr(w.err, DEV_ERR_BARRIER_TIMEOUT);
+                ok = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+        *sh_ok = ok;
+    }
+    __syncthreads();
+    return *sh_ok != 0;
+}
 
 template <int BLOCK>
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -222,13 +274,27 @@ __device__ __forceinline__ double block_sum_dyn(double v, double* sh) {
     return t;  // valid in thread 0
 }
 
+// The stop test of the reference's solvers (dfsph.cu:254-258,296-299): the
+// mean error below eta rho0. The reference sums in FP32 (CUB) and compares
+// in float; here the sum is FP64 and, in the FP32 builds, the mean is rounded
+// to float and compared with eta rho0 evaluated in float, as the reference
+// compares. The FP64 build compares in double.
+struct StopTest {
+    double n;    // particles in the mean
+    double thr;  // eta rho0 in the working type
+    int f32;     // 1: round the mean to float before the comparison
+};
+__device__ __forceinline__ bool below_threshold(double s, const StopTest& t) {
+    const double m = s / t.n;
+    return (t.f32 ? double(float(m)) : m) < t.thr;
+}
+
 // Thread 0 of every block calls this with the block's partial; the last block
 // to arrive sums all partials in block order, so the result does not depend on
 // block scheduling. Decides convergence: stop when (iter >= first_check) and
-// mean < threshold (dfsph.cu:254-258).
+// the mean passes the stop test.
 static __device__ __forceinline__ void finish_reduction(double partial, double* partials, IterCtl* ctl,
-                                                 u32 iter, u32 first_check, double inv_n,
-                                                 double threshold) {
+                                                 u32 iter, u32 first_check, StopTest rule) {
     partials[blockIdx.x] = partial;
     __threadfence();
     const u32 done = atomicAdd(&ctl->blocks_done, 1u);
@@ -238,7 +304,7 @@ static __device__ __forceinline__ void finish_reduction(double partial, double* 
         for (u32 b = 0; b < gridDim.x; ++b) s += *((volatile double*)&partials[b]);
         ctl->err_sum = s;
         ctl->blocks_done = 0;
-        if (iter >= first_check && s * inv_n < threshold) ctl->stop_iter = iter;
+        if (iter >= first_check && below_threshold(s, rule)) ctl->stop_iter = iter;
         if (!(s == s)) ctl->flags |= 1u;
     }
 }
@@ -266,9 +332,17 @@ struct FrameCtl {
 // Step size and the quantities derived from it, either fixed by the host
 // (dev == null) or read from the device frame control at kernel start.
 template <class R> struct StepDt {
-    R dt, decay, gx, gy, gz;   // gravity
+    R dt, damping, gx, gy, gz;   // gravity
     const FrameCtl* dev;
 };
+
+// e^{-damping dt} as the reference evaluates it: apply_gravity_kernel
+// (solvers/dfsph/src/dfsph_kernels.cu:347-355) computes expf(-damping * dt)
+// on the device, built with -use_fast_math, which makes expf the fast
+// exponential __expf. Host-stepped and device-stepped substeps both take it
+// from here, so they agree to the bit. The FP64 build uses exp.
+__device__ __forceinline__ float damping_decay(float damping, float dt) { return __expf(__fmul_rn(-damping, dt)); }
+__device__ __forceinline__ double damping_decay(double damping, double dt) { return exp(-damping * dt); }
 
 template <class R> __device__ __forceinline__ R mul_rn(R a, R b);
 template <> __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
@@ -278,7 +352,7 @@ template <class R> __device__ __forceinline__ R step_dt(const StepDt<R>& s) {
     return s.dev ? R(*((volatile const float*)&s.dev->dt)) : s.dt;
 }
 template <class R> __device__ __forceinline__ R step_decay(const StepDt<R>& s) {
-    if (!s.dev) return s.decay;
+    if (!s.dev) return damping_decay(s.damping, s.dt);
     return sizeof(R) == sizeof(float) ? R(*((volatile const float*)&s.dev->decay_f))
                                       : R(*((volatile const double*)&s.dev->decay_d));
 }
@@ -388,6 +462,7 @@ static __global__ void __launch_bounds__(1024) scan_tile_offsets(u32* __restrict
             ctl[k].iters = 0u;
             for (int w = 0; w < MAXV_SLOTS; ++w) ctl[k].maxv_slot[w] = 0u;
             ctl[k].flags = 0u;
+            ctl[k].bar_arrive = 0u;
         }
     }
 }
@@ -748,11 +823,21 @@ struct BoundaryDev {
 // alpha = rho / (|sum m gradW|^2 + sum |m gradW|^2). KAHAN compensates the
 // density sums.
 // ---------------------------------------------------------------------------
+// A 32-bit integer mix (the "lowbias32" finaliser of C. Wellons' hash
+// prospector): the candidate-set signature adds the mixed ids of a
+// particle's candidates, so two builds that visit the same set agree.
+__device__ __forceinline__ u32 mix32(u32 x) {
+    x ^= x >> 16; x *= 0x7feb352du;
+    x ^= x >> 15; x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+
 template <class R, bool KAHAN, bool DIAG, int LB>
 __global__ void __launch_bounds__(LB) density_alpha_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, R* __restrict__ alpha,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, u32* __restrict__ nbr_f,
-    u32* __restrict__ nbr_b, const u32* __restrict__ id, Tape1<R> tp) {
+    u32* __restrict__ nbr_b, u32* __restrict__ nbr_sig, const u32* __restrict__ id, Tape1<R> tp) {
     pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -760,9 +845,12 @@ __global__ void __launch_bounds__(LB) density_alpha_kernel(
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
     R ws = 0, wc = 0;
     R gx = 0, gy = 0, gz = 0, gq = 0;
-    u32 cf = 0, cb = 0;
+    u32 cf = 0, cb = 0, sig = 0;
     for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
-        if (DIAG) cf += e - b;
+        if (DIAG) {
+            cf += e - b;
+            for (u32 j = b; j < e; ++j) sig += mix32(__ldg(id + j));
+        }
 #pragma unroll 2
         for (u32 j = b; j < e; ++j) {
             const R4<R> pj = ld(xk + j);
@@ -815,12 +903,18 @@ __global__ void __launch_bounds__(LB) density_alpha_kernel(
     } else if (DIAG && bd.has) {
         for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) { cb += e - b; });
     }
+    if (DIAG && bd.has) {
+        // wall candidates by their sorted slot (the wall order is fixed)
+        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+            for (u32 j = b; j < e; ++j) sig += mix32(j ^ 0x80000000u);
+        });
+    }
     const R denom = gx * gx + gy * gy + gz * gz + gq;
     R4<R> v = vr[i];
     v.w = rho;
     vr[i] = v;
     alpha[i] = denom > R(1e-9) ? rho / denom : R(0);
-    if (DIAG) { nbr_f[i] = cf; nbr_b[i] = cb; }
+    if (DIAG) { nbr_f[i] = cf; nbr_b[i] = cb; nbr_sig[i] = sig; }
     if (tp.x) {
         tp.x[i] = {pi.x, pi.y, pi.z, rho};
         tp.g[i] = {gx, gy, gz, denom};
@@ -943,8 +1037,8 @@ __global__ void __launch_bounds__(LB) pressure_rate_kernel(
     int n, const R4<R>* __restrict__ xk_in, R4<R>* __restrict__ xk_out,
     const R4<R>* __restrict__ vr, const R* __restrict__ alpha, R* __restrict__ rho_adv,
     R* __restrict__ kap, const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd,
-    StepDt<R> sd, double* __restrict__ partials, IterCtl* ctl, u32 iter, u32 first_check, double inv_n,
-    double threshold, R4<R>* __restrict__ tape_v, const u32* dev_iter) {
+    StepDt<R> sd, double* __restrict__ partials, IterCtl* ctl, u32 iter, u32 first_check, StopTest rule,
+    R4<R>* __restrict__ tape_v, const u32* dev_iter) {
     pdl_wait();
     __shared__ double sh[LB / 32];
     // Inside a device-resident loop (DEVLOOP) the iteration comes from the
@@ -966,7 +1060,7 @@ __global__ void __launch_bounds__(LB) pressure_rate_kernel(
         err = rate_particle<R, DIVERGENCE>(i, xk_in, xk_out, vr, alpha, rho_adv, kap, cs, g, p, bd, dt, tape_v);
     if (REDUCE) {
         const double t = block_sum_dyn(err, sh);
-        if (threadIdx.x == 0) finish_reduction(t, partials, ctl, iter, first_check, inv_n, threshold);
+        if (threadIdx.x == 0) finish_reduction(t, partials, ctl, iter, first_check, rule);
     }
 }
 
@@ -1198,12 +1292,10 @@ template <class R, bool DIV, int P>
 __global__ void __launch_bounds__(4 * P + 32) jacobi_solve_kernel(
     int n, R4<R>* xa, R4<R>* xb, R4<R>* vr, const R* __restrict__ alpha, R* rho_adv, R* kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, double* wsums,
-    IterCtl* ctl, u32 max_iters, u32 first_check, double inv_n, double threshold, u32 stage_cap,
-    u32 wall_cap, u32 pass_block) {
+    IterCtl* ctl, u32 max_iters, u32 first_check, StopTest rule, u32 stage_cap,
+    u32 wall_cap, u32 pass_block, WaitCfg wait) {
     static_assert(P % 32 == 0, "whole warps of particles");
     constexpr int W = 4 * P;  // particle lanes
-    namespace cg = cooperative_groups;
-    cg::grid_group grid = cg::this_grid();
     extern __shared__ __align__(16) unsigned char jacobi_stage[];
     R4<R>* sx = reinterpret_cast<R4<R>*>(jacobi_stage);
     R4<R>* sv = sx + stage_cap;
@@ -1215,6 +1307,8 @@ __global__ void __launch_bounds__(4 * P + 32) jacobi_solve_kernel(
     __shared__ u32 run_b[9 * P], run_e[9 * P];
     __shared__ u32 wrun_b[9 * P], wrun_e[9 * P];
     __shared__ u32 wspan_lo, wspan_hi;
+    __shared__ int bar_ok;
+    u32 bar_k = 0;  // grid barriers passed
     // threads W .. W + 31: the decision warp
     const bool worker = threadIdx.x < W;
     // a barrier of the particle lanes alone (named barrier 1)
@@ -1337,7 +1431,7 @@ __global__ void __launch_bounds__(4 * P + 32) jacobi_solve_kernel(
                 if ((threadIdx.x & 31) == 0 && warp < n_warps) wsums[warp] = e;
             }
         }
-        grid.sync();
+        if (!grid_barrier(&ctl->bar_arrive, bar_k++, wait, &bar_ok)) return;
         if (!worker) {
             // the decision: the per-pass partials, each from its warps' sums
             // in warp order (warps past the last particle add +0 there), then
@@ -1353,7 +1447,7 @@ __global__ void __launch_bounds__(4 * P + 32) jacobi_solve_kernel(
             if (lane == 0) {
                 double s = 0;
                 for (u32 b = 0; b < n_pass; ++b) s += part[b];
-                const bool done = it >= first_check && s * inv_n < threshold;
+                const bool done = it >= first_check && below_threshold(s, rule);
                 stop = done ? 1 : 0;
                 if (blockIdx.x == 0) {
                     ctl->err_sum = s;
@@ -1373,7 +1467,8 @@ __global__ void __launch_bounds__(4 * P + 32) jacobi_solve_kernel(
             }
         }
         ++it;
-        grid.sync();  // velocities complete before the next rate pass; stop visible
+        // velocities complete before the next rate pass; stop visible
+        if (!grid_barrier(&ctl->bar_arrive, bar_k++, wait, &bar_ok)) return;
         if (stop != 0) break;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) ctl->iters = it;

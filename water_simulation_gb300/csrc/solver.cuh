@@ -106,7 +106,7 @@ public:
         rho_dot_.alloc(cap_);
         key_.alloc(cap_); rank_.alloc(cap_); tmp_src_.alloc(cap_); tmp_id_.alloc(cap_);
         key_sorted_.alloc(cap_);
-        if (cfg_.record_diagnostics) { nbr_f_.alloc(cap_); nbr_b_.alloc(cap_); }
+        if (cfg_.record_diagnostics) { nbr_f_.alloc(cap_); nbr_b_.alloc(cap_); nbr_sig_.alloc(cap_); }
         count_.alloc(keys_);
         cell_start_.alloc(keys_ + 1);  // closing entry = n
         n_tiles_ = static_cast<u32>((keys_ + SCAN_TILE - 1) / SCAN_TILE);
@@ -115,6 +115,7 @@ public:
         // and the per-warp sums of the cooperative solve
         partials_.alloc(std::max<size_t>(1, (std::max(cap_, 1u) + 31) / 32));
         ctl_.alloc(3);
+        dev_err_.alloc(1);
         staging_.alloc(std::max<size_t>(size_t(std::max(cap_, bcap_)) * 6, 6));
         if (bcap_) {
             for (int k = 0; k < 2; ++k) { xb_[k].alloc(bcap_); bid_[k].alloc(bcap_); }
@@ -137,6 +138,7 @@ public:
         DFSPH_CUDA(cudaMemsetAsync(cell_start_.p, 0, (keys_ + 1) * sizeof(u32), stream_));
         DFSPH_CUDA(cudaMemsetAsync(bcs_.p, 0, (size_t(cells1_) + 1) * sizeof(u32), stream_));
         DFSPH_CUDA(cudaMemsetAsync(ctl_.p, 0, 3 * sizeof(IterCtl), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(dev_err_.p, 0, sizeof(u32), stream_));
         DFSPH_CUDA(cudaMemsetAsync(alpha_.p, 0, size_t(cap_) * sizeof(R), stream_));
         DFSPH_CUDA(cudaMemsetAsync(rho_adv_.p, 0, size_t(cap_) * sizeof(R), stream_));
         DFSPH_CUDA(cudaMemsetAsync(kap_.p, 0, size_t(cap_) * sizeof(R), stream_));
@@ -144,6 +146,7 @@ public:
         if (cfg_.record_diagnostics) {
             DFSPH_CUDA(cudaMemsetAsync(nbr_f_.p, 0, size_t(cap_) * sizeof(u32), stream_));
             DFSPH_CUDA(cudaMemsetAsync(nbr_b_.p, 0, size_t(cap_) * sizeof(u32), stream_));
+            DFSPH_CUDA(cudaMemsetAsync(nbr_sig_.p, 0, size_t(cap_) * sizeof(u32), stream_));
         }
         DFSPH_CUDA(cudaMallocHost(reinterpret_cast<void**>(&host_ctl_), 3 * sizeof(IterCtl)));
         DFSPH_CUDA(cudaStreamSynchronize(stream_));
@@ -362,7 +365,7 @@ public:
             case DFSPH_FIELD_DENSITY: case DFSPH_FIELD_ALPHA: case DFSPH_FIELD_KAPPA:
             case DFSPH_FIELD_DENSITY_ADV: case DFSPH_FIELD_KAPPA_V: need = n * sizeof(float); break;
             case DFSPH_FIELD_CELL_KEY: case DFSPH_FIELD_SORTED_INDEX: case DFSPH_FIELD_NBR_FLUID:
-            case DFSPH_FIELD_NBR_BOUNDARY: need = n * sizeof(u32); break;
+            case DFSPH_FIELD_NBR_BOUNDARY: case DFSPH_FIELD_NBR_SIGNATURE: need = n * sizeof(u32); break;
             case DFSPH_FIELD_CELL_START: need = keys_ * sizeof(u32); break;
             case DFSPH_FIELD_BOUNDARY_CELL_START: need = size_t(cells1_) * sizeof(u32); break;
             case DFSPH_FIELD_BOUNDARY_MASS: need = size_t(nb_) * sizeof(float); break;
@@ -370,7 +373,8 @@ public:
             default: throw Error(DFSPH_ERR_INVALID_ARGUMENT, "unknown field " + std::to_string(field));
         }
         if (bytes < need) throw Error(DFSPH_ERR_INVALID_ARGUMENT, "destination too small for field");
-        if ((field == DFSPH_FIELD_NBR_FLUID || field == DFSPH_FIELD_NBR_BOUNDARY) && !cfg_.record_diagnostics)
+        if ((field == DFSPH_FIELD_NBR_FLUID || field == DFSPH_FIELD_NBR_BOUNDARY ||
+             field == DFSPH_FIELD_NBR_SIGNATURE) && !cfg_.record_diagnostics)
             throw Error(DFSPH_ERR_STATE, "neighbour counts need record_diagnostics = 1");
         if (need == 0) return;
         if (mem == DFSPH_MEM_HOST && export_mapped(field, dst)) return;
@@ -408,6 +412,8 @@ public:
                 launch(DFSPH_KERNEL_IO, unsort_kernel<u32, u32>, nb, 256, int(n), id, nbr_f_.p, (u32*)out); break;
             case DFSPH_FIELD_NBR_BOUNDARY:
                 launch(DFSPH_KERNEL_IO, unsort_kernel<u32, u32>, nb, 256, int(n), id, nbr_b_.p, (u32*)out); break;
+            case DFSPH_FIELD_NBR_SIGNATURE:
+                launch(DFSPH_KERNEL_IO, unsort_kernel<u32, u32>, nb, 256, int(n), id, nbr_sig_.p, (u32*)out); break;
             case DFSPH_FIELD_BOUNDARY_MASS:
                 launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, float>, blocks_for(nb_, 256), 256, int(nb_), bid_[0].p,
                        xb_[0].p, 3, (float*)out);
@@ -459,6 +465,7 @@ public:
             case DFSPH_SCALAR_KERNEL_LAUNCHES: return double(launches_);
             case DFSPH_SCALAR_ACTIVE_BOUNDARY: return double(active_boundary());
             case DFSPH_SCALAR_FRAME_GRAPH: return double(last_frame_graph_);
+            case DFSPH_SCALAR_COOP_SOLVES: return double(coop_launches_);
             case DFSPH_SCALAR_BOUNDS_VIOLATIONS: {
 #ifdef DFSPH_BOUNDS_CHECK
                 u32 v = 0;
@@ -493,7 +500,33 @@ public:
         }
     }
 
-    void synchronize() override { DFSPH_CUDA(cudaStreamSynchronize(stream_)); }
+    void synchronize() override {
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        check_device_status();
+    }
+
+    // The device error word is written only by the cooperative solve (its
+    // bounded grid barrier); until one was launched or captured there is
+    // nothing to read.
+    void check_device_status() override {
+        if (!coop_used_) return;
+        u32 w = 0;
+        DFSPH_CUDA(cudaMemcpyAsync(&w, dev_err_.p, sizeof(u32), cudaMemcpyDeviceToHost, stream_));
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        if (w == 0) return;
+        DFSPH_CUDA(cudaMemsetAsync(dev_err_.p, 0, sizeof(u32), stream_));
+        DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        throw Error(DFSPH_ERR_DEVICE_TIMEOUT,
+                    "a grid barrier of the cooperative Jacobi solve gave up after " +
+                        std::to_string(double(wait_limit_ns_) * 1e-6) +
+                        " ms; the state of that step is not valid (set it again to continue)");
+    }
+
+    void set_wait_limit(unsigned long long limit_ns, u32 missing_blocks) override {
+        wait_limit_ns_ = limit_ns;
+        wait_missing_ = missing_blocks;
+        drop_graph();  // captured launches carry the old limit
+    }
 
     void profile_enable(u32 mask) override {
         profile_mask_ = mask;
@@ -1137,9 +1170,9 @@ private:
             launch(DFSPH_KERNEL_ADJOINT, adjoint_rate_kernel<R>, b128, 128, n, (const V4*)xr_.p,
                    (const V4*)(t.v[1] + it * st), (const u32*)t.cs, g_, phys_, bd, vbar_[cur].p, xbar_.p);
         }
-        const R decay = std::exp(-R(cfg_.damping) * dt);
         launch(DFSPH_KERNEL_ADJOINT, adjoint_xsph_kernel<R>, b128, 128, n, (const V4*)t.x, (const V4*)t.vx,
-               (const V4*)vbar_[cur].p, vbar_[cur ^ 1].p, (const u32*)t.cs, g_, phys_, decay, R(ad_eps_), xbar_.p,
+               (const V4*)vbar_[cur].p, vbar_[cur ^ 1].p, (const u32*)t.cs, g_, phys_, R(cfg_.damping), dt,
+               R(ad_eps_), xbar_.p,
                rhobar_.p, eps_part_.p, eps_ctr_.p, eps_acc_.p);
         cur ^= 1;
         for (u32 it = cfg_.max_divergence_iters; it-- > 0;) {
@@ -1259,8 +1292,30 @@ private:
     // device dt; frame_control } -> frame_end. The substep is captured once;
     // steps leave the buffer parity unchanged, so every iteration replays the
     // same pointers. Rebuilt when the stream, the state or the parity changes.
+    // Before a capture: every cooperative solve that the captured steps would
+    // launch is launched once eagerly, with no iterations (it reads the state
+    // and writes only a scratch control block), so that the capture records
+    // only cooperative launches this device has accepted; a refused one makes
+    // the capture use the per-pass solve.
+    void verify_cooperative() {
+        if (!have_state_ || n_ == 0) return;
+        if (!probe_ctl_.p) {
+            probe_ctl_.alloc(1);
+            DFSPH_CUDA(cudaMemsetAsync(probe_ctl_.p, 0, sizeof(IterCtl), stream_));
+        }
+        StepDt<R> sd{};
+        sd.dt = R(1);
+        sd.dev = nullptr;
+        const StopTest none{double(n_), 0.0, 0};
+        if (cfg_.max_divergence_iters > 0 && coop_ok_[1] == 0)
+            solve_cooperative<true>(sd, 0, none, 0, probe_ctl_.p, kap_v_.p, rho_dot_.p, cell_start_.p, true);
+        if (cfg_.max_density_iters > 0 && coop_ok_[0] == 0)
+            solve_cooperative<false>(sd, 0, none, 1, probe_ctl_.p, kap_.p, rho_adv_.p, cell_start_.p, true);
+    }
+
     void ensure_frame_graph() {
         if (frame_exec_ && cx_ == fg_cx_ && cv_ == fg_cv_ && ci_ == fg_ci_) return;
+        verify_cooperative();
         if (frame_exec_) cudaGraphExecDestroy(frame_exec_);
         if (frame_graph_) cudaGraphDestroy(frame_graph_);
         frame_exec_ = nullptr;
@@ -1336,6 +1391,7 @@ private:
         // step would not, so the graph is only reused at its capture parity
         if (graph_exec_ && graph_dt_ == dt && cx_ == graph_cx_ && cv_ == graph_cv_ && ci_ == graph_ci_) return;
         drop_graph();
+        verify_cooperative();
         const int cx = cx_, cv = cv_, ci = ci_;
         const bool counted = counts_valid_, stepped = stepped_;
         // Capture on a private stream (the caller's may be the legacy default
@@ -1459,7 +1515,10 @@ private:
               const StepTape<R>* tp, FusedAdvect* fa = nullptr) {
         const int n = int(n_);
         const bool adaptive = eta > 0.0f;
-        const double thr = double(eta) * double(cfg_.rest_density);
+        // eta rho0 in the working type (dfsph.cu:255: cfg_.eta_density * cfg_.rest_density in f32)
+        const bool f32 = sizeof(R) == sizeof(float);
+        const StopTest thr{double(n), f32 ? double(eta * cfg_.rest_density)
+                                          : double(eta) * double(cfg_.rest_density), f32 ? 1 : 0};
         const u32 first_check = DIV ? 0u : 1u;  // density: from the 2nd iteration (dfsph.cu:255)
         if (!tp) {
             // small scenes: the whole solve in one cooperative launch (with
@@ -1481,11 +1540,11 @@ private:
             if (adaptive)
                 launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true, false, 128>, pressure_rate_kernel<R, DIV, true, false, 256>, n,
                        xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl,
-                       it, first_check, 1.0 / double(n), thr, tv, (const u32*)nullptr);
+                       it, first_check, thr, tv, (const u32*)nullptr);
             else
                 launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, false, false, 128>, pressure_rate_kernel<R, DIV, false, false, 256>, n,
                        xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl,
-                       it, first_check, 1.0 / double(n), thr, tv, (const u32*)nullptr);
+                       it, first_check, thr, tv, (const u32*)nullptr);
             if (!tp) cx_ ^= 1;
             // the last iteration of a fixed-count solve may carry the
             // integrator, when the other position buffer is the one the step
@@ -1538,10 +1597,19 @@ private:
     // they do not or when the passes are being timed one by one.
     // Like the graph-resident loop it leaves the step's positions in both
     // buffers and the iteration count in IterCtl::iters.
+    // With probe = true the launch runs no iteration (it only builds its run
+    // tables): verify_cooperative uses it to learn, outside any capture,
+    // whether the device accepts the launch.
     template <bool DIV>
-    bool solve_cooperative(const StepDt<R>& sd, u32 max_iters, double thr, u32 first_check, IterCtl* ctl,
-                           R* kap_out, R* adv_out, const u32* cs) {
-        if (max_iters == 0 || profile_mask_ != 0) return false;
+    bool solve_cooperative(const StepDt<R>& sd, u32 max_iters, const StopTest& thr, u32 first_check, IterCtl* ctl,
+                           R* kap_out, R* adv_out, const u32* cs, bool probe = false) {
+        if ((max_iters == 0 && !probe) || profile_mask_ != 0) return false;
+        int& accepted = coop_ok_[DIV ? 1 : 0];
+        // a capture records only launches that this device has accepted
+        // eagerly: a refusal inside a capture would fail the capture or, on a
+        // partitioned GPU, the graph's replays
+        if (capturing_ && accepted != 1) return false;
+        if (accepted < 0) return false;
         const int lb = bs_[DFSPH_KERNEL_PRESSURE_RATE];  // the per-pass reduction's block size
         if (lb != 128 && lb != 256) return false;
         const int n = int(n_);
@@ -1592,11 +1660,10 @@ private:
         lc.numAttrs = 1;
         V4* xa = xk_[cx_].p;
         V4* xb = xk_[cx_ ^ 1].p;
-        const double inv_n = 1.0 / double(n);
         auto go = [&](auto kernel) {
             return cudaLaunchKernelEx(&lc, kernel, n, xa, xb, vr_[cv_].p, (const R*)alpha_.p, adv_out, kap_out, cs,
-                                      g_, phys_, bdev(), sd, partials_.p, ctl, max_iters, first_check, inv_n, thr,
-                                      stage_cap, wall_cap, u32(lb));
+                                      g_, phys_, bdev(), sd, partials_.p, ctl, max_iters, first_check, thr,
+                                      stage_cap, wall_cap, u32(lb), WaitCfg{wait_limit_ns_, wait_missing_, dev_err_.p});
         };
         cudaError_t e;
         if (cb == 32) e = go(jacobi_solve_kernel<R, DIV, 32>);
@@ -1608,16 +1675,20 @@ private:
             // per-pass solve from now on
             cudaGetLastError();
             for (int k = 0; k < 4; ++k) coop_blocks_[DIV ? 1 : 0][k] = 0;
+            accepted = -1;
             return false;
         }
         DFSPH_CUDA(e);
+        if (!capturing_) accepted = 1;
+        coop_used_ = true;
+        if (!probe) ++coop_launches_;
         if (capturing_) ++graph_kernels_;
         else ++launches_;
         return true;
     }
 
     template <bool DIV>
-    u32 solve_on_device(const StepDt<R>& sd, u32 max_iters, double thr, u32 first_check, IterCtl* ctl, R* kap_out,
+    u32 solve_on_device(const StepDt<R>& sd, u32 max_iters, const StopTest& thr, u32 first_check, IterCtl* ctl, R* kap_out,
                         R* adv_out, const u32* cs) {
         if (max_iters == 0) return 0;
         const int n = int(n_);
@@ -1650,7 +1721,7 @@ private:
             const u32* dit = &ctl->iters;
             launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true, true, 128>, pressure_rate_kernel<R, DIV, true, true, 256>, n,
                    (const V4*)xa, xb, vr_[cv_].p, alpha_.p, adv_out, kap_out, cs, g_, phys_, bdev(), sd, partials_.p,
-                   ctl, 0u, first_check, 1.0 / double(n), thr, (V4*)nullptr, dit);
+                   ctl, 0u, first_check, thr, (V4*)nullptr, dit);
             launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R, true, 128>, pressure_apply_kernel<R, true, 256>, n, (const V4*)xb,
                    vr_[cv_].p, kap_out, cs, g_, phys_, bdev(), sd, (const IterCtl*)ctl, 0u, (const V4*)xa, dit);
             launch(DFSPH_KERNEL_OTHER, iteration_control_kernel, 1, 32, ctl, max_iters, h);
@@ -1676,7 +1747,7 @@ private:
         const int cx0 = cx_;
         StepDt<R> sd;
         sd.dt = dt;
-        sd.decay = std::exp(-R(cfg_.damping) * dt);
+        sd.damping = R(cfg_.damping);  // the kernels derive e^{-damping dt} (damping_decay)
         sd.gx = R(cfg_.gravity[0]);
         sd.gy = R(cfg_.gravity[1]);
         sd.gz = R(cfg_.gravity[2]);
@@ -1702,17 +1773,17 @@ private:
         if (cfg_.record_diagnostics) {
             if (kahan)
                 launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, true, 128>, density_alpha_kernel<R, true, true, 256>, n,
-                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, nbr_f_.p, nbr_b_.p, idn, t1);
+                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, nbr_f_.p, nbr_b_.p, nbr_sig_.p, idn, t1);
             else
                 launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, true, 128>, density_alpha_kernel<R, false, true, 256>, n,
-                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, nbr_f_.p, nbr_b_.p, idn, t1);
+                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, nbr_f_.p, nbr_b_.p, nbr_sig_.p, idn, t1);
         } else {
             if (kahan)
                 launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, false, 128>, density_alpha_kernel<R, true, false, 256>, n,
-                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr, idn, t1);
+                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr, (u32*)nullptr, idn, t1);
             else
                 launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, false, 128>, density_alpha_kernel<R, false, false, 256>, n,
-                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr, idn, t1);
+                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr, (u32*)nullptr, idn, t1);
         }
         // 3. divergence solve (the reference's plan; 0 iterations = the reference)
         last_divergence_launched_ = 0;
@@ -1784,13 +1855,18 @@ private:
     DevBuf<V4> xk_[2], vr_[2], xb_[2], bscratch_[2];
     DevBuf<u32> id_[2], bid_[2];
     DevBuf<R> alpha_, rho_adv_, kap_, kap_v_, rho_dot_, eps_scene_;
-    DevBuf<u32> key_, rank_, tmp_src_, tmp_id_, key_sorted_, nbr_f_, nbr_b_, maxv_scene_;
+    DevBuf<u32> key_, rank_, tmp_src_, tmp_id_, key_sorted_, nbr_f_, nbr_b_, nbr_sig_, maxv_scene_;
     DevBuf<unsigned short> slot_scene_;
     DevBuf<u32> bkey_, brank_, bkey_sorted_, btmp_src_, btmp_id_;
     DevBuf<u32> count_, cell_start_, tile_sums_, bcs_;
     DevBuf<unsigned char> bmask_;
     DevBuf<double> partials_;
     DevBuf<IterCtl> ctl_;
+    DevBuf<u32> dev_err_;  // device error word (DEV_ERR_*), sticky until check_device_status
+    unsigned long long wait_limit_ns_ = 1000000000ull;  // bounded device waits: 1 s
+    u32 wait_missing_ = 0;  // test hook: blocks the grid barrier waits for in vain
+    bool coop_used_ = false;
+    unsigned long long coop_launches_ = 0;  // cooperative solves launched or captured
     DevBuf<float> staging_;
     DevBuf<unsigned char> readback_;
     IterCtl* host_ctl_ = nullptr;
@@ -1827,6 +1903,10 @@ private:
     // blocks of jacobi_solve_kernel one launch may hold, [DIV][32, 64, 128,
     // 224 particles] (-1: not probed yet)
     int coop_blocks_[2][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}};
+    // [DIV]: 1 once a cooperative solve launched outside a capture, -1 once
+    // one was refused, 0 before either (captures need 1)
+    int coop_ok_[2] = {0, 0};
+    DevBuf<IterCtl> probe_ctl_;  // written by the no-iteration launches of verify_cooperative
     bool fuse_advect_ = true;  // last density iteration carries the integrator when it can
     DevBuf<V4> tune_ck_;
     DevBuf<IterCtl> tune_ctl_;

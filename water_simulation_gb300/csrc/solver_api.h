@@ -31,6 +31,10 @@ struct SolverBase {
     virtual void get_field(int field, void* dst, std::size_t bytes, int mem) = 0;
     virtual double get_scalar(int which) = 0;
     virtual void synchronize() = 0;
+    // Throws DFSPH_ERR_DEVICE_TIMEOUT (and clears the word) when a bounded
+    // device wait gave up since the last check; call after the stream synced.
+    virtual void check_device_status() = 0;
+    virtual void set_wait_limit(unsigned long long limit_ns, std::uint32_t missing_blocks) = 0;
     virtual void profile_enable(std::uint32_t mask) = 0;
     virtual void profile_read(int kclass, double* total_ms, unsigned long long* count) = 0;
     virtual void step_frames(const dfsph_frame_config& fc, std::uint32_t n_frames, std::uint32_t* substeps) = 0;

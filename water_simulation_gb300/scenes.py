@@ -128,26 +128,31 @@ class Scene:
         return c
 
 
-def puddle(seed: int = 1) -> Scene:
+def puddle(seed: int = 1, sampler=None) -> Scene:
     """Settled puddle: 17^3 particles, r = 0.01, corner (0.3, 0.5, 0.3), box [0,1]^3,
-    XSPH 0.01, dt 1e-3, divergence 0.1 % / density 0.01 % tolerances, <= 100 iterations."""
+    XSPH 0.01, dt 1e-3, divergence 0.1 % / density 0.01 % tolerances, <= 100 iterations.
+    `sampler(lo, hi, spacing, n_layers)` samples the walls (default: the
+    library's sample_aabb_boundary)."""
+    sampler = sampler or sample_aabb_boundary
     r = 0.01
     s = 2 * r
     fluid = lattice_block((0.3, 0.5, 0.3), (17, 17, 17), s, 0.05 * r, seed)
     lo, hi = (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)
     return Scene("puddle_4913", r, lo, hi, fluid, np.zeros_like(fluid),
-                 sample_aabb_boundary(lo, hi, s, 3), dt=1e-3, steps=1500, viscosity=0.01,
+                 sampler(lo, hi, s, 3), dt=1e-3, steps=1500, viscosity=0.01,
                  max_density_iters=100, max_divergence_iters=100, eta_density=1e-4,
                  eta_divergence=1e-3)
 
 
-def dam_break(scale: int = 1, reference_mode: bool = True) -> Scene:
+def dam_break(scale: int = 1, reference_mode: bool = True, sampler=None) -> Scene:
     """Dam break: a (40 x 80 x 40) * scale column at spacing 0.01 / scale against the
     x = 0 wall of a 1.6 x 1.0 x 0.6 m tank (scale 1: 128,000 particles, scale 2:
     1,024,000). The block starts 3 spacings inside the x = 0 wall and the floor
     (the wall layers occupy [0, 2s]), lattice points at lo + (i + 1/2) s, i.e. at
     cell centres; the column is centred in z. Fixed 4 density iterations and,
-    outside reference mode, 2 divergence iterations; dt = 5e-4 / scale."""
+    outside reference mode, 2 divergence iterations; dt = 5e-4 / scale.
+    `sampler` as for puddle()."""
+    sampler = sampler or sample_aabb_boundary
     r = 0.005 / scale
     s = 2 * r
     nx, ny, nz = 40 * scale, 80 * scale, 40 * scale
@@ -155,7 +160,7 @@ def dam_break(scale: int = 1, reference_mode: bool = True) -> Scene:
     fluid = lattice_block(lo, (nx, ny, nz), s, 0.05 * r, 2 if scale == 1 else 3)
     dlo, dhi = (0.0, 0.0, 0.0), (1.6, 1.0, 0.6)
     return Scene(f"dam_break_{nx * ny * nz}", r, dlo, dhi, fluid, np.zeros_like(fluid),
-                 sample_aabb_boundary(dlo, dhi, s, 3), dt=5e-4 / scale,
+                 sampler(dlo, dhi, s, 3), dt=5e-4 / scale,
                  steps=2000 if scale == 1 else 500, viscosity=0.01,
                  max_density_iters=4, max_divergence_iters=0 if reference_mode else 2)
 

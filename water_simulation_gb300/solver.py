@@ -25,6 +25,7 @@ _FIELD_DTYPE = {
     _lib.FIELD_SORTED_INDEX: (np.uint32, 1),
     _lib.FIELD_NBR_FLUID: (np.uint32, 1),
     _lib.FIELD_NBR_BOUNDARY: (np.uint32, 1),
+    _lib.FIELD_NBR_SIGNATURE: (np.uint32, 1),
 }
 
 
@@ -165,6 +166,16 @@ class Solver:
 
     def synchronize(self) -> None:
         self._check(self._lib.dfsph_synchronize(self._ctx))
+
+    def set_wait_limit(self, seconds: float) -> None:
+        """Time limit of every bounded device wait (the cooperative solve's
+        grid barrier); a wait that runs out makes the next synchronising call
+        raise DfsphError with ERR_DEVICE_TIMEOUT."""
+        self._check(self._lib.dfsph_set_wait_limit(self._ctx, int(seconds * 1e9)))
+
+    def test_stall_waits(self, missing_blocks: int) -> None:
+        """Test hook: the grid barrier waits for blocks that never arrive."""
+        self._check(self._lib.dfsph_test_stall_waits(self._ctx, missing_blocks))
 
     def set_stream(self, stream: int) -> None:
         self._check(self._lib.dfsph_set_stream(self._ctx, ctypes.c_void_p(stream)))
