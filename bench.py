@@ -61,12 +61,17 @@ FALLBACK_HBM_GBS = 6800.0
 
 # DRAM bytes (read + write) per fluid particle of one launch of each kernel
 # class, from `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum` on the
-# 1M dam break (profiles/dfsph_kernels_dam1m.md, one launch per kernel). The
-# traffic of a launch on another workload is scaled by its particle count.
+# 1M dam break (one launch per kernel). The traffic of a launch on another
+# workload is scaled by its particle count.
 NCU_TRAFFIC_PER_PARTICLE: dict = {
     "pressure_rate": 46.1, "pressure_apply": 40.2, "density_alpha": 25.0, "forces_xsph": 38.2,
     "advect": 37.3, "grid_reorder": 52.7, "grid_scatter": 17.6, "grid_count": 20.7,
 }
+
+
+# Warp instructions per fluid particle of one launch of each neighbour pass,
+# from `ncu --metrics smsp__inst_executed.sum` on the 1M dam break.
+NCU_WARP_INST_PER_PARTICLE: dict = {}
 
 
 def parse():
@@ -87,6 +92,9 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default 128-thread neighbour passes")
     ap.add_argument("--no-lbvh", action="store_true", help="skip the LBVH build/refit timing")
     ap.add_argument("--no-puddle", action="store_true", help="skip the adaptive-puddle leg")
+    ap.add_argument("--no-morton", action="store_true", help="skip the Morton slot-order comparison")
+    ap.add_argument("--slot-order", default="cell_key", choices=["cell_key", "morton"],
+                    help="slot order of the timed context (the reference's is cell_key)")
     return ap.parse_args()
 
 
@@ -119,6 +127,24 @@ def peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return FALLBACK_HBM_GBS, "fallback"
+
+
+def issue_roofline(kclass: str, n: int, avg_ms: float, clocks: dict, sms: int) -> dict | None:
+    """The roof these neighbour passes actually meet: warp instructions
+    issued per launch (ncu smsp__inst_executed.sum of one launch on the 1M dam
+    break, per particle, scaled by the particle count) over the launch's mean
+    duration, against the SMs' issue capacity at the sampled clock (4
+    schedulers per SM, one warp instruction per scheduler per cycle)."""
+    per = NCU_WARP_INST_PER_PARTICLE.get(kclass)
+    mhz = (clocks or {}).get("sm_mhz")
+    if not per or not mhz or not avg_ms:
+        return None
+    inst = per * n
+    achieved = inst / (avg_ms * 1e-3)
+    peak = 4.0 * sms * mhz * 1e6
+    return {"kernel": kclass, "warp_instructions_per_launch": inst, "achieved": achieved, "peak": peak,
+            "unit": "warp instructions/s", "frac": achieved / peak, "sm_mhz": mhz, "sms": sms,
+            "source": "ncu smsp__inst_executed.sum of one launch on the 1M dam break, scaled by particle count"}
 
 
 def algorithmic_bytes(kclass: str, n: int, nb_active: int, cells: int) -> float | None:
@@ -228,7 +254,16 @@ def bench_ours(args, rank, world):
     torch.cuda.set_device(local)
     sc = make_scene(args.workload)
     stream = torch.cuda.current_stream()
-    s = solver_for(sc, stream=stream.cuda_stream, device=local)
+    if args.slot_order == "morton":
+        from water_simulation_gb300.solver import Solver
+
+        cfg = sc.config()
+        cfg.slot_order = _lib.ORDER_MORTON
+        s = Solver(cfg, device=local, stream=stream.cuda_stream)
+        s.set_boundary(sc.boundary)
+        s.set_fluid(sc.fluid, sc.velocity)
+    else:
+        s = solver_for(sc, stream=stream.cuda_stream, device=local)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     # launch shapes of the neighbour passes, measured on this workload (the
     # state is restored afterwards)
@@ -275,6 +310,7 @@ def bench_ours(args, rank, world):
 
     ms_max, work = replicas.aggregate(ms, float(sc.n) * args.steps, world)
     res = {"ms_total": ms_max, "work": work, "wall_s": wall, "launches": launches, "clocks": clk.summary(),
+           "sms": torch.cuda.get_device_properties(local).multi_processor_count,
            "dominant": dominant, "dominant_ms": dom_ms, "dominant_launches": dom_launches,
            "dominant_timed_in": "warm-up steps (passes apart)" if coop else "timed steps",
            "nb_active": nb_active,
@@ -734,6 +770,49 @@ def bench_lbvh(sc, reps=20, warmup=3):
     return res
 
 
+def bench_morton(sc, steps=20, warmup=3):
+    """The step in Morton slot order (cells ranked by the Morton code of their
+    coordinates, SpatialAccel's key) against the reference's x-major order, on
+    the same input: ms per step (CUDA events, L2 flushed before every step)
+    and the final state compared bit for bit (both orders give every particle
+    the same candidates in the same sequence)."""
+    import torch
+
+    from water_simulation_gb300 import _lib
+    from water_simulation_gb300.solver import Solver
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    out, final = {}, {}
+    for name, order in (("cell_key", _lib.ORDER_CELL_KEY), ("morton", _lib.ORDER_MORTON)):
+        cfg = sc.config()
+        cfg.slot_order = order
+        t0 = time.perf_counter()
+        s = Solver(cfg, stream=stream.cuda_stream)
+        setup_s = time.perf_counter() - t0
+        s.set_boundary(sc.boundary)
+        s.set_fluid(sc.fluid, sc.velocity)
+        for _ in range(warmup):
+            flush.zero_()
+            s.step(sc.dt)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k in range(steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            s.step(sc.dt)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+        final[name] = (s.positions(), s.velocities())
+        out[name] = {"ms_per_step": ms, "particle_steps_per_s": sc.n / (ms * 1e-3), "context_setup_s": setup_s}
+        s.close()
+    out["morton_over_cell_key_time"] = out["morton"]["ms_per_step"] / out["cell_key"]["ms_per_step"]
+    out["same_state"] = bool(np.array_equal(final["cell_key"][0], final["morton"][0]) and
+                             np.array_equal(final["cell_key"][1], final["morton"][1]))
+    out["steps"] = steps
+    return out
+
+
 def bench_ref_cuda(sc, steps, warmup=1):
     from oracle import oracle as O
     from oracle import reference as R
@@ -860,7 +939,7 @@ def main():
                    "density_iters": sc.max_density_iters, "divergence_iters": sc.max_divergence_iters,
                    "dt": sc.dt, "parallelism": f"replicas x{world}",
                    "l2": "flushed before every timed step (256 MB write)",
-                   "threads_per_block": res["block_sizes"]},
+                   "threads_per_block": res["block_sizes"], "slot_order": args.slot_order},
         "gpu_launches": res["launches"],
         "clocks": res["clocks"],
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
@@ -868,9 +947,10 @@ def main():
                      "peak_source": f"{hbm_src} (MEASURED_PEAKS.json hbm_gbs)" if hbm_src == "measured" else "fallback",
                      "algorithmic_bytes_per_launch": alg, "avg_launch_ms": avg_ms,
                      "traffic": (traffic * sc.n) if traffic else None,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch on the 1M dam "
-                                       "break, scaled by particle count (profiles/dfsph_kernels_dam1m.md)",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 1M "
+                                       "dam break, scaled by particle count",
                      "active_boundary_particles": res["nb_active"], "timed_in": res["dominant_timed_in"]},
+        "issue_roofline": issue_roofline(dom, sc.n, avg_ms, res["clocks"], res["sms"]),
         "kernel_share_warmup": res["warmup_share"],
     }
     # every kernel class against the same peak (warm-up steps, per-launch
@@ -937,6 +1017,11 @@ def main():
             line["lbvh"] = bench_lbvh(sc)
         except Exception as e:
             line["lbvh"] = {"unavailable": str(e)[:200]}
+    if rank == 0 and not args.no_morton and args.slot_order == "cell_key":
+        try:
+            line["morton_order"] = bench_morton(sc)
+        except Exception as e:
+            line["morton_order"] = {"unavailable": str(e)[:200]}
     if rank == 0 and not args.no_ref_cuda:
         try:
             big = sc.n > 500000  # the reference's 1M step takes ~0.24 s: a bounded sample

@@ -72,7 +72,21 @@ typedef struct dfsph_config {
                                        they share geometry, wall particles and dt */
     uint32_t use_cuda_graph;        /* 1 => dfsph_step replays a captured CUDA graph of
                                        two steps (only with eta = 0, no profiling) */
+    uint32_t slot_order;            /* DFSPH_ORDER_*: the order of the sorted particle slots */
 } dfsph_config;
+
+/* Slot orders (dfsph_config.slot_order). The reference sorts by the x-major cell
+ * key (core/src/cell_grid.cu:10-30); SpatialAccel's Morton order
+ * (core/src/spatial_accel.cu:11-40) is kept as a variant for comparison: cells
+ * ranked by the Morton code of their (x, y, z) cell coordinates. Both orders
+ * give every particle the same candidates in the same sequence (the stencil is
+ * walked cell by cell in x-major order either way), so with fixed iteration
+ * counts the two steps give the same fields bit for bit; only the memory
+ * layout, and with it the cache behaviour, differs. In Morton order the grid
+ * fields (cell keys, cell_start, sorted indices) are indexed by Morton rank
+ * and small scenes keep the per-pass Jacobi solve. */
+#define DFSPH_ORDER_CELL_KEY 0
+#define DFSPH_ORDER_MORTON   1
 
 typedef struct dfsph_ctx dfsph_ctx;
 

@@ -28,6 +28,9 @@ PRECISION_FP32 = 0
 PRECISION_FP32_KAHAN = 1
 PRECISION_FP64 = 2
 
+ORDER_CELL_KEY = 0
+ORDER_MORTON = 1
+
 FIELD_POSITION = 0
 FIELD_VELOCITY = 1
 FIELD_DENSITY = 2
@@ -102,6 +105,7 @@ class DfsphConfig(ctypes.Structure):
         ("record_diagnostics", ctypes.c_uint32),
         ("n_scenes", ctypes.c_uint32),
         ("use_cuda_graph", ctypes.c_uint32),
+        ("slot_order", ctypes.c_uint32),
     ]
 
 

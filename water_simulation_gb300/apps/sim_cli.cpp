@@ -64,52 +64,57 @@ struct Args {
     std::exit(code);
 }
 
+// The command line as a table of options: a flag, whether it takes a value,
+// and what it sets. Unknown flags, a missing value, a malformed --frames range
+// and a missing --scene end the program with status 2; --help with status 0.
+struct Option {
+    const char* flag;
+    bool takes_value;
+    void (*apply)(Args&, const char* value);
+};
+
+[[noreturn]] void fail(const std::string& msg) {
+    std::fprintf(stderr, "%s\n", msg.c_str());
+    std::exit(2);
+}
+
+void set_frames(Args& a, const char* v) {
+    const std::string r = v;
+    const auto colon = r.find(':');
+    if (colon == std::string::npos) fail("--frames expects START:END");
+    a.frames_start = std::stoi(r.substr(0, colon));
+    a.frames_end = std::stoi(r.substr(colon + 1));
+}
+
+const Option kOptions[] = {
+    {"--scene", true, [](Args& a, const char* v) { a.scene_path = v; }},
+    {"--frames", true, set_frames},
+    {"--record", false, [](Args& a, const char*) { a.record = true; }},
+    {"--out", true, [](Args& a, const char* v) { a.out_dir = v; }},
+    {"--no-vulkan", false, [](Args&, const char*) {}},  // no graphics path exists
+    {"--damping", true, [](Args& a, const char* v) { a.damping = std::stof(v); }},
+    {"--viscosity", true, [](Args& a, const char* v) { a.viscosity = std::stof(v); }},
+    {"--fixed-iters", true, [](Args& a, const char* v) { a.fixed_iters = std::stoi(v); }},
+    {"--host-substeps", false, [](Args& a, const char*) { a.host_substeps = true; }},
+    {"--load-state", true, [](Args& a, const char* v) { a.load_state = v; }},
+    {"--save-state", true, [](Args& a, const char* v) { a.save_state = v; }},
+    {"--solver-params", false, [](Args& a, const char*) { a.solver_params = true; }},
+};
+
 Args parse(int argc, char** argv) {
     Args a;
-    for (int i = 1; i < argc; ++i) {
-        const std::string s = argv[i];
-        if (s == "--scene" && i + 1 < argc) {
-            a.scene_path = argv[++i];
-        } else if (s == "--frames" && i + 1 < argc) {
-            const std::string r = argv[++i];
-            const auto colon = r.find(':');
-            if (colon == std::string::npos) {
-                std::fprintf(stderr, "--frames expects START:END\n");
-                std::exit(2);
-            }
-            a.frames_start = std::stoi(r.substr(0, colon));
-            a.frames_end = std::stoi(r.substr(colon + 1));
-        } else if (s == "--record") {
-            a.record = true;
-        } else if (s == "--out" && i + 1 < argc) {
-            a.out_dir = argv[++i];
-        } else if (s == "--no-vulkan") {
-            // accepted: there is no graphics path
-        } else if (s == "--damping" && i + 1 < argc) {
-            a.damping = std::stof(argv[++i]);
-        } else if (s == "--viscosity" && i + 1 < argc) {
-            a.viscosity = std::stof(argv[++i]);
-        } else if (s == "--fixed-iters" && i + 1 < argc) {
-            a.fixed_iters = std::stoi(argv[++i]);
-        } else if (s == "--host-substeps") {
-            a.host_substeps = true;
-        } else if (s == "--load-state" && i + 1 < argc) {
-            a.load_state = argv[++i];
-        } else if (s == "--save-state" && i + 1 < argc) {
-            a.save_state = argv[++i];
-        } else if (s == "--solver-params") {
-            a.solver_params = true;
-        } else if (s == "-h" || s == "--help") {
-            usage_exit(0);
-        } else {
-            std::fprintf(stderr, "Unknown arg: %s\n", s.c_str());
-            std::exit(2);
-        }
+    int i = 1;
+    while (i < argc) {
+        const std::string flag = argv[i++];
+        if (flag == "-h" || flag == "--help") usage_exit(0);
+        const Option* opt = nullptr;
+        for (const Option& o : kOptions)
+            if (flag == o.flag) opt = &o;
+        if (!opt) fail("Unknown arg: " + flag);
+        if (opt->takes_value && i >= argc) fail("Unknown arg: " + flag);  // a flag without its value
+        opt->apply(a, opt->takes_value ? argv[i++] : nullptr);
     }
-    if (a.scene_path.empty()) {
-        std::fprintf(stderr, "Error: --scene required\n");
-        std::exit(2);
-    }
+    if (a.scene_path.empty()) fail("Error: --scene required");
     return a;
 }
 

@@ -148,7 +148,7 @@ __global__ void __launch_bounds__(128) adjoint_apply_kernel(
     R bgv = 0, JX = 0, JY = 0, JZ = 0;
     if (bd.has && boundary_near(c, g, bd.mask)) {
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
-        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+        for_each_run(c, wall_grid(g), bd.bcs, [&](u32 b, u32 e) {
             for (u32 j = b; j < e; ++j) {
                 const R4<R> pj = ld(xb + j);
                 const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(128) adjoint_rate_kernel(
     R BX = 0, BY = 0, BZ = 0, JX = 0, JY = 0, JZ = 0;
     if (bd.has && boundary_near(c, g, bd.mask)) {
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
-        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+        for_each_run(c, wall_grid(g), bd.bcs, [&](u32 b, u32 e) {
             for (u32 j = b; j < e; ++j) {
                 const R4<R> pj = ld(xb + j);
                 const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(128) adjoint_density_kernel(
     if (bd.has && boundary_near(c, g, bd.mask)) {
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
         R bx = 0, by = 0, bz = 0;
-        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+        for_each_run(c, wall_grid(g), bd.bcs, [&](u32 b, u32 e) {
             for (u32 j = b; j < e; ++j) {
                 const R4<R> pj = ld(xb + j);
                 const R rx = xi.x - pj.x, ry = xi.y - pj.y, rz = xi.z - pj.z;

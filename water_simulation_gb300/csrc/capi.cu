@@ -102,6 +102,10 @@ int dfsph_create(const dfsph_config* cfg, int device, void* stream, dfsph_ctx** 
         g_create_error = "dfsph_create: unknown precision";
         return DFSPH_ERR_INVALID_ARGUMENT;
     }
+    if (cfg->slot_order > DFSPH_ORDER_MORTON) {
+        g_create_error = "dfsph_create: unknown slot order";
+        return DFSPH_ERR_INVALID_ARGUMENT;
+    }
     {
         const dfsph::GridGeom g = dfsph::make_grid_geom(cfg->domain_min, cfg->domain_max, cfg->smoothing_length);
         const double cells = double(g.dims[0]) * double(g.dims[1]) * double(g.dims[2]);

@@ -67,6 +67,10 @@ template <class R> struct GridDev {
     // last). slot_scene[s] is the scene of sorted slot s (null: one scene).
     u32 cells1;
     const unsigned short* slot_scene;
+    // Morton slot order: rank[c] is the sort key of x-major cell c (its rank
+    // in the Morton order of the grid's cells; rank[total] = total); null for
+    // the reference's x-major order, where the sort key is c itself.
+    const u32* rank;
 };
 
 template <class R> inline GridDev<R> to_dev(const GridGeom& g) {
@@ -78,6 +82,7 @@ template <class R> inline GridDev<R> to_dev(const GridGeom& g) {
     d.slot_scene = nullptr;
     d.inv_bin = g.inv_bin;
     d.inv_stencil = g.inv_stencil;
+    d.rank = nullptr;
     return d;
 }
 
@@ -99,6 +104,16 @@ __device__ __forceinline__ u32 cell_key(R px, R py, R pz, const GridDev<R>& g) {
     if (cx < 0 || cx >= g.nx || cy < 0 || cy >= g.ny || cz < 0 || cz >= g.nz) return g.total;
     return (static_cast<u32>(cx) * static_cast<u32>(g.ny) + static_cast<u32>(cy)) *
                static_cast<u32>(g.nz) + static_cast<u32>(cz);
+}
+
+// The sort key of x-major cell c: c itself, or in Morton slot order its
+// Morton rank (rank[total] = total keeps the out-of-grid key last).
+template <bool MORTON, class R> __device__ __forceinline__ u32 sort_key(const GridDev<R>& g, u32 c) {
+    if constexpr (MORTON) {
+        return __ldg(g.rank + c);
+    } else {
+        return c;
+    }
 }
 
 // Programmatic dependent launch: a kernel launched with programmatic stream
@@ -150,6 +165,16 @@ __device__ __forceinline__ Centre stencil_centre(R px, R py, R pz, const GridDev
 static __device__ u32 g_bounds_violations;
 #endif
 
+// The grid of the wall particles: the fluid grid's geometry in the x-major
+// order, whatever the fluid's slot order (walls are always sorted by x-major
+// key, and their cell_start is indexed by it). for_each_run ignores rank; the
+// copy keeps the wall walks free of the fluid's rank table all the same.
+template <class R> __device__ __forceinline__ GridDev<R> wall_grid(const GridDev<R>& g) {
+    GridDev<R> w = g;
+    w.rank = nullptr;
+    return w;
+}
+
 template <class R, class F>
 __device__ __forceinline__ void for_each_run(const Centre& c, const GridDev<R>& g,
                                              const u32* __restrict__ cs, F&& f) {
@@ -180,6 +205,57 @@ __device__ __forceinline__ void for_each_run(const Centre& c, const GridDev<R>& 
 #endif
             f(b, e);
         }
+    }
+}
+
+// The same 27 cells in the same sequence in Morton slot order (g.rank set):
+// a column's cells are not adjacent in slot order, so each cell is one run,
+// looked up through the rank table.
+template <class R, class F>
+__device__ __forceinline__ void for_each_run_ranked(const Centre& c, const GridDev<R>& g,
+                                                    const u32* __restrict__ cs, F&& f) {
+    const int z0 = max(c.z - 1, 0);
+    const int z1 = min(c.z + 1, g.nz - 1);
+    if (z0 > z1) return;
+#ifdef DFSPH_BOUNDS_CHECK
+    const u32 limit = __ldg(cs + g.cells1);
+#endif
+#pragma unroll 1
+    for (int dx = -1; dx <= 1; ++dx) {
+        const int nx = c.x + dx;
+        if (nx < 0 || nx >= g.nx) continue;
+#pragma unroll 1
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int ny = c.y + dy;
+            if (ny < 0 || ny >= g.ny) continue;
+            const u32 base = (static_cast<u32>(nx) * static_cast<u32>(g.ny) + static_cast<u32>(ny)) *
+                             static_cast<u32>(g.nz);
+#pragma unroll 1
+            for (int z = z0; z <= z1; ++z) {
+                const u32 r = __ldg(g.rank + base + static_cast<u32>(z));
+                const u32 b = __ldg(cs + r);
+                const u32 e = __ldg(cs + r + 1);
+#ifdef DFSPH_BOUNDS_CHECK
+                if (b > e || e > limit) {
+                    atomicAdd(&g_bounds_violations, 1u);
+                    continue;
+                }
+#endif
+                f(b, e);
+            }
+        }
+    }
+}
+
+// The fluid stencil walk of a kernel instantiated for the x-major slot order
+// (MORTON = false, the reference's) or the Morton one.
+template <bool MORTON, class R, class F>
+__device__ __forceinline__ void for_each_fluid_run(const Centre& c, const GridDev<R>& g, const u32* __restrict__ cs,
+                                                   F&& f) {
+    if constexpr (MORTON) {
+        for_each_run_ranked(c, g, cs, f);
+    } else {
+        for_each_run(c, g, cs, f);
     }
 }
 

@@ -376,7 +376,8 @@ __global__ void __launch_bounds__(256) count_kernel(int n, const R4<R>* __restri
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const R4<R> p = ld(xk + s);
-    const u32 k = cell_key(p.x, p.y, p.z, g) + scene_of(g, s) * g.cells1;
+    const u32 c = cell_key(p.x, p.y, p.z, g);
+    const u32 k = (g.rank ? __ldg(g.rank + c) : c) + scene_of(g, s) * g.cells1;
     key[s] = k;
     rank[s] = atomicAdd(count + k, 1u);
 }
@@ -769,7 +770,7 @@ __global__ void __launch_bounds__(256) boundary_mask_kernel(u32 total, const u32
 }
 
 // 1 per boundary particle that has a fluid particle within the support.
-template <class R>
+template <class R, bool MORTON = false>
 __global__ void __launch_bounds__(128) active_boundary_kernel(int nb, const R4<R>* __restrict__ xb,
                                                               const R4<R>* __restrict__ xk,
                                                               const u32* __restrict__ cs, GridDev<R> g,
@@ -780,7 +781,7 @@ __global__ void __launch_bounds__(128) active_boundary_kernel(int nb, const R4<R
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
     u32 any = 0;
     for (int sc = 0; sc < n_scenes && !any; ++sc)
-        for_each_run(c, g, cs + size_t(sc) * g.cells1, [&](u32 b, u32 e) {
+        for_each_fluid_run<MORTON>(c, g, cs + size_t(sc) * g.cells1, [&](u32 b, u32 e) {
             for (u32 j = b; j < e && !any; ++j) {
                 const R4<R> pj = ld(xk + j);
                 const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
@@ -833,7 +834,7 @@ __device__ __forceinline__ u32 mix32(u32 x) {
     return x;
 }
 
-template <class R, bool KAHAN, bool DIAG, int LB>
+template <class R, bool KAHAN, bool DIAG, int LB, bool MORTON = false>
 __global__ void __launch_bounds__(LB) density_alpha_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, R* __restrict__ alpha,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, u32* __restrict__ nbr_f,
@@ -846,7 +847,7 @@ __global__ void __launch_bounds__(LB) density_alpha_kernel(
     R ws = 0, wc = 0;
     R gx = 0, gy = 0, gz = 0, gq = 0;
     u32 cf = 0, cb = 0, sig = 0;
-    for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+    for_each_fluid_run<MORTON>(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
         if (DIAG) {
             cf += e - b;
             for (u32 j = b; j < e; ++j) sig += mix32(__ldg(id + j));
@@ -877,7 +878,7 @@ __global__ void __launch_bounds__(LB) density_alpha_kernel(
     if (bd.has && boundary_near(c, g, bd.mask)) {
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
         R bs = 0, bsc = 0;
-        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+        for_each_run(c, wall_grid(g), bd.bcs, [&](u32 b, u32 e) {
             if (DIAG) cb += e - b;
             for (u32 j = b; j < e; ++j) {
                 const R4<R> pj = ld(xb + j);
@@ -901,11 +902,11 @@ __global__ void __launch_bounds__(LB) density_alpha_kernel(
         });
         rho += bs;
     } else if (DIAG && bd.has) {
-        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) { cb += e - b; });
+        for_each_run(c, wall_grid(g), bd.bcs, [&](u32 b, u32 e) { cb += e - b; });
     }
     if (DIAG && bd.has) {
         // wall candidates by their sorted slot (the wall order is fixed)
-        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+        for_each_run(c, wall_grid(g), bd.bcs, [&](u32 b, u32 e) {
             for (u32 j = b; j < e; ++j) sig += mix32(j ^ 0x80000000u);
         });
     }
@@ -928,7 +929,7 @@ __global__ void __launch_bounds__(LB) density_alpha_kernel(
 // and, because g dt cancels in v'_j - v'_i, the XSPH term of v' equals
 // e^{-d dt} times the XSPH term of v. Reads vr_in, writes vr_out.
 // ---------------------------------------------------------------------------
-template <class R, int LB>
+template <class R, int LB, bool MORTON = false>
 __global__ void __launch_bounds__(LB) forces_xsph_kernel(
     int n, const R4<R>* __restrict__ xk, const R4<R>* __restrict__ vr_in, R4<R>* __restrict__ vr_out,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, StepDt<R> sd, R eps,
@@ -946,7 +947,7 @@ __global__ void __launch_bounds__(LB) forces_xsph_kernel(
     if (do_xsph) {
         const R4<R> pi = ld(xk + i);
         const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
-        for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+        for_each_fluid_run<MORTON>(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
             for (u32 j = b; j < e; ++j) {
                 const R4<R> pj = ld(xk + j);
                 const R4<R> vj = ld(vr_in + j);
@@ -969,7 +970,7 @@ __global__ void __launch_bounds__(LB) forces_xsph_kernel(
 
 // One particle of the rate pass: rho_adv, kappa and (x, kappa / rho^2) of
 // particle i; returns its error term (the reduction's input).
-template <class R, bool DIVERGENCE>
+template <class R, bool DIVERGENCE, bool MORTON = false>
 __device__ __forceinline__ double rate_particle(int i, const R4<R>* __restrict__ xk_in, R4<R>* __restrict__ xk_out,
                                                 const R4<R>* __restrict__ vr, const R* __restrict__ alpha,
                                                 R* __restrict__ rho_adv, R* __restrict__ kap,
@@ -986,7 +987,7 @@ __device__ __forceinline__ double rate_particle(int i, const R4<R>* __restrict__
         rate_fluid_terms(pi, vi, pj, vj, p, f, d);
         rd = fma_r(f, d, rd);
     };
-    for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+    for_each_fluid_run<MORTON>(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
 #pragma unroll 2
         for (u32 j = b; j < e; ++j) pair(ld(xk_in + j), ld(vr + j));
     });
@@ -999,7 +1000,7 @@ __device__ __forceinline__ double rate_particle(int i, const R4<R>* __restrict__
             rate_wall_terms(pi, vi, pj, p, f, d);
             rb = fma_r(f, d, rb);
         };
-        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+        for_each_run(c, wall_grid(g), bd.bcs, [&](u32 b, u32 e) {
             for (u32 j = b; j < e; ++j) wall(ld(xb + j));
         });
         rd += rb;
@@ -1032,7 +1033,7 @@ __device__ __forceinline__ double rate_particle(int i, const R4<R>* __restrict__
 // max(0, rho_dot). Writes xk_out = (x, kappa / max(rho^2, 1e-9)); xk_in is
 // not written.
 // ---------------------------------------------------------------------------
-template <class R, bool DIVERGENCE, bool REDUCE, bool DEVLOOP, int LB>
+template <class R, bool DIVERGENCE, bool REDUCE, bool DEVLOOP, int LB, bool MORTON = false>
 __global__ void __launch_bounds__(LB) pressure_rate_kernel(
     int n, const R4<R>* __restrict__ xk_in, R4<R>* __restrict__ xk_out,
     const R4<R>* __restrict__ vr, const R* __restrict__ alpha, R* __restrict__ rho_adv,
@@ -1057,7 +1058,8 @@ __global__ void __launch_bounds__(LB) pressure_rate_kernel(
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double err = 0;
     if (i < n)
-        err = rate_particle<R, DIVERGENCE>(i, xk_in, xk_out, vr, alpha, rho_adv, kap, cs, g, p, bd, dt, tape_v);
+        err = rate_particle<R, DIVERGENCE, MORTON>(i, xk_in, xk_out, vr, alpha, rho_adv, kap, cs, g, p, bd, dt,
+                                                   tape_v);
     if (REDUCE) {
         const double t = block_sum_dyn(err, sh);
         if (threadIdx.x == 0) finish_reduction(t, partials, ctl, iter, first_check, rule);
@@ -1068,7 +1070,7 @@ __global__ void __launch_bounds__(LB) pressure_rate_kernel(
 // v_i -= dt sum_j m (kfac_i + kfac_j) gradW over fluid and
 // dt sum_b m_b (kfac_i + kappa_i / max(rho0^2, 1e-9)) gradW over the boundary.
 // One particle of the apply pass: its velocity after the pressure update.
-template <class R>
+template <class R, bool MORTON = false>
 __device__ __forceinline__ R4<R> apply_velocity(int i, const R4<R>* __restrict__ xk, const R4<R>* __restrict__ vr,
                                                 const R* __restrict__ kap, const u32* __restrict__ cs,
                                                 const GridDev<R>& g, const Phys<R>& p, const BoundaryDev& bd, R dt) {
@@ -1080,7 +1082,7 @@ __device__ __forceinline__ R4<R> apply_velocity(int i, const R4<R>* __restrict__
         apply_terms(pi, pj, pi.w + pj.w, p, f, rx, ry, rz);
         ax = fma_r(f, rx, ax); ay = fma_r(f, ry, ay); az = fma_r(f, rz, az);
     };
-    for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
+    for_each_fluid_run<MORTON>(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
         for (u32 j = b; j < e; ++j) pair(ld(xk + j));
     });
     const R sf = -dt * p.mass;
@@ -1094,7 +1096,7 @@ __device__ __forceinline__ R4<R> apply_velocity(int i, const R4<R>* __restrict__
             apply_terms(pi, pj, pj.w, p, f, rx, ry, rz);
             bx = fma_r(f, rx, bx); by = fma_r(f, ry, by); bz = fma_r(f, rz, bz);
         };
-        for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+        for_each_run(c, wall_grid(g), bd.bcs, [&](u32 b, u32 e) {
             for (u32 j = b; j < e; ++j) wall(ld(xb + j));
         });
         const R sb = -dt * kb;
@@ -1105,7 +1107,7 @@ __device__ __forceinline__ R4<R> apply_velocity(int i, const R4<R>* __restrict__
     return v;
 }
 
-template <class R, bool DEVLOOP, int LB>
+template <class R, bool DEVLOOP, int LB, bool MORTON = false>
 __global__ void __launch_bounds__(LB) pressure_apply_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, const R* __restrict__ kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, const IterCtl* ctl,
@@ -1119,7 +1121,7 @@ __global__ void __launch_bounds__(LB) pressure_apply_kernel(
     const R dt = step_dt(sd);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    vr[i] = apply_velocity(i, xk, vr, kap, cs, g, p, bd, dt);
+    vr[i] = apply_velocity<R, MORTON>(i, xk, vr, kap, cs, g, p, bd, dt);
 }
 
 // The rate and apply passes of jacobi_solve_kernel with one particle per quad
@@ -1362,7 +1364,7 @@ __global__ void __launch_bounds__(4 * P + 32) jacobi_solve_kernel(
         if (bd.has && boundary_near(c, g, bd.mask)) {
             u32 wl = 0xFFFFFFFFu, wh = 0u;
             int kw = 0;
-            for_each_run(c, g, bd.bcs, [&](u32 b, u32 e) {
+            for_each_run(c, wall_grid(g), bd.bcs, [&](u32 b, u32 e) {
                 if (b < e) {
                     wrun_b[kw * P + pl] = b;
                     wrun_e[kw * P + pl] = e;
@@ -1488,7 +1490,7 @@ template <class R> struct Domain {
 // One particle of the integrator: writes v and x (to xk_out), the next
 // step's cell key and rank when COUNT, the clamp mask when recording; returns
 // the bits of |v| (non-negative floats order as integers).
-template <class R, bool COUNT>
+template <class R, bool COUNT, bool MORTON = false>
 __device__ __forceinline__ u32 integrate_particle(int i, R4<R> v, const R4<R>& x, R dt, const Domain<R>& d,
                                                   const GridDev<R>& g, R4<R>* __restrict__ vr, R4<R>* xk_out,
                                                   u32* __restrict__ key, u32* __restrict__ rank,
@@ -1515,7 +1517,7 @@ __device__ __forceinline__ u32 integrate_particle(int i, R4<R> v, const R4<R>& x
     vr[i] = {v.x, v.y, v.z, v.w};
     xk_out[i] = {px, py, pz, R(0)};
     if (COUNT) {
-        const u32 k = cell_key(px, py, pz, g) + scene_of(g, i) * g.cells1;
+        const u32 k = sort_key<MORTON>(g, cell_key(px, py, pz, g)) + scene_of(g, i) * g.cells1;
         key[i] = k;
         rank[i] = atomicAdd(count + k, 1u);
     }
@@ -1546,7 +1548,7 @@ __device__ __forceinline__ void max_velocity_epilogue(bool valid, u32 vbits, u32
     }
 }
 
-template <class R, bool COUNT>
+template <class R, bool COUNT, bool MORTON = false>
 __global__ void __launch_bounds__(256) advect_kernel(
     int n, const R4<R>* xk, R4<R>* xk_out, R4<R>* __restrict__ vr, StepDt<R> sd, Domain<R> d, GridDev<R> g,
     u32* __restrict__ key, u32* __restrict__ rank, u32* __restrict__ count, IterCtl* ctl,
@@ -1559,7 +1561,7 @@ __global__ void __launch_bounds__(256) advect_kernel(
     if (i < n) {
         const R4<R> v = vr[i];
         if (tape_v) tape_v[i] = v;
-        vbits = integrate_particle<R, COUNT>(i, v, xk[i], dt, d, g, vr, xk_out, key, rank, count, tape_mask);
+        vbits = integrate_particle<R, COUNT, MORTON>(i, v, xk[i], dt, d, g, vr, xk_out, key, rank, count, tape_mask);
         scene = scene_of(g, i);
     }
     max_velocity_epilogue<256>(i < n, vbits, scene, ctl, maxv_scene);
@@ -1570,7 +1572,7 @@ __global__ void __launch_bounds__(256) advect_kernel(
 // (same values as the two passes: the apply pass's velocity, positions from
 // the same buffer). xk_out is the other position buffer, which nothing in
 // this pass reads.
-template <class R, bool COUNT, int LB>
+template <class R, bool COUNT, int LB, bool MORTON = false>
 __global__ void __launch_bounds__(LB) apply_advect_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* xk_out, R4<R>* __restrict__ vr, const R* __restrict__ kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, Domain<R> d,
@@ -1582,8 +1584,9 @@ __global__ void __launch_bounds__(LB) apply_advect_kernel(
     u32 vbits = 0;
     u32 scene = 0xffffffffu;
     if (i < n) {
-        const R4<R> v = apply_velocity(i, xk, vr, kap, cs, g, p, bd, dt);
-        vbits = integrate_particle<R, COUNT>(i, v, ld(xk + i), dt, d, g, vr, xk_out, key, rank, count, nullptr);
+        const R4<R> v = apply_velocity<R, MORTON>(i, xk, vr, kap, cs, g, p, bd, dt);
+        vbits = integrate_particle<R, COUNT, MORTON>(i, v, ld(xk + i), dt, d, g, vr, xk_out, key, rank, count,
+                                                     nullptr);
         scene = scene_of(g, i);
     }
     max_velocity_epilogue<LB>(i < n, vbits, scene, ctl, maxv_scene);

@@ -15,6 +15,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include <nvtx3/nvToolsExt.h>
@@ -51,6 +52,47 @@ struct NvtxRange {
     NvtxRange(const NvtxRange&) = delete;
     NvtxRange& operator=(const NvtxRange&) = delete;
 };
+
+// The rank of every cell of a dims[0] x dims[1] x dims[2] grid in the Morton
+// order of its cell coordinates (bits interleaved x highest, as SpatialAccel's
+// morton3D, core/src/spatial_accel.cu:11-28), indexed by x-major cell id, with
+// the out-of-grid key (the cell count) ranked last.
+inline std::vector<u32> morton_cell_ranks(const int dims[3]) {
+    auto spread = [](u64 v) {  // bit k of v to bit 3k
+        v &= 0x1FFFFFull;
+        v = (v | (v << 32)) & 0x1F00000000FFFFull;
+        v = (v | (v << 16)) & 0x1F0000FF0000FFull;
+        v = (v | (v << 8)) & 0x100F00F00F00F00Full;
+        v = (v | (v << 4)) & 0x10C30C30C30C30C3ull;
+        v = (v | (v << 2)) & 0x1249249249249249ull;
+        return v;
+    };
+    auto gather = [](u64 v) {  // inverse of spread
+        v &= 0x1249249249249249ull;
+        v = (v ^ (v >> 2)) & 0x10C30C30C30C30C3ull;
+        v = (v ^ (v >> 4)) & 0x100F00F00F00F00Full;
+        v = (v ^ (v >> 8)) & 0x1F0000FF0000FFull;
+        v = (v ^ (v >> 16)) & 0x1F00000000FFFFull;
+        v = (v ^ (v >> 32)) & 0x1FFFFFull;
+        return v;
+    };
+    const u64 nx = u64(dims[0]), ny = u64(dims[1]), nz = u64(dims[2]);
+    const u64 total = nx * ny * nz;
+    std::vector<u64> codes;
+    codes.reserve(total);
+    for (u64 x = 0; x < nx; ++x)
+        for (u64 y = 0; y < ny; ++y)
+            for (u64 z = 0; z < nz; ++z) codes.push_back((spread(x) << 2) | (spread(y) << 1) | spread(z));
+    std::sort(codes.begin(), codes.end());
+    std::vector<u32> rank(total + 1);
+    for (u64 k = 0; k < total; ++k) {
+        const u64 c = codes[k];
+        const u64 x = gather(c >> 2), y = gather(c >> 1), z = gather(c);
+        rank[(x * ny + y) * nz + z] = static_cast<u32>(k);
+    }
+    rank[total] = static_cast<u32>(total);
+    return rank;
+}
 
 template <class R>
 class Solver final : public SolverBase {
@@ -124,6 +166,16 @@ public:
         }
         bcs_.alloc(size_t(cells1_) + 1);
         bmask_.alloc(std::max<size_t>(geom_.total, 1));
+        if (cfg_.slot_order == DFSPH_ORDER_MORTON) {
+            // the fluid slots follow the Morton order of the cells; the wall
+            // grid (gb_) keeps the x-major order
+            const std::vector<u32> rank = morton_cell_ranks(geom_.dims);
+            morton_rank_.alloc(rank.size());
+            DFSPH_CUDA(cudaMemcpyAsync(morton_rank_.p, rank.data(), rank.size() * sizeof(u32),
+                                       cudaMemcpyHostToDevice, stream_));
+            DFSPH_CUDA(cudaStreamSynchronize(stream_));  // the host vector goes out of scope
+            g_.rank = morton_rank_.p;
+        }
         if (scenes_ > 1) {
             slot_scene_.alloc(std::max(cap_, 1u));
             eps_scene_.alloc(scenes_);
@@ -168,6 +220,13 @@ public:
         if (host_fctl_) cudaFreeHost(host_fctl_);
         for (const Record& r : records_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
         for (cudaEvent_t e : free_events_) cudaEventDestroy(e);
+    }
+
+    // Calls f with std::true_type when the fluid slots are in Morton order
+    // (the kernels' MORTON instantiation) and std::false_type otherwise.
+    template <class F> void with_slot_order(F&& f) {
+        if (g_.rank) f(std::true_type{});
+        else f(std::false_type{});
     }
 
     void set_stream(cudaStream_t s) override {
@@ -987,6 +1046,7 @@ private:
 
     void check_adjoint_config() const {
         if (scenes_ != 1) throw Error(DFSPH_ERR_STATE, "the adjoint steps one scene");
+        if (g_.rank) throw Error(DFSPH_ERR_STATE, "the adjoint needs the x-major slot order");
         if ((cfg_.max_density_iters > 0 && cfg_.eta_density > 0.0f) ||
             (cfg_.max_divergence_iters > 0 && cfg_.eta_divergence > 0.0f))
             throw Error(DFSPH_ERR_STATE, "the adjoint needs fixed iteration counts (eta_density = eta_divergence = 0)");
@@ -1465,8 +1525,10 @@ private:
         if (nb_ == 0 || n_ == 0 || !stepped_) return 0;
         u32* d = static_cast<u32*>(scratch_bytes(sizeof(u32)));
         DFSPH_CUDA(cudaMemsetAsync(d, 0, sizeof(u32), stream_));
-        launch(DFSPH_KERNEL_OTHER, active_boundary_kernel<R>, blocks_for(nb_, 128), 128, int(nb_), xb_[0].p,
-               xk_[cx_].p, cell_start_.p, gb_, phys_, int(scenes_), d);
+        with_slot_order([&](auto order) {
+            launch(DFSPH_KERNEL_OTHER, active_boundary_kernel<R, decltype(order)::value>, blocks_for(nb_, 128), 128,
+                   int(nb_), xb_[0].p, xk_[cx_].p, cell_start_.p, g_, phys_, int(scenes_), d);
+        });
         u32 h = 0;
         DFSPH_CUDA(cudaMemcpyAsync(&h, d, sizeof(u32), cudaMemcpyDeviceToHost, stream_));
         DFSPH_CUDA(cudaStreamSynchronize(stream_));
@@ -1537,36 +1599,48 @@ private:
             R* kap_it = tp ? tp->kap[w] + it * tp->stride : kap_out;
             R* adv_it = tp ? tp->adv[w] + it * tp->stride : adv_out;
             V4* tv = tp ? tp->v[w] + it * tp->stride : nullptr;
-            if (adaptive)
-                launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true, false, 128>, pressure_rate_kernel<R, DIV, true, false, 256>, n,
-                       xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl,
-                       it, first_check, thr, tv, (const u32*)nullptr);
-            else
-                launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, false, false, 128>, pressure_rate_kernel<R, DIV, false, false, 256>, n,
-                       xin, xout, vr_[cv_].p, alpha_.p, adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl,
-                       it, first_check, thr, tv, (const u32*)nullptr);
+            with_slot_order([&](auto order) {
+                constexpr bool M = decltype(order)::value;
+                if (adaptive)
+                    launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true, false, 128, M>,
+                                pressure_rate_kernel<R, DIV, true, false, 256, M>, n, xin, xout, vr_[cv_].p, alpha_.p,
+                                adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl, it, first_check, thr, tv,
+                                (const u32*)nullptr);
+                else
+                    launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, false, false, 128, M>,
+                                pressure_rate_kernel<R, DIV, false, false, 256, M>, n, xin, xout, vr_[cv_].p, alpha_.p,
+                                adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl, it, first_check, thr, tv,
+                                (const u32*)nullptr);
+            });
             if (!tp) cx_ ^= 1;
             // the last iteration of a fixed-count solve may carry the
             // integrator, when the other position buffer is the one the step
             // must end in
             if (fa && !adaptive && it + 1 == max_iters && cx_ != fa->cx0) {
-                if (fa->count)
-                    launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, apply_advect_kernel<R, true, 128>,
-                                apply_advect_kernel<R, true, 256>, n, (const V4*)xout, xk_[cx_ ^ 1].p, vr_[cv_].p,
-                                (const R*)kap_it, cs, g_, phys_, bdev(), sd, fa->d, key_.p, rank_.p, count_.p, ctl_.p,
-                                fa->mvs);
-                else
-                    launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, apply_advect_kernel<R, false, 128>,
-                                apply_advect_kernel<R, false, 256>, n, (const V4*)xout, xk_[cx_ ^ 1].p, vr_[cv_].p,
-                                (const R*)kap_it, cs, g_, phys_, bdev(), sd, fa->d, key_.p, rank_.p, count_.p, ctl_.p,
-                                fa->mvs);
+                with_slot_order([&](auto order) {
+                    constexpr bool M = decltype(order)::value;
+                    if (fa->count)
+                        launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, apply_advect_kernel<R, true, 128, M>,
+                                    apply_advect_kernel<R, true, 256, M>, n, (const V4*)xout, xk_[cx_ ^ 1].p,
+                                    vr_[cv_].p, (const R*)kap_it, cs, g_, phys_, bdev(), sd, fa->d, key_.p, rank_.p,
+                                    count_.p, ctl_.p, fa->mvs);
+                    else
+                        launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, apply_advect_kernel<R, false, 128, M>,
+                                    apply_advect_kernel<R, false, 256, M>, n, (const V4*)xout, xk_[cx_ ^ 1].p,
+                                    vr_[cv_].p, (const R*)kap_it, cs, g_, phys_, bdev(), sd, fa->d, key_.p, rank_.p,
+                                    count_.p, ctl_.p, fa->mvs);
+                });
                 cx_ ^= 1;
                 fa->done = true;
                 launched = it + 1;
                 break;
             }
-            launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R, false, 128>, pressure_apply_kernel<R, false, 256>, n, xout,
-                   vr_[cv_].p, kap_it, cs, g_, phys_, bdev(), sd, ctl, it, (const V4*)nullptr, (const u32*)nullptr);
+            with_slot_order([&](auto order) {
+                constexpr bool M = decltype(order)::value;
+                launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R, false, 128, M>,
+                            pressure_apply_kernel<R, false, 256, M>, n, xout, vr_[cv_].p, kap_it, cs, g_, phys_, bdev(),
+                            sd, ctl, it, (const V4*)nullptr, (const u32*)nullptr);
+            });
             launched = it + 1;
             if (adaptive && it + 1 > first_check) {  // it >= first_check
                 // The reference reads the error back every iteration
@@ -1604,6 +1678,7 @@ private:
     bool solve_cooperative(const StepDt<R>& sd, u32 max_iters, const StopTest& thr, u32 first_check, IterCtl* ctl,
                            R* kap_out, R* adv_out, const u32* cs, bool probe = false) {
         if ((max_iters == 0 && !probe) || profile_mask_ != 0) return false;
+        if (g_.rank) return false;  // its run tables hold the 9 column runs of the x-major order
         int& accepted = coop_ok_[DIV ? 1 : 0];
         // a capture records only launches that this device has accepted
         // eagerly: a refusal inside a capture would fail the capture or, on a
@@ -1691,6 +1766,9 @@ private:
     u32 solve_on_device(const StepDt<R>& sd, u32 max_iters, const StopTest& thr, u32 first_check, IterCtl* ctl, R* kap_out,
                         R* adv_out, const u32* cs) {
         if (max_iters == 0) return 0;
+        if (g_.rank)
+            throw Error(DFSPH_ERR_STATE, "adaptive solves inside CUDA graphs (device-resident loops) need the x-major "
+                                         "slot order");
         const int n = int(n_);
         cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
         cudaGraph_t g = nullptr;
@@ -1770,21 +1848,28 @@ private:
         const BoundaryDev bd = bdev();
         const bool kahan = cfg_.precision == DFSPH_PRECISION_FP32_KAHAN;
         const u32* idn = id_[ci_].p;
-        if (cfg_.record_diagnostics) {
-            if (kahan)
-                launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, true, 128>, density_alpha_kernel<R, true, true, 256>, n,
-                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, nbr_f_.p, nbr_b_.p, nbr_sig_.p, idn, t1);
-            else
-                launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, true, 128>, density_alpha_kernel<R, false, true, 256>, n,
-                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, nbr_f_.p, nbr_b_.p, nbr_sig_.p, idn, t1);
-        } else {
-            if (kahan)
-                launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, false, 128>, density_alpha_kernel<R, true, false, 256>, n,
-                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr, (u32*)nullptr, idn, t1);
-            else
-                launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, false, 128>, density_alpha_kernel<R, false, false, 256>, n,
-                       xk_[cx_].p, vr_[cv_].p, alpha_.p, cs, g_, phys_, bd, (u32*)nullptr, (u32*)nullptr, (u32*)nullptr, idn, t1);
-        }
+        with_slot_order([&](auto order) {
+            constexpr bool M = decltype(order)::value;
+            if (cfg_.record_diagnostics) {
+                if (kahan)
+                    launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, true, 128, M>,
+                                density_alpha_kernel<R, true, true, 256, M>, n, xk_[cx_].p, vr_[cv_].p, alpha_.p, cs,
+                                g_, phys_, bd, nbr_f_.p, nbr_b_.p, nbr_sig_.p, idn, t1);
+                else
+                    launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, true, 128, M>,
+                                density_alpha_kernel<R, false, true, 256, M>, n, xk_[cx_].p, vr_[cv_].p, alpha_.p, cs,
+                                g_, phys_, bd, nbr_f_.p, nbr_b_.p, nbr_sig_.p, idn, t1);
+            } else {
+                if (kahan)
+                    launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, true, false, 128, M>,
+                                density_alpha_kernel<R, true, false, 256, M>, n, xk_[cx_].p, vr_[cv_].p, alpha_.p, cs,
+                                g_, phys_, bd, (u32*)nullptr, (u32*)nullptr, (u32*)nullptr, idn, t1);
+                else
+                    launch_pass(DFSPH_KERNEL_DENSITY_ALPHA, density_alpha_kernel<R, false, false, 128, M>,
+                                density_alpha_kernel<R, false, false, 256, M>, n, xk_[cx_].p, vr_[cv_].p, alpha_.p, cs,
+                                g_, phys_, bd, (u32*)nullptr, (u32*)nullptr, (u32*)nullptr, idn, t1);
+            }
+        });
         // 3. divergence solve (the reference's plan; 0 iterations = the reference)
         last_divergence_launched_ = 0;
         if (cfg_.max_divergence_iters > 0)
@@ -1792,9 +1877,13 @@ private:
                                                     kap_v_.p, rho_dot_.p, cs, tp);
         // 4. gravity + damping + XSPH (dfsph.cu:188-213)
         const bool xsph = explicit_eps_ ? any_xsph_ : cfg_.viscosity > 0.0f;
-        launch_pass(DFSPH_KERNEL_FORCES_XSPH, forces_xsph_kernel<R, 128>, forces_xsph_kernel<R, 256>, n, xk_[cx_].p, vr_[cv_].p,
-               vr_[cv_ ^ 1].p, cs, g_, phys_, sd, R(cfg_.viscosity),
-               scenes_ > 1 ? (const R*)eps_scene_.p : (const R*)nullptr, xsph ? 1 : 0, tp ? tp->vx : nullptr);
+        with_slot_order([&](auto order) {
+            constexpr bool M = decltype(order)::value;
+            launch_pass(DFSPH_KERNEL_FORCES_XSPH, forces_xsph_kernel<R, 128, M>, forces_xsph_kernel<R, 256, M>, n,
+                        xk_[cx_].p, vr_[cv_].p, vr_[cv_ ^ 1].p, cs, g_, phys_, sd, R(cfg_.viscosity),
+                        scenes_ > 1 ? (const R*)eps_scene_.p : (const R*)nullptr, xsph ? 1 : 0,
+                        tp ? tp->vx : nullptr);
+        });
         cv_ ^= 1;
         // 5. density solve (dfsph.cu:215-260), its last iteration fused with
         // the integrator where possible
@@ -1812,16 +1901,18 @@ private:
         const V4* xin = xk_[cx_].p;
         V4* xout = cx_ != cx0 ? xk_[cx_ ^ 1].p : xk_[cx_].p;
         cx_ = cx0;
-        if (count_next) {
-            launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, true>, blocks_for(n, 256), 256, n, xin, xout, vr_[cv_].p,
-                   sd, dom, g_, key_.p, rank_.p, count_.p, ctl_.p, mvs, tp ? tp->va : nullptr,
-                   tp ? tp->amask : nullptr);
-            counts_valid_ = true;
-        } else {
-            launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, false>, blocks_for(n, 256), 256, n, xin, xout, vr_[cv_].p,
-                   sd, dom, g_, key_.p, rank_.p, count_.p, ctl_.p, mvs, tp ? tp->va : nullptr,
-                   tp ? tp->amask : nullptr);
-        }
+        with_slot_order([&](auto order) {
+            constexpr bool M = decltype(order)::value;
+            if (count_next)
+                launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, true, M>, blocks_for(n, 256), 256, n, xin, xout,
+                       vr_[cv_].p, sd, dom, g_, key_.p, rank_.p, count_.p, ctl_.p, mvs, tp ? tp->va : nullptr,
+                       tp ? tp->amask : nullptr);
+            else
+                launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, false, M>, blocks_for(n, 256), 256, n, xin, xout,
+                       vr_[cv_].p, sd, dom, g_, key_.p, rank_.p, count_.p, ctl_.p, mvs, tp ? tp->va : nullptr,
+                       tp ? tp->amask : nullptr);
+        });
+        if (count_next) counts_valid_ = true;
     }
 
     dfsph_config cfg_;
@@ -1860,6 +1951,7 @@ private:
     DevBuf<u32> bkey_, brank_, bkey_sorted_, btmp_src_, btmp_id_;
     DevBuf<u32> count_, cell_start_, tile_sums_, bcs_;
     DevBuf<unsigned char> bmask_;
+    DevBuf<u32> morton_rank_;  // Morton slot order: sort key of every x-major cell
     DevBuf<double> partials_;
     DevBuf<IterCtl> ctl_;
     DevBuf<u32> dev_err_;  // device error word (DEV_ERR_*), sticky until check_device_status
