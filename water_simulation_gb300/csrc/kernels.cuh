@@ -140,21 +140,41 @@ template <class R> __device__ __forceinline__ R grad_factor_x(R r, R rinv, const
     return r < p.l ? inner : outer;
 }
 
+// a.x - b.x and a.y - b.y. In FP32 both differences are one f32x2
+// instruction (sm_100 and later pair FP32 operations; each lane is the IEEE
+// round-to-nearest operation, so the lanes are the scalar differences bit
+// for bit): the x and y of a record arrive in a register pair from its
+// 16-byte load, so no register moves are needed. a - b is computed as
+// fma(b, -1, a), whose product is exact and whose one rounding is the
+// subtraction's.
+template <class R> struct XY { R x, y; };
+template <class R> __device__ __forceinline__ XY<R> diff_xy(const R4<R>& a, const R4<R>& b) {
+    if constexpr (sizeof(R) == sizeof(float)) {
+        const float2 d = __ffma2_rn(make_float2(b.x, b.y), make_float2(-1.0f, -1.0f), make_float2(a.x, a.y));
+        return {d.x, d.y};
+    } else {
+        return {a.x - b.x, a.y - b.y};
+    }
+}
+
 // rate pass, fluid candidate j: rd = fma(f, d, rd)
 template <class R>
 __device__ __forceinline__ void rate_fluid_terms(const R4<R>& pi, const R4<R>& vi, const R4<R>& pj,
                                                  const R4<R>& vj, const Phys<R>& p, R& f, R& d) {
-    const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+    const XY<R> rxy = diff_xy(pi, pj);
+    const R rx = rxy.x, ry = rxy.y, rz = pi.z - pj.z;
     R rinv;
     const R r = pair_r_x(dot3(rx, ry, rz, rx, ry, rz), rinv);
     f = grad_factor_x(r, rinv, p);
-    d = dot3(vi.x - vj.x, vi.y - vj.y, vi.z - vj.z, rx, ry, rz);
+    const XY<R> dv = diff_xy(vi, vj);
+    d = dot3(dv.x, dv.y, vi.z - vj.z, rx, ry, rz);
 }
 // rate pass, wall candidate j (wall velocity 0): rb = fma(f, d, rb)
 template <class R>
 __device__ __forceinline__ void rate_wall_terms(const R4<R>& pi, const R4<R>& vi, const R4<R>& pj,
                                                 const Phys<R>& p, R& f, R& d) {
-    const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
+    const XY<R> rxy = diff_xy(pi, pj);
+    const R rx = rxy.x, ry = rxy.y, rz = pi.z - pj.z;
     R rinv;
     const R r = pair_r_x(dot3(rx, ry, rz, rx, ry, rz), rinv);
     f = mul_r(pj.w, grad_factor_x(r, rinv, p));
@@ -165,7 +185,8 @@ __device__ __forceinline__ void rate_wall_terms(const R4<R>& pi, const R4<R>& vi
 template <class R>
 __device__ __forceinline__ void apply_terms(const R4<R>& pi, const R4<R>& pj, R w, const Phys<R>& p, R& f, R& rx,
                                             R& ry, R& rz) {
-    rx = pi.x - pj.x; ry = pi.y - pj.y; rz = pi.z - pj.z;
+    const XY<R> rxy = diff_xy(pi, pj);
+    rx = rxy.x; ry = rxy.y; rz = pi.z - pj.z;
     R rinv;
     const R r = pair_r_x(dot3(rx, ry, rz, rx, ry, rz), rinv);
     f = mul_r(w, grad_factor_x(r, rinv, p));
