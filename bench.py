@@ -74,8 +74,12 @@ NCU_TRAFFIC_PER_PARTICLE: dict = {
 
 
 # Warp instructions per fluid particle of one launch of each neighbour pass,
-# from `ncu --metrics smsp__inst_executed.sum` on the 1M dam break.
-NCU_WARP_INST_PER_PARTICLE: dict = {}
+# from `ncu --metrics smsp__inst_executed.sum` on the 1M dam break (the apply
+# class averages three apply passes and the fused last apply + integrator).
+NCU_WARP_INST_PER_PARTICLE: dict = {
+    "pressure_rate": 46.97e6 / 1024000, "pressure_apply": (3 * 40.93e6 + 44.43e6) / 4 / 1024000,
+    "density_alpha": 48.30e6 / 1024000, "forces_xsph": 51.43e6 / 1024000,
+}
 
 
 def parse():
@@ -316,12 +320,18 @@ def bench_ours(args, rank, world):
     if coop:
         dom_ms, dom_launches = share[dominant]
     else:
-        s.profile_enable(1 << dom_id)
+        # every class bracketed, so every launch runs alone (with one class
+        # bracketed, the pass after it, launched with programmatic stream
+        # serialization, could start beside it and slow it)
+        s.profile_enable((1 << _lib.KERNEL_CLASSES) - 1)
         for _ in range(args.steps):
             flush.zero_()
             s.step(sc.dt)
         torch.cuda.synchronize()
         dom_ms, dom_launches = s.profile_read(dom_id)
+        for k in range(_lib.KERNEL_CLASSES):
+            if k != dom_id:
+                s.profile_read(k)  # forget the other classes' records
         s.profile_enable(0)
     from water_simulation_gb300 import replicas
 
@@ -330,7 +340,7 @@ def bench_ours(args, rank, world):
            "sms": torch.cuda.get_device_properties(local).multi_processor_count,
            "dominant": dominant, "dominant_ms": dom_ms, "dominant_launches": dom_launches,
            "dominant_timed_in": "warm-up steps (passes apart)" if coop else
-                                "as many steps again after the timed ones, with that pass bracketed by CUDA events "
+                                "as many steps again after the timed ones, every pass bracketed by CUDA events "
                                 "(the timed steps run unprofiled)",
            "nb_active": nb_active,
            "block_sizes": {k: tuned[k] for k in ("density_alpha", "pressure_rate", "pressure_apply", "forces_xsph")},
@@ -432,21 +442,10 @@ def bench_batch(steps, n_scenes=64, warmup=3):
             "batched_ms_per_step": ms_batch / steps, "sequential_ms_per_step": ms_seq / steps}
 
 
-def bench_frames(n_frames=24):
-    """sim_cli's frame loop (24 fps) on the settled-puddle scene with the
-    reference's adaptive solvers (4,913 particles; density eta 1e-4, divergence
-    eta 1e-3, at most 100 iterations each): every substep size chosen on the
-    device and both solves run as device-resident loops, one graph launch per
-    frame, against the reference's host loop (max |v| read back before every
-    substep, the mean error after every iteration). Wall time of n_frames
-    frames from rest. Both paths take e^{-d dt} from the same device function,
-    so they take the same substeps and iterations and end in the same state
-    (checked: same_substeps, same_state)."""
-    from water_simulation_gb300 import scenes
+def _frames_run(sc, label, n_frames):
     from water_simulation_gb300.solver import Solver
 
-    sc = scenes.puddle()
-    out = {"workload": "puddle_4913, adaptive solvers, 24 fps", "frames": n_frames}
+    out = {"workload": label, "frames": n_frames}
     final = {}
     for name, graph in (("device", True), ("host_loop", False)):
         cfg = sc.config()
@@ -470,6 +469,27 @@ def bench_frames(n_frames=24):
     a, b = final["device"], final["host_loop"]
     out["same_substeps"] = a[0] == b[0]
     out["same_state"] = bool(np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2]))
+    return out
+
+
+def bench_frames(n_frames=24):
+    """sim_cli's frame loop (24 fps) on the settled-puddle scene: every
+    substep size chosen on the device, one graph launch per frame, against the
+    reference's host loop (max |v| read back before every substep). Wall time
+    of n_frames frames from rest. Both paths take e^{-d dt} from the same
+    device function, so they take the same substeps and iterations and end in
+    the same state (checked: same_substeps, same_state). Two settings: the
+    settled puddle with the reference's adaptive solvers (4,913 particles;
+    density eta 1e-4, divergence eta 1e-3, at most 100 iterations each; both
+    solves run as device-resident loops, the host loop reads the error after
+    every iteration), and, with short substeps, a 16^3 block falling with
+    N(0, 0.5^2) m/s velocities and fixed iterations (4 density, no divergence)
+    over the 6 frames before it reaches the floor."""
+    from water_simulation_gb300 import scenes
+
+    out = _frames_run(scenes.puddle(), "puddle_4913, adaptive solvers, 24 fps", n_frames)
+    block = scenes.falling_block(n_side=(16, 16, 16), velocity_sigma=0.5)
+    out["fixed_iterations"] = _frames_run(block, "falling block 4,096, 4 fixed density iterations, 24 fps", 6)
     return out
 
 
@@ -853,6 +873,24 @@ def bench_ref_cuda(sc, steps, warmup=1):
             "steps": steps, "kind": "reference kernels from its sources, sm_103a, same GPU"}
 
 
+def workload_config(sc, world):
+    """The `config` of both arms' JSON lines (identical for the same workload)."""
+    cells = 1
+    for a in range(3):
+        ext = np.float32(np.float32(sc.domain_max[a]) - np.float32(sc.domain_min[a]))
+        cells *= int(np.ceil(ext / np.float32(2 * np.float32(sc.radius)))) + 2
+    # state and grid bytes a step touches: ~96 B per fluid particle (positions,
+    # velocities, scalars, indices, both buffers), 16 B per wall particle,
+    # 13 B per cell (counts, starts, wall starts, wall mask)
+    touched = 96 * sc.n + 16 * sc.nb + 13 * cells
+    l2 = ("every step touches more than the 129 MB GPU L2 holds; the GPU arm also writes 256 MB before "
+          "every timed step" if touched > 129e6 else
+          "the GPU arm writes 256 MB (more than the 129 MB L2) before every timed step")
+    return {"workload": sc.name, "particles": sc.n, "boundary_particles": sc.nb,
+            "density_iters": sc.max_density_iters, "divergence_iters": sc.max_divergence_iters, "dt": sc.dt,
+            "parallelism": f"replicas x{world}", "l2": l2}
+
+
 def oracle_config(sc):
     """The oracle's configuration of a scene, built without the library (the
     values Scene.config() gives the library's dfsph_config). The stencil is
@@ -914,8 +952,7 @@ def reference_arm(args, rank, world):
         "value": val, "unit": "particle-steps/s",
         "n_gpus": world, "steps": done, "warmup": warm, "ms_per_step": 1e3 * sec / max(done, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": sc.name, "particles": sc.n, "boundary_particles": sc.nb,
-                   "density_iters": sc.max_density_iters, "divergence_iters": sc.max_divergence_iters, "dt": sc.dt},
+        "config": workload_config(sc, world),
         "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": cores, "kind": "port",
                          "sample": f"{done} full steps of the {sc.n}-particle workload (bounded to {budget_s:.0f} s)"},
         "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -954,11 +991,8 @@ def main():
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded lattice + SplitMix64 jitter, water_simulation_gb300/scenes.py)",
-        "config": {"workload": sc.name, "particles": sc.n, "boundary_particles": sc.nb,
-                   "density_iters": sc.max_density_iters, "divergence_iters": sc.max_divergence_iters,
-                   "dt": sc.dt, "parallelism": f"replicas x{world}",
-                   "l2": "flushed before every timed step (256 MB write)",
-                   "threads_per_block": res["block_sizes"], "slot_order": args.slot_order},
+        "config": workload_config(sc, world),
+        "run": {"threads_per_block": res["block_sizes"], "slot_order": args.slot_order},
         "gpu_launches": res["launches"],
         "clocks": res["clocks"],
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",

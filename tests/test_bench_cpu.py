@@ -77,3 +77,15 @@ def test_reference_arm_scene_is_the_benchmark_scene():
     for name, _ in O.OracleConfig._fields_:
         x, y = getattr(c, name), getattr(d, name)
         assert (list(x) == list(y)) if hasattr(x, "__len__") else x == y, name
+
+
+def test_both_arms_carry_the_same_config():
+    """The reference arm's `config` equals the one the GPU arm prints for the
+    same workload (the driver compares them)."""
+    from oracle import oracle as O
+
+    args = argparse.Namespace(workload="puddle", steps=1, warmup=3, gpus=1, impl="reference")
+    line = bench.reference_arm(args, rank=0, world=1)
+    assert line["config"] == bench.workload_config(bench.make_scene("puddle"), 1)
+    big = bench.workload_config(bench.make_scene("dam1m", sampler=O.sample_aabb_boundary), 1)
+    assert big["particles"] == 1024000 and "touches more" in big["l2"]

@@ -754,26 +754,55 @@ public:
         DFSPH_CUDA(cudaMemcpyAsync(tune_ctl_.p, ctl_.p, 3 * sizeof(IterCtl), cudaMemcpyDeviceToDevice, stream_));
         const u32 saved_mask = profile_mask_;
         const bool saved_stepped = stepped_;
-        double best[4] = {1e300, 1e300, 1e300, 1e300};
-        int pick[4] = {bs_[kClasses[0]], bs_[kClasses[1]], bs_[kClasses[2]], bs_[kClasses[3]]};
-        for (const Record& r : records_) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
-        records_.clear();
-        for (int c = 0; c < 3; ++c) {
-            for (int k = 0; k < 4; ++k) bs_[kClasses[k]] = kCandidates[c];
+        profile_mask_ = 0;  // whole steps, unprofiled: passes keep their launch overlap
+        // Every trial step starts from a cold L2, as a step of a large scene
+        // does: a temporary buffer larger than the L2 is written before it.
+        size_t l2 = 0;
+        {
+            int bytes = 0;
+            DFSPH_CUDA(cudaDeviceGetAttribute(&bytes, cudaDevAttrL2CacheSize, device_));
+            l2 = size_t(bytes);
+        }
+        DevBuf<unsigned char> flush;
+        flush.alloc(2 * l2 + (1u << 20));
+        cudaEvent_t ea = take_event(), eb = take_event();
+        // median time of `trials` steps from the snapshot with the current shapes
+        const u32 trials = std::max(steps, 5u);
+        auto time_config = [&]() {
             restore_tuning_state();
             step_once(R(dt), true);  // untimed: first touch of this configuration
-            profile_mask_ = 0;
-            for (int k = 0; k < 4; ++k) profile_mask_ |= 1u << kClasses[k];
-            for (u32 s = 0; s < steps; ++s) step_once(R(dt), true);
-            profile_mask_ = 0;
-            for (int k = 0; k < 4; ++k) {
-                double ms = 0.0;
-                unsigned long long cnt = 0;
-                profile_read(kClasses[k], &ms, &cnt);
-                const double per = cnt ? ms / double(cnt) : 1e300;
-                if (per < best[k]) { best[k] = per; pick[k] = kCandidates[c]; }
+            std::vector<float> t(trials);
+            for (u32 s = 0; s < trials; ++s) {
+                DFSPH_CUDA(cudaMemsetAsync(flush.p, 0, flush.n, stream_));
+                DFSPH_CUDA(cudaEventRecord(ea, stream_));
+                step_once(R(dt), true);
+                DFSPH_CUDA(cudaEventRecord(eb, stream_));
+                DFSPH_CUDA(cudaEventSynchronize(eb));
+                DFSPH_CUDA(cudaEventElapsedTime(&t[s], ea, eb));
+            }
+            std::sort(t.begin(), t.end());
+            return double(t[trials / 2]);
+        };
+        // coordinate descent: each pass in turn takes the launch shape that
+        // gives the shortest whole step with the other passes' shapes fixed;
+        // a shape replaces the current one only when it saves more than 1 %
+        // of the step, more than run-to-run noise
+        int pick[4] = {bs_[kClasses[0]], bs_[kClasses[1]], bs_[kClasses[2]], bs_[kClasses[3]]};
+        double best_ms = time_config();
+        for (int k = 0; k < 4; ++k) {
+            for (int c = 0; c < 3; ++c) {
+                if (kCandidates[c] == pick[k]) continue;
+                bs_[kClasses[k]] = kCandidates[c];
+                const double ms = time_config();
+                if (ms < 0.99 * best_ms) {
+                    best_ms = ms;
+                    pick[k] = kCandidates[c];
+                }
+                bs_[kClasses[k]] = pick[k];
             }
         }
+        free_events_.push_back(ea);
+        free_events_.push_back(eb);
         for (int k = 0; k < 4; ++k) bs_[kClasses[k]] = pick[k];
         restore_tuning_state();
         DFSPH_CUDA(cudaMemcpyAsync(ctl_.p, tune_ctl_.p, 3 * sizeof(IterCtl), cudaMemcpyDeviceToDevice, stream_));
