@@ -484,7 +484,7 @@ def bench_frames(n_frames=24):
     solves run as device-resident loops, the host loop reads the error after
     every iteration), and, with short substeps, a 16^3 block falling with
     N(0, 0.5^2) m/s velocities and fixed iterations (4 density, no divergence)
-    over the 6 frames before it reaches the floor."""
+    for 6 frames."""
     from water_simulation_gb300 import scenes
 
     out = _frames_run(scenes.puddle(), "puddle_4913, adaptive solvers, 24 fps", n_frames)
