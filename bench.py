@@ -68,8 +68,8 @@ FALLBACK_HBM_GBS = 6800.0
 # 1M dam break (one launch per kernel). The traffic of a launch on another
 # workload is scaled by its particle count.
 NCU_TRAFFIC_PER_PARTICLE: dict = {
-    "pressure_rate": 46.1, "pressure_apply": 40.2, "density_alpha": 25.0, "forces_xsph": 38.2,
-    "advect": 37.3, "grid_reorder": 52.7, "grid_scatter": 17.6, "grid_count": 20.7,
+    "pressure_rate": 46.0, "pressure_apply": 40.2, "density_alpha": 24.96, "forces_xsph": 38.1,
+    "grid_reorder": 52.3, "grid_scatter": 17.55, "grid_count": 20.96,
 }
 
 
@@ -393,7 +393,9 @@ def bench_e2e(s, sc, steps):
 def bench_batch(steps, n_scenes=64, warmup=3):
     """64 independent falling-block scenes (2,000-60,000 particles each): one
     batched context replaying a captured CUDA graph of two steps, against 64
-    single-scene contexts stepped one after another with plain launches."""
+    single-scene contexts stepped one after another with plain launches. Also
+    the batched kernels' own time per step, and the fraction of the replayed
+    step that is not kernel time (launch gaps)."""
     import torch
 
     from water_simulation_gb300 import scenes
@@ -420,6 +422,17 @@ def bench_batch(steps, n_scenes=64, warmup=3):
     torch.cuda.synchronize()
     ms_batch = e0.elapsed_time(e1)
     launches_batch = b.kernel_launches() - l0
+    # the kernels' own time per step (every launch bracketed by CUDA events,
+    # which replaces the graph with plain launches): what is left of the
+    # replayed step is launch gaps, the most a single persistent launch of the
+    # whole step could remove
+    from water_simulation_gb300 import _lib
+
+    b.profile_enable((1 << _lib.KERNEL_CLASSES) - 1)
+    b.step(scs[0].dt, steps)
+    torch.cuda.synchronize()
+    kernel_ms = sum(b.profile_read(k)[0] for k in range(_lib.KERNEL_CLASSES))
+    b.profile_enable(0)
     b.close()
     singles = [solver_for(s, stream=stream.cuda_stream) for s in scs]
     for s in singles:
@@ -439,7 +452,9 @@ def bench_batch(steps, n_scenes=64, warmup=3):
             "batched_scene_steps_per_s": n_scenes * steps / (ms_batch * 1e-3),
             "sequential_particle_steps_per_s": n_total * steps / (ms_seq * 1e-3),
             "speedup_vs_sequential": ms_seq / ms_batch, "batched_launches": launches_batch,
-            "batched_ms_per_step": ms_batch / steps, "sequential_ms_per_step": ms_seq / steps}
+            "batched_ms_per_step": ms_batch / steps, "sequential_ms_per_step": ms_seq / steps,
+            "batched_kernel_ms_per_step": kernel_ms / steps,
+            "launch_gap_fraction": max(0.0, 1.0 - kernel_ms / ms_batch)}
 
 
 def _frames_run(sc, label, n_frames):
@@ -675,8 +690,10 @@ def bench_adjoint(graph: bool):
     return res
 
 
-def cpu_sample(sc, steps, threads=0):
-    """The FP32 restatement of the reference step on the host cores."""
+def cpu_sample(sc, seconds=10.0, max_steps=2000, threads=0):
+    """The FP32 restatement of the reference step on the host cores, on a
+    bounded sample: whole steps from the workload's start (after one untimed
+    step) until `seconds` of CPU time have passed."""
     from oracle import oracle as O
 
     c = O.config_from(sc.config())
@@ -686,12 +703,16 @@ def cpu_sample(sc, steps, threads=0):
     cores = L.oracle_max_threads()
     o = O.Oracle(c, sc.fluid, sc.velocity, sc.boundary, precision=32)
     o.step(sc.dt, 1)  # warm the arrays
+    steps = 0
     t0 = time.perf_counter()
-    o.step(sc.dt, steps)
+    while steps < max_steps and time.perf_counter() - t0 < seconds:
+        o.step(sc.dt, 1)
+        steps += 1
     sec = time.perf_counter() - t0
     o.close()
     return {"value": sc.n * steps / sec, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-            "sample": f"{steps} full steps of the {sc.n}-particle workload after 1 untimed step",
+            "sample": f"{steps} full steps of the {sc.n}-particle workload after 1 untimed step "
+                      f"({sec:.1f} s on {cores} threads)",
             "ms_per_step": 1e3 * sec / steps}
 
 
@@ -1034,7 +1055,7 @@ def main():
         line["e2e"] = res["e2e"]
     if rank == 0 and not args.no_cpu:
         try:
-            line["cpu_baseline"] = cpu_sample(sc, 1 if sc.n > 500000 else 3)
+            line["cpu_baseline"] = cpu_sample(sc)
         except Exception as e:  # the baseline is a report, not the product
             line["cpu_baseline"] = {"unavailable": str(e)[:200]}
     if rank == 0 and not args.no_batch:
