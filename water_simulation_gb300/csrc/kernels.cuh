@@ -102,9 +102,19 @@ template <class R> struct NbrSrc {
 // ---------------------------------------------------------------------------
 template <class R> __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
 
-// a / b for b in [1e-9, 1e30]: the fast single-precision divide (2 ulp) where
-// the working type is float, the IEEE divide where it is double.
-__device__ __forceinline__ float fast_div(float a, float b) { return __fdividef(a, b); }
+// a / b for b in [1e-9, 1e30]: a fast approximate quotient where the working
+// type is float, the IEEE divide where it is double.
+// In FP32: a times the approximate reciprocal of b (PTX rcp.approx.ftz.f32).
+// The one caller passes b >= 1e-9, so the reciprocal is never taken of a
+// subnormal; the product is an ordinary multiply, exact for subnormal a.
+// Same results as __fdividef on the 1M-particle dam break (positions and
+// velocities hashed after 55 steps), 2.6 M fewer warp instructions in the
+// XSPH pass.
+__device__ __forceinline__ float fast_div(float a, float b) {
+    float rb;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rb) : "f"(b));
+    return a * rb;
+}
 __device__ __forceinline__ double fast_div(double a, double b) { return a / b; }
 
 template <class R> __device__ __forceinline__ R pair_r(R r2, R& rinv) {
