@@ -77,8 +77,8 @@ NCU_TRAFFIC_PER_PARTICLE: dict = {
 # from `ncu --metrics smsp__inst_executed.sum` on the 1M dam break (the apply
 # class averages three apply passes and the fused last apply + integrator).
 NCU_WARP_INST_PER_PARTICLE: dict = {
-    "pressure_rate": 46.97e6 / 1024000, "pressure_apply": (3 * 40.93e6 + 44.43e6) / 4 / 1024000,
-    "density_alpha": 48.30e6 / 1024000, "forces_xsph": 51.43e6 / 1024000,
+    "pressure_rate": 43.14e6 / 1024000, "pressure_apply": (3 * 35.06e6 + 39.13e6) / 4 / 1024000,
+    "density_alpha": 43.40e6 / 1024000, "forces_xsph": 45.12e6 / 1024000,
 }
 
 

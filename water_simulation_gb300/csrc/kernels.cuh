@@ -100,6 +100,15 @@ template <class R> struct NbrSrc {
 // zero, which is how the reference's explicit self-skips and its r < 1e-12
 // guard (sph_kernels.cuh:29) come out here.
 // ---------------------------------------------------------------------------
+// Minimum resident blocks for __launch_bounds__ of the FP32 density + alpha
+// pass and the fused last apply + integrator: six 256-thread (twelve
+// 128-thread) blocks per SM, which holds them at 40 registers (48 otherwise;
+// measured on the 1M dam break: density + alpha -1.3 us, the fused pass
+// -3 us, step -0.5 %). The XSPH pass spills at 40 registers and runs slower
+// there; the FP64 build and the diagnostic density pass (neighbour counts and
+// candidate-set signatures) are left unbounded.
+template <class R> constexpr int fp32_min_blocks(int lb) { return sizeof(R) == sizeof(float) ? 1536 / lb : 1; }
+
 template <class R> __device__ __forceinline__ R rmax(R a, R b) { return a > b ? a : b; }
 
 // a / b for b in [1e-9, 1e30]: a fast approximate quotient where the working
@@ -894,7 +903,7 @@ __device__ __forceinline__ u32 mix32(u32 x) {
 }
 
 template <class R, bool KAHAN, bool DIAG, int LB, bool MORTON = false>
-__global__ void __launch_bounds__(LB) density_alpha_kernel(
+__global__ void __launch_bounds__(LB, DIAG ? 1 : fp32_min_blocks<R>(LB)) density_alpha_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* __restrict__ vr, R* __restrict__ alpha,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, u32* __restrict__ nbr_f,
     u32* __restrict__ nbr_b, u32* __restrict__ nbr_sig, const u32* __restrict__ id, Tape1<R> tp) {
@@ -1640,7 +1649,7 @@ __global__ void __launch_bounds__(256) advect_kernel(
 // the same buffer). xk_out is the other position buffer, which nothing in
 // this pass reads.
 template <class R, bool COUNT, int LB, bool MORTON = false>
-__global__ void __launch_bounds__(LB) apply_advect_kernel(
+__global__ void __launch_bounds__(LB, fp32_min_blocks<R>(LB)) apply_advect_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* xk_out, R4<R>* __restrict__ vr, const R* __restrict__ kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, Domain<R> d,
     u32* __restrict__ key, u32* __restrict__ rank, u32* __restrict__ count, IterCtl* ctl,
