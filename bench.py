@@ -68,7 +68,7 @@ FALLBACK_HBM_GBS = 6800.0
 # 1M dam break (one launch per kernel). The traffic of a launch on another
 # workload is scaled by its particle count.
 NCU_TRAFFIC_PER_PARTICLE: dict = {
-    "pressure_rate": 46.0, "pressure_apply": 40.2, "density_alpha": 24.96, "forces_xsph": 38.1,
+    "pressure_rate": 46.0, "pressure_apply": 40.2, "density_alpha": 25.02, "forces_xsph": 38.34,
     "grid_reorder": 52.3, "grid_scatter": 17.55, "grid_count": 20.96,
 }
 
@@ -77,8 +77,8 @@ NCU_TRAFFIC_PER_PARTICLE: dict = {
 # from `ncu --metrics smsp__inst_executed.sum` on the 1M dam break (the apply
 # class averages three apply passes and the fused last apply + integrator).
 NCU_WARP_INST_PER_PARTICLE: dict = {
-    "pressure_rate": 43.14e6 / 1024000, "pressure_apply": (3 * 35.06e6 + 39.13e6) / 4 / 1024000,
-    "density_alpha": 43.40e6 / 1024000, "forces_xsph": 45.12e6 / 1024000,
+    "pressure_rate": 43.14e6 / 1024000, "pressure_apply": (3 * 35.06e6 + 39.59e6) / 4 / 1024000,
+    "density_alpha": 43.63e6 / 1024000, "forces_xsph": 45.12e6 / 1024000,
 }
 
 
