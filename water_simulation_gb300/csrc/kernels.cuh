@@ -35,11 +35,10 @@ template <class R> struct Phys {
 // and outputs flushed to zero (PTX rsqrt.approx.ftz.f32). Every caller clamps
 // its argument at 1e-24, and for any float from 1e-24 up neither the argument
 // nor its reciprocal square root (1e12 down to 5e-20) is subnormal, so the
-// flush never applies: the result is the one
-// rsqrtf gives (positions and velocities bit-identical after 40 steps of the
-// 1M-particle dam break), without the handling of subnormal arguments that
-// rsqrtf carries: 3 instructions fewer per pair term, 2.6 M fewer warp
-// instructions per neighbour pass at 1M particles.
+// flush never applies. The results are those of rsqrtf (positions and
+// velocities bit-identical after 40 steps of the 1M-particle dam break),
+// without rsqrtf's handling of subnormal arguments: 3 instructions fewer per
+// pair term, 2.6 M fewer warp instructions per neighbour pass at 1M particles.
 __device__ __forceinline__ float rsqrt_r(float v) {
     float r;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(v));
