@@ -509,9 +509,9 @@ def bench_frames(n_frames=24):
 
 
 def bench_precision(sc, checkpoints=(50, 500)):
-    """Field error of the FP32 step (plain and with Kahan density sums; both
-    with FP64 convergence reductions) against the FP64 build of the same
-    kernels. Every build bins and centres the stencil with the same float
+    """Field error of the FP32 step (plain, with Kahan density sums, and with
+    Kahan density sums and compensated position updates; all with FP64
+    convergence reductions) against the FP64 build of the same kernels. Every build bins and centres the stencil with the same float
     arithmetic, so from identical inputs the builds visit identical neighbour
     sets and differ by rounding only ("one_step_from_same_input"). Along one
     trajectory (the checkpoints) the positions drift apart by rounding, and a
@@ -548,9 +548,10 @@ def bench_precision(sc, checkpoints=(50, 500)):
             out["density_max_rel_without_flips"] = float(rel[~mask].max()) if (~mask).any() else 0.0
         return out, rel
 
-    ctxs = {name: solver_for(sc, precision=prec, diagnostics=(name != "fp32_kahan"))
+    ctxs = {name: solver_for(sc, precision=prec, diagnostics=name in ("fp64", "fp32"))
             for name, prec in (("fp64", _lib.PRECISION_FP64), ("fp32", _lib.PRECISION_FP32),
-                               ("fp32_kahan", _lib.PRECISION_FP32_KAHAN))}
+                               ("fp32_kahan", _lib.PRECISION_FP32_KAHAN),
+                               ("fp32_compensated", _lib.PRECISION_FP32_COMPENSATED))}
     # lockstep to the first checkpoint, candidate-set signatures compared every step
     first = checkpoints[0]
     flipped = np.zeros(sc.n, bool)
@@ -584,7 +585,7 @@ def bench_precision(sc, checkpoints=(50, 500)):
     near = grid[keys] | flipped
     f = {name: snap(s) for name, s in ctxs.items()}
     out = {}
-    for name in ("fp32", "fp32_kahan"):
+    for name in ("fp32", "fp32_kahan", "fp32_compensated"):
         e, rel = errors(f[name], f["fp64"], flipped)
         e["density_max_rel_away_from_flips"] = float(rel[~near].max()) if (~near).any() else 0.0
         e["over_1e-4"] = int((rel > 1e-4).sum())
@@ -608,12 +609,22 @@ def bench_precision(sc, checkpoints=(50, 500)):
     e1, _ = errors(probe["fp32"], probe["fp64"])
     e1["candidate_sets_differ"] = int((probe["fp32"]["sig"] != probe["fp64"]["sig"]).sum())
     out[f"one_step_from_same_input_at_step_{first}"] = e1
-    # the rest of the trajectory
+    # the rest of the trajectory, each form's steps timed with CUDA events
+    import torch
+
+    stream = torch.cuda.current_stream()
+    ms_per_step = {}
     for c in checkpoints[1:]:
-        for s in ctxs.values():
+        for name, s in ctxs.items():
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
             s.step(sc.dt, c - first)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms_per_step[name] = e0.elapsed_time(e1) / (c - first)
         g = {name: snap(s) for name, s in ctxs.items()}
-        for name in ("fp32", "fp32_kahan"):
+        for name in ("fp32", "fp32_kahan", "fp32_compensated"):
             out[f"{name}_at_{c}_steps"] = errors(g[name], g["fp64"])[0]
     for s in ctxs.values():
         s.close()
@@ -631,6 +642,8 @@ def bench_precision(sc, checkpoints=(50, 500)):
         else None
     out["steps"] = first
     out["checkpoints"] = list(checkpoints)
+    if len(checkpoints) > 1:
+        out["ms_per_step"] = {"steps": f"{first + 1}-{checkpoints[-1]}", **ms_per_step}
     out["lockstep_wall_s"] = lockstep_s
     out["reference"] = "FP64 build of the same kernels (float cell arithmetic, as the FP32 build)"
     return out

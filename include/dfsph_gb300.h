@@ -43,6 +43,14 @@ extern "C" {
 #define DFSPH_PRECISION_FP32        0  /* plain FP32                                        */
 #define DFSPH_PRECISION_FP32_KAHAN  1  /* FP32 state, compensated density sums               */
 #define DFSPH_PRECISION_FP64        2  /* the same kernels instantiated in FP64 (GPU oracle) */
+/* FP32 state with compensated density sums and compensated position updates
+ * (no counterpart in the reference): the integrator keeps, per particle, what
+ * rounding x + v dt to float dropped and adds it back at the next step
+ * (Kahan summation over the steps), so position rounding no longer
+ * accumulates. The carries restart at zero on every new fluid state
+ * (dfsph_set_fluid*, dfsph_step_store, dfsph_load_state) and are not part of
+ * the state file. The adjoint refuses such a context (DFSPH_ERR_STATE). */
+#define DFSPH_PRECISION_FP32_COMPENSATED 3
 
 /* ---- configuration ----------------------------------------------------- */
 /* Mirrors water::solvers::DFSPHSolver::Config

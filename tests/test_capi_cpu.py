@@ -114,11 +114,28 @@ def test_create_rejects_invalid_configs_without_touching_a_device():
     lib.dfsph_config_init(ctypes.byref(c))
     c.precision = 7
     assert lib.dfsph_create(ctypes.byref(c), 0, None, ctypes.byref(out)) == _lib.ERR_INVALID_ARGUMENT
+    assert b"precision" in lib.dfsph_last_error(None)
+    c.precision = _lib.PRECISION_FP32_COMPENSATED + 1
+    assert lib.dfsph_create(ctypes.byref(c), 0, None, ctypes.byref(out)) == _lib.ERR_INVALID_ARGUMENT
+    assert b"precision" in lib.dfsph_last_error(None)
     lib.dfsph_config_init(ctypes.byref(c))
     c.smoothing_length = 1e-6  # far more than 2^32 cells
     assert lib.dfsph_create(ctypes.byref(c), 0, None, ctypes.byref(out)) == _lib.ERR_INVALID_ARGUMENT
     assert not out.value
     assert lib.dfsph_create(None, 0, None, ctypes.byref(out)) == _lib.ERR_INVALID_ARGUMENT
+
+
+def test_compensated_precision_passes_config_validation():
+    lib = _lib.load()
+    out = ctypes.c_void_p()
+    c = _lib.DfsphConfig()
+    lib.dfsph_config_init(ctypes.byref(c))
+    c.precision = _lib.PRECISION_FP32_COMPENSATED
+    rc = lib.dfsph_create(ctypes.byref(c), 0, None, ctypes.byref(out))
+    if rc != 0:
+        assert b"precision" not in lib.dfsph_last_error(None)
+    else:
+        lib.dfsph_destroy(out)
 
 
 def test_null_context_calls_fail_cleanly():

@@ -27,6 +27,7 @@ MEM_DEVICE = 1
 PRECISION_FP32 = 0
 PRECISION_FP32_KAHAN = 1
 PRECISION_FP64 = 2
+PRECISION_FP32_COMPENSATED = 3
 
 ORDER_CELL_KEY = 0
 ORDER_MORTON = 1

@@ -98,7 +98,7 @@ int dfsph_create(const dfsph_config* cfg, int device, void* stream, dfsph_ctx** 
             g_create_error = "dfsph_create: domain_max must exceed domain_min on every axis";
             return DFSPH_ERR_INVALID_ARGUMENT;
         }
-    if (cfg->precision > DFSPH_PRECISION_FP64) {
+    if (cfg->precision > DFSPH_PRECISION_FP32_COMPENSATED) {
         g_create_error = "dfsph_create: unknown precision";
         return DFSPH_ERR_INVALID_ARGUMENT;
     }

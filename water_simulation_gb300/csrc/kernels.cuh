@@ -1567,14 +1567,32 @@ template <class R> struct Domain {
     R lox, loy, loz, hix, hiy, hiz;
 };
 
+__device__ __forceinline__ float add_r(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_r(double a, double b) { return __dadd_rn(a, b); }
+
+// x + dx with the rounding error of earlier updates carried in c (Kahan
+// summation over the steps): the position in the working type stays the
+// rounded sum, c holds what that rounding dropped, and the next update adds
+// it back. Every operation is written as an explicit rounding.
+template <class R> __device__ __forceinline__ R compensated_add(R x, R dx, R& c) {
+    const R y = sub_r(dx, c);
+    const R t = add_r(x, y);
+    c = sub_r(sub_r(t, x), y);
+    return t;
+}
+
 // One particle of the integrator: writes v and x (to xk_out), the next
 // step's cell key and rank when COUNT, the clamp mask when recording; returns
-// the bits of |v| (non-negative floats order as integers).
-template <class R, bool COUNT, bool MORTON = false>
+// the bits of |v| (non-negative floats order as integers). COMP: the position
+// update is compensated (DFSPH_PRECISION_FP32_COMPENSATED), its carries kept
+// per particle in xc in the original particle order (id = original index of
+// slot i); a clamped component restarts its carry at zero.
+template <class R, bool COUNT, bool MORTON = false, bool COMP = false>
 __device__ __forceinline__ u32 integrate_particle(int i, R4<R> v, const R4<R>& x, R dt, const Domain<R>& d,
                                                   const GridDev<R>& g, R4<R>* __restrict__ vr, R4<R>* xk_out,
                                                   u32* __restrict__ key, u32* __restrict__ rank,
-                                                  u32* __restrict__ count, unsigned char* __restrict__ tape_mask) {
+                                                  u32* __restrict__ count, unsigned char* __restrict__ tape_mask,
+                                                  const u32* __restrict__ id = nullptr, R4<R>* __restrict__ xc = nullptr) {
     // mask bits (recorded for the adjoint): 0-2 position clamped on x/y/z,
     // 3-5 velocity component zeroed, 6 speed clamped
     u32 mk = 0;
@@ -1585,7 +1603,20 @@ __device__ __forceinline__ u32 integrate_particle(int i, R4<R> v, const R4<R>& x
         v.x *= s; v.y *= s; v.z *= s;
         mk |= 64u;
     }
-    R px = x.x + v.x * dt, py = x.y + v.y * dt, pz = x.z + v.z * dt;
+    R px, py, pz;
+    R4<R> c{};
+    u32 oid = 0;
+    if constexpr (COMP) {
+        oid = id[i];
+        c = xc[oid];
+        px = compensated_add(x.x, mul_r(v.x, dt), c.x);
+        py = compensated_add(x.y, mul_r(v.y, dt), c.y);
+        pz = compensated_add(x.z, mul_r(v.z, dt), c.z);
+    } else {
+        px = x.x + v.x * dt;
+        py = x.y + v.y * dt;
+        pz = x.z + v.z * dt;
+    }
     const R eps = R(1e-3);
     if (px < d.lox + eps) { px = d.lox + eps; mk |= 1u; if (v.x < R(0)) { v.x = R(0); mk |= 8u; } }
     if (py < d.loy + eps) { py = d.loy + eps; mk |= 2u; if (v.y < R(0)) { v.y = R(0); mk |= 16u; } }
@@ -1593,6 +1624,12 @@ __device__ __forceinline__ u32 integrate_particle(int i, R4<R> v, const R4<R>& x
     if (px > d.hix - eps) { px = d.hix - eps; mk |= 1u; if (v.x > R(0)) { v.x = R(0); mk |= 8u; } }
     if (py > d.hiy - eps) { py = d.hiy - eps; mk |= 2u; if (v.y > R(0)) { v.y = R(0); mk |= 16u; } }
     if (pz > d.hiz - eps) { pz = d.hiz - eps; mk |= 4u; if (v.z > R(0)) { v.z = R(0); mk |= 32u; } }
+    if constexpr (COMP) {
+        if (mk & 1u) c.x = R(0);
+        if (mk & 2u) c.y = R(0);
+        if (mk & 4u) c.z = R(0);
+        xc[oid] = c;
+    }
     if (tape_mask) tape_mask[i] = static_cast<unsigned char>(mk);
     vr[i] = {v.x, v.y, v.z, v.w};
     xk_out[i] = {px, py, pz, R(0)};
@@ -1628,11 +1665,12 @@ __device__ __forceinline__ void max_velocity_epilogue(bool valid, u32 vbits, u32
     }
 }
 
-template <class R, bool COUNT, bool MORTON = false>
+template <class R, bool COUNT, bool MORTON = false, bool COMP = false>
 __global__ void __launch_bounds__(256) advect_kernel(
     int n, const R4<R>* xk, R4<R>* xk_out, R4<R>* __restrict__ vr, StepDt<R> sd, Domain<R> d, GridDev<R> g,
     u32* __restrict__ key, u32* __restrict__ rank, u32* __restrict__ count, IterCtl* ctl,
-    u32* __restrict__ maxv_scene, R4<R>* __restrict__ tape_v, unsigned char* __restrict__ tape_mask) {
+    u32* __restrict__ maxv_scene, R4<R>* __restrict__ tape_v, unsigned char* __restrict__ tape_mask,
+    const u32* __restrict__ id, R4<R>* __restrict__ xc) {
     pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const R dt = step_dt(sd);
@@ -1641,7 +1679,8 @@ __global__ void __launch_bounds__(256) advect_kernel(
     if (i < n) {
         const R4<R> v = vr[i];
         if (tape_v) tape_v[i] = v;
-        vbits = integrate_particle<R, COUNT, MORTON>(i, v, xk[i], dt, d, g, vr, xk_out, key, rank, count, tape_mask);
+        vbits = integrate_particle<R, COUNT, MORTON, COMP>(i, v, xk[i], dt, d, g, vr, xk_out, key, rank, count,
+                                                           tape_mask, id, xc);
         scene = scene_of(g, i);
     }
     max_velocity_epilogue<256>(i < n, vbits, scene, ctl, maxv_scene);
@@ -1652,12 +1691,12 @@ __global__ void __launch_bounds__(256) advect_kernel(
 // (same values as the two passes: the apply pass's velocity, positions from
 // the same buffer). xk_out is the other position buffer, which nothing in
 // this pass reads.
-template <class R, bool COUNT, int LB, bool MORTON = false>
+template <class R, bool COUNT, int LB, bool MORTON = false, bool COMP = false>
 __global__ void __launch_bounds__(LB, fp32_min_blocks<R>(LB)) apply_advect_kernel(
     int n, const R4<R>* __restrict__ xk, R4<R>* xk_out, R4<R>* __restrict__ vr, const R* __restrict__ kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, Domain<R> d,
     u32* __restrict__ key, u32* __restrict__ rank, u32* __restrict__ count, IterCtl* ctl,
-    u32* __restrict__ maxv_scene) {
+    u32* __restrict__ maxv_scene, const u32* __restrict__ id, R4<R>* __restrict__ xc) {
     pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const R dt = step_dt(sd);
@@ -1665,8 +1704,8 @@ __global__ void __launch_bounds__(LB, fp32_min_blocks<R>(LB)) apply_advect_kerne
     u32 scene = 0xffffffffu;
     if (i < n) {
         const R4<R> v = apply_velocity<R, MORTON>(i, xk, vr, kap, cs, g, p, bd, dt);
-        vbits = integrate_particle<R, COUNT, MORTON>(i, v, ld(xk + i), dt, d, g, vr, xk_out, key, rank, count,
-                                                     nullptr);
+        vbits = integrate_particle<R, COUNT, MORTON, COMP>(i, v, ld(xk + i), dt, d, g, vr, xk_out, key, rank,
+                                                           count, nullptr, id, xc);
         scene = scene_of(g, i);
     }
     max_velocity_epilogue<LB>(i < n, vbits, scene, ctl, maxv_scene);

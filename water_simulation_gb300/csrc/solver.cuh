@@ -166,6 +166,10 @@ public:
         }
         bcs_.alloc(size_t(cells1_) + 1);
         bmask_.alloc(std::max<size_t>(geom_.total, 1));
+        if (comp_) {
+            xc_.alloc(std::max(cap_, 1u));
+            DFSPH_CUDA(cudaMemsetAsync(xc_.p, 0, size_t(std::max(cap_, 1u)) * sizeof(V4), stream_));
+        }
         if (cfg_.slot_order == DFSPH_ORDER_MORTON) {
             // the fluid slots follow the Morton order of the cells; the wall
             // grid (gb_) keeps the x-major order
@@ -226,6 +230,11 @@ public:
     // (the kernels' MORTON instantiation) and std::false_type otherwise.
     template <class F> void with_slot_order(F&& f) {
         if (g_.rank) f(std::true_type{});
+        else f(std::false_type{});
+    }
+    // the integrator's instantiations: compensated position update or not
+    template <class F> void with_compensation(bool on, F&& f) {
+        if (on) f(std::true_type{});
         else f(std::false_type{});
     }
 
@@ -295,6 +304,7 @@ public:
             launch_import(n, pos, v, xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
         }
         counts_valid_ = false;
+        reset_compensation();
         have_state_ = true;
     }
 
@@ -409,6 +419,7 @@ public:
         if (n == 0) return;  // dfsph.cu:121-122
         launch_import(n, pos, vel, xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
         counts_valid_ = false;
+        reset_compensation();
         have_state_ = true;
         step_once(R(dt), /*count_next=*/false);
         launch(DFSPH_KERNEL_IO, export_kernel<R>, blocks_for(n, 256), 256, int(n), id_[ci_].p, xk_[cx_].p,
@@ -732,6 +743,7 @@ public:
         DFSPH_CUDA(cudaStreamSynchronize(stream_));
         stepped_ = h.stepped != 0;
         counts_valid_ = false;
+        reset_compensation();
         have_state_ = true;
     }
 
@@ -752,6 +764,10 @@ public:
         launch(DFSPH_KERNEL_IO, save_state_kernel<R>, blocks_for(n, 256), 256, int(n), id_[ci_].p, xk_[cx_].p,
                vr_[cv_].p, tune_ck_.p, tune_ck_.p + n);
         DFSPH_CUDA(cudaMemcpyAsync(tune_ctl_.p, ctl_.p, 3 * sizeof(IterCtl), cudaMemcpyDeviceToDevice, stream_));
+        if (comp_) {
+            if (tune_xc_.n < n) tune_xc_.alloc(n);
+            DFSPH_CUDA(cudaMemcpyAsync(tune_xc_.p, xc_.p, n * sizeof(V4), cudaMemcpyDeviceToDevice, stream_));
+        }
         const u32 saved_mask = profile_mask_;
         const bool saved_stepped = stepped_;
         profile_mask_ = 0;  // whole steps, unprofiled: passes keep their launch overlap
@@ -912,6 +928,7 @@ public:
         launch(DFSPH_KERNEL_IO, load_state_kernel<R>, nb, 256, int(n), (const V4*)xg_.p, (const V4*)vg_.p,
                xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
         counts_valid_ = false;
+        reset_compensation();
         have_state_ = true;
     }
 
@@ -1070,11 +1087,16 @@ private:
         drop_pending_counts();
         launch(DFSPH_KERNEL_IO, load_state_kernel<R>, blocks_for(n, 256), 256, int(n), (const V4*)tune_ck_.p,
                (const V4*)(tune_ck_.p + n), xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
+        if (comp_)
+            DFSPH_CUDA(cudaMemcpyAsync(xc_.p, tune_xc_.p, n * sizeof(V4), cudaMemcpyDeviceToDevice, stream_));
         counts_valid_ = false;
     }
 
     void check_adjoint_config() const {
         if (scenes_ != 1) throw Error(DFSPH_ERR_STATE, "the adjoint steps one scene");
+        if (comp_)
+            throw Error(DFSPH_ERR_STATE, "the adjoint differentiates the FP32, FP32_KAHAN or FP64 step, not the "
+                                         "compensated position update of FP32_COMPENSATED");
         if (g_.rank) throw Error(DFSPH_ERR_STATE, "the adjoint needs the x-major slot order");
         if ((cfg_.max_density_iters > 0 && cfg_.eta_density > 0.0f) ||
             (cfg_.max_divergence_iters > 0 && cfg_.eta_divergence > 0.0f))
@@ -1325,6 +1347,12 @@ private:
         bool count;
         bool done;
     };
+    // the integrator's compensation carries when this step uses them
+    const u32* comp_id() const { return comp_ ? id_[ci_].p : nullptr; }
+    V4* comp_xc() const { return comp_ ? xc_.p : nullptr; }
+    void reset_compensation() {
+        if (comp_ && cap_) DFSPH_CUDA(cudaMemsetAsync(xc_.p, 0, size_t(cap_) * sizeof(V4), stream_));
+    }
 
     // A neighbour pass at the tuned block size: the instantiation bounded by
     // 256 threads for 256-thread blocks, the one bounded by 128 otherwise
@@ -1648,16 +1676,19 @@ private:
             if (fa && !adaptive && it + 1 == max_iters && cx_ != fa->cx0) {
                 with_slot_order([&](auto order) {
                     constexpr bool M = decltype(order)::value;
-                    if (fa->count)
-                        launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, apply_advect_kernel<R, true, 128, M>,
-                                    apply_advect_kernel<R, true, 256, M>, n, (const V4*)xout, xk_[cx_ ^ 1].p,
-                                    vr_[cv_].p, (const R*)kap_it, cs, g_, phys_, bdev(), sd, fa->d, key_.p, rank_.p,
-                                    count_.p, ctl_.p, fa->mvs);
-                    else
-                        launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, apply_advect_kernel<R, false, 128, M>,
-                                    apply_advect_kernel<R, false, 256, M>, n, (const V4*)xout, xk_[cx_ ^ 1].p,
-                                    vr_[cv_].p, (const R*)kap_it, cs, g_, phys_, bdev(), sd, fa->d, key_.p, rank_.p,
-                                    count_.p, ctl_.p, fa->mvs);
+                    with_compensation(comp_, [&](auto comp) {
+                        constexpr bool C = decltype(comp)::value;
+                        if (fa->count)
+                            launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, apply_advect_kernel<R, true, 128, M, C>,
+                                        apply_advect_kernel<R, true, 256, M, C>, n, (const V4*)xout, xk_[cx_ ^ 1].p,
+                                        vr_[cv_].p, (const R*)kap_it, cs, g_, phys_, bdev(), sd, fa->d, key_.p,
+                                        rank_.p, count_.p, ctl_.p, fa->mvs, comp_id(), comp_xc());
+                        else
+                            launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, apply_advect_kernel<R, false, 128, M, C>,
+                                        apply_advect_kernel<R, false, 256, M, C>, n, (const V4*)xout,
+                                        xk_[cx_ ^ 1].p, vr_[cv_].p, (const R*)kap_it, cs, g_, phys_, bdev(), sd, fa->d,
+                                        key_.p, rank_.p, count_.p, ctl_.p, fa->mvs, comp_id(), comp_xc());
+                    });
                 });
                 cx_ ^= 1;
                 fa->done = true;
@@ -1875,7 +1906,7 @@ private:
         counts_valid_ = false;
         // 2. density + alpha (dfsph.cu:137-186)
         const BoundaryDev bd = bdev();
-        const bool kahan = cfg_.precision == DFSPH_PRECISION_FP32_KAHAN;
+        const bool kahan = cfg_.precision == DFSPH_PRECISION_FP32_KAHAN || comp_;
         const u32* idn = id_[ci_].p;
         with_slot_order([&](auto order) {
             constexpr bool M = decltype(order)::value;
@@ -1930,16 +1961,22 @@ private:
         const V4* xin = xk_[cx_].p;
         V4* xout = cx_ != cx0 ? xk_[cx_ ^ 1].p : xk_[cx_].p;
         cx_ = cx0;
+        // taped steps (the adjoint's replays) never compensate: the adjoint
+        // refuses DFSPH_PRECISION_FP32_COMPENSATED contexts
+        const bool comp = comp_ && !tp;
         with_slot_order([&](auto order) {
             constexpr bool M = decltype(order)::value;
-            if (count_next)
-                launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, true, M>, blocks_for(n, 256), 256, n, xin, xout,
-                       vr_[cv_].p, sd, dom, g_, key_.p, rank_.p, count_.p, ctl_.p, mvs, tp ? tp->va : nullptr,
-                       tp ? tp->amask : nullptr);
-            else
-                launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, false, M>, blocks_for(n, 256), 256, n, xin, xout,
-                       vr_[cv_].p, sd, dom, g_, key_.p, rank_.p, count_.p, ctl_.p, mvs, tp ? tp->va : nullptr,
-                       tp ? tp->amask : nullptr);
+            with_compensation(comp, [&](auto cflag) {
+                constexpr bool C = decltype(cflag)::value;
+                if (count_next)
+                    launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, true, M, C>, blocks_for(n, 256), 256, n, xin, xout,
+                           vr_[cv_].p, sd, dom, g_, key_.p, rank_.p, count_.p, ctl_.p, mvs, tp ? tp->va : nullptr,
+                           tp ? tp->amask : nullptr, comp ? comp_id() : nullptr, comp ? comp_xc() : nullptr);
+                else
+                    launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, false, M, C>, blocks_for(n, 256), 256, n, xin, xout,
+                           vr_[cv_].p, sd, dom, g_, key_.p, rank_.p, count_.p, ctl_.p, mvs, tp ? tp->va : nullptr,
+                           tp ? tp->amask : nullptr, comp ? comp_id() : nullptr, comp ? comp_xc() : nullptr);
+            });
         });
         if (count_next) counts_valid_ = true;
     }
@@ -2029,6 +2066,11 @@ private:
     int coop_ok_[2] = {0, 0};
     DevBuf<IterCtl> probe_ctl_;  // written by the no-iteration launches of verify_cooperative
     bool fuse_advect_ = true;  // last density iteration carries the integrator when it can
+    // DFSPH_PRECISION_FP32_COMPENSATED: the integrator's per-particle carries
+    // (original particle order), zero on every new fluid state
+    const bool comp_ = cfg_.precision == DFSPH_PRECISION_FP32_COMPENSATED;
+    DevBuf<V4> xc_;
+    DevBuf<V4> tune_xc_;
     DevBuf<V4> tune_ck_;
     DevBuf<IterCtl> tune_ctl_;
     // threads per block of each kernel class (the neighbour passes are tuned;
