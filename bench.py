@@ -354,7 +354,9 @@ def bench_ours(args, rank, world):
 
 
 def bench_e2e(s, sc, steps):
-    """Host buffers in, host buffers out, every step, through the C ABI."""
+    """Host buffers in, host buffers out, every step, through the C ABI:
+    dfsph_set_fluid from page-locked x and v, one dfsph_step, dfsph_get_state
+    back into the same arrays (the next step's input)."""
     import torch
 
     from water_simulation_gb300 import _lib
@@ -370,9 +372,7 @@ def bench_e2e(s, sc, steps):
         s._check(lib.dfsph_set_fluid(s._ctx, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(v.data_ptr()), sc.n,
                                      _lib.MEM_HOST))
         s.step(sc.dt)
-        s._check(lib.dfsph_get_field(s._ctx, _lib.FIELD_POSITION, ctypes.c_void_p(x.data_ptr()), nbytes,
-                                     _lib.MEM_HOST))
-        s._check(lib.dfsph_get_field(s._ctx, _lib.FIELD_VELOCITY, ctypes.c_void_p(v.data_ptr()), nbytes,
+        s._check(lib.dfsph_get_state(s._ctx, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(v.data_ptr()),
                                      _lib.MEM_HOST))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -380,9 +380,7 @@ def bench_e2e(s, sc, steps):
         s._check(lib.dfsph_set_fluid(s._ctx, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(v.data_ptr()), sc.n,
                                      _lib.MEM_HOST))
         s.step(sc.dt)
-        s._check(lib.dfsph_get_field(s._ctx, _lib.FIELD_POSITION, ctypes.c_void_p(x.data_ptr()), nbytes,
-                                     _lib.MEM_HOST))
-        s._check(lib.dfsph_get_field(s._ctx, _lib.FIELD_VELOCITY, ctypes.c_void_p(v.data_ptr()), nbytes,
+        s._check(lib.dfsph_get_state(s._ctx, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(v.data_ptr()),
                                      _lib.MEM_HOST))
     torch.cuda.synchronize()
     sec = time.perf_counter() - t0

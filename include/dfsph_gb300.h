@@ -244,6 +244,14 @@ int dfsph_step_frames(dfsph_ctx* ctx, const dfsph_frame_config* fc, uint32_t n_f
  * in place by a kernel; other host memory receives a copy. Returns when the
  * data is in dst. */
 int dfsph_get_field(dfsph_ctx* ctx, int field, void* dst, size_t dst_bytes, int mem);
+/* Positions and velocities (float[3n] each, original order; either pointer may
+ * be NULL) in one call: the host copies of the ParticleStore arrays that the
+ * reference's sim_cli makes after a frame (apps/sim_cli/main.cpp:186-189,
+ * positions there). No counterpart in the reference's API. Bound for
+ * page-locked 16-byte-aligned host memory, both are written in place by one
+ * kernel with one synchronisation; otherwise as two dfsph_get_field calls.
+ * Returns when the data is in pos and vel. */
+int dfsph_get_state(dfsph_ctx* ctx, float* pos, float* vel, int mem);
 int dfsph_get_scalar(dfsph_ctx* ctx, int which, double* out);
 
 /* Per-kernel device timing with CUDA events on the context's stream (no

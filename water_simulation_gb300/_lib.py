@@ -140,6 +140,7 @@ _SIGNATURES = [
     ("dfsph_step", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_uint32]),
     ("dfsph_step_store", ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, ctypes.c_float, _P, _P, _P, _P]),
     ("dfsph_get_field", ctypes.c_int, [_P, ctypes.c_int, _P, ctypes.c_size_t, ctypes.c_int]),
+    ("dfsph_get_state", ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
     ("dfsph_get_scalar", ctypes.c_int, [_P, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("dfsph_synchronize", ctypes.c_int, [_P]),
     ("dfsph_set_wait_limit", ctypes.c_int, [_P, ctypes.c_uint64]),

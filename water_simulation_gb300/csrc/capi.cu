@@ -229,6 +229,15 @@ int dfsph_step_store(dfsph_ctx* ctx, float* pos, float* vel, uint32_t n, float d
     });
 }
 
+int dfsph_get_state(dfsph_ctx* ctx, float* pos, float* vel, int mem) {
+    if (!ctx || (mem != DFSPH_MEM_HOST && mem != DFSPH_MEM_DEVICE)) return DFSPH_ERR_INVALID_ARGUMENT;
+    return guarded(ctx, [&] {
+        cudaSetDevice(ctx->device);
+        ctx->solver->get_state(pos, vel, mem);
+        ctx->solver->check_device_status();
+    });
+}
+
 int dfsph_get_field(dfsph_ctx* ctx, int field, void* dst, size_t dst_bytes, int mem) {
     if (!ctx || !dst || (mem != DFSPH_MEM_HOST && mem != DFSPH_MEM_DEVICE)) return DFSPH_ERR_INVALID_ARGUMENT;
     return guarded(ctx, [&] {

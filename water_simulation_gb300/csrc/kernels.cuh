@@ -714,6 +714,39 @@ __device__ __forceinline__ void store_triples(float* __restrict__ dst, int base,
     if (t < nf - 4 * n4) dst[3 * size_t(base) + 4 * n4 + t] = tile[4 * n4 + t];
 }
 
+// Positions and velocities in one pass to page-locked host memory (original
+// order; either output may be null): export_mapped_kernel for both fields
+// from one inverse permutation.
+template <class R>
+__global__ void __launch_bounds__(256) export_state_mapped_kernel(int n, const u32* __restrict__ inv,
+                                                                  const R4<R>* __restrict__ xk,
+                                                                  const R4<R>* __restrict__ vr,
+                                                                  float* __restrict__ pos, float* __restrict__ vel) {
+    __shared__ __align__(16) float tp[3 * 256];
+    __shared__ __align__(16) float tv[3 * 256];
+    const int base = blockIdx.x * 256;
+    const int cnt = min(256, n - base);
+    const int t = threadIdx.x;
+    if (t < cnt) {
+        const u32 s = inv[base + t];
+        if (pos) {
+            const R4<R> x = xk[s];
+            tp[3 * t] = float(x.x);
+            tp[3 * t + 1] = float(x.y);
+            tp[3 * t + 2] = float(x.z);
+        }
+        if (vel) {
+            const R4<R> v = vr[s];
+            tv[3 * t] = float(v.x);
+            tv[3 * t + 1] = float(v.y);
+            tv[3 * t + 2] = float(v.z);
+        }
+    }
+    __syncthreads();
+    if (pos) store_triples(pos, base, cnt, tp);
+    if (vel) store_triples(vel, base, cnt, tv);
+}
+
 // import_kernel on caller memory read in place (vel null: zero velocities)
 template <class R>
 __global__ void __launch_bounds__(256) import_mapped_kernel(int n, const float* __restrict__ pos,

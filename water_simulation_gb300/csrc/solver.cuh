@@ -497,6 +497,27 @@ public:
         }
     }
 
+    // Positions and velocities (original order, float3 each; either may be
+    // null): one inverse permutation, one export pass and one
+    // synchronisation when both destinations are page-locked host memory;
+    // otherwise the two fields one after the other.
+    void get_state(float* pos, float* vel, int mem) override {
+        const size_t n = n_;
+        if (n == 0 || (!pos && !vel)) return;
+        float* mp = pos && mem == DFSPH_MEM_HOST ? const_cast<float*>(mapped_host(pos)) : nullptr;
+        float* mv = vel && mem == DFSPH_MEM_HOST ? const_cast<float*>(mapped_host(vel)) : nullptr;
+        if ((!pos || mp) && (!vel || mv)) {
+            u32* inv = static_cast<u32*>(scratch_bytes(n * sizeof(u32)));
+            launch(DFSPH_KERNEL_IO, invert_kernel, blocks_for(n, 256), 256, int(n), (const u32*)id_[ci_].p, inv);
+            launch(DFSPH_KERNEL_IO, export_state_mapped_kernel<R>, blocks_for(n, 256), 256, int(n), (const u32*)inv,
+                   (const V4*)xk_[cx_].p, (const V4*)vr_[cv_].p, mp, mv);
+            DFSPH_CUDA(cudaStreamSynchronize(stream_));
+            return;
+        }
+        if (pos) get_field(DFSPH_FIELD_POSITION, pos, 3 * n * sizeof(float), mem);
+        if (vel) get_field(DFSPH_FIELD_VELOCITY, vel, 3 * n * sizeof(float), mem);
+    }
+
     // The float particle fields written in place to page-locked host memory
     // (export_mapped_kernel, in original order); false for other fields or
     // memory, which take the staging copy.

@@ -29,6 +29,7 @@ struct SolverBase {
     virtual void step_store(float* pos, float* vel, std::uint32_t n, float dt, float* density, float* alpha,
                             float* kappa, float* density_adv) = 0;
     virtual void get_field(int field, void* dst, std::size_t bytes, int mem) = 0;
+    virtual void get_state(float* pos, float* vel, int mem) = 0;
     virtual double get_scalar(int which) = 0;
     virtual void synchronize() = 0;
     // Throws DFSPH_ERR_DEVICE_TIMEOUT (and clears the word) when a bounded

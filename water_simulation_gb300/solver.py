@@ -197,6 +197,22 @@ class Solver:
                                               out.nbytes, _lib.MEM_HOST))
         return out
 
+    def get_state(self, pos: np.ndarray | None, vel: np.ndarray | None = None) -> None:
+        """Positions and velocities into host float32 arrays of shape (n, 3)
+        (either may be None) with one call; page-locked arrays are written in
+        place by one kernel."""
+        for a in (pos, vel):
+            if a is not None and (a.dtype != np.float32 or a.size < 3 * self.n or not a.flags.c_contiguous):
+                raise ValueError("pos / vel must be C-contiguous float32 arrays of at least 3n values")
+        p = ctypes.c_void_p(pos.ctypes.data) if pos is not None else None
+        v = ctypes.c_void_p(vel.ctypes.data) if vel is not None else None
+        self._check(self._lib.dfsph_get_state(self._ctx, p, v, _lib.MEM_HOST))
+
+    def get_state_ptr(self, pos_ptr: int, vel_ptr: int, mem: int = _lib.MEM_HOST) -> None:
+        """dfsph_get_state on raw pointers (host or device memory)."""
+        self._check(self._lib.dfsph_get_state(self._ctx, ctypes.c_void_p(pos_ptr or 0), ctypes.c_void_p(vel_ptr or 0),
+                                              mem))
+
     def field_device(self, which: int, dst_ptr: int, nbytes: int) -> None:
         self._check(self._lib.dfsph_get_field(self._ctx, which, ctypes.c_void_p(dst_ptr), nbytes,
                                               _lib.MEM_DEVICE))
