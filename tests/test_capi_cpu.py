@@ -163,3 +163,20 @@ def test_create_without_device_reports_no_device():
 def test_python_wrapper_raises_on_missing_library(tmp_path):
     with pytest.raises(RuntimeError, match="missing"):
         _lib.load(str(tmp_path / "nope.so"))
+
+
+def header_defines():
+    txt = open(os.path.join(ROOT, "include", "dfsph_gb300.h")).read()
+    return {k: int(v) for k, v in re.findall(r"#define\s+(DFSPH_[A-Z0-9_]+)\s+(-?\d+)\b", txt)}
+
+
+def test_binding_constants_match_the_header():
+    d = header_defines()
+    assert d["DFSPH_PRECISION_FP32_COMPENSATED"] == _lib.PRECISION_FP32_COMPENSATED
+    checked = 0
+    for name, value in d.items():
+        py = name[len("DFSPH_"):]
+        if hasattr(_lib, py):
+            assert getattr(_lib, py) == value, name
+            checked += 1
+    assert checked >= 20
