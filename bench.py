@@ -1049,6 +1049,10 @@ def main():
         units = cnt / 3.0 if k == "grid_scan" else cnt
         gbs = alg * units / (ms * 1e-3) / 1e9
         kr[k] = {"GB/s": round(gbs, 1), "frac": round(gbs / hbm, 4)}
+        # the neighbour passes against the SMs' instruction issue rate too
+        ir = issue_roofline(k, sc.n, ms / cnt, res["clocks"], res["sms"])
+        if ir:
+            kr[k]["issue_frac"] = round(ir["frac"], 4)
     line["kernel_roofline_warmup"] = kr
     # the whole step against the same peak: compulsory bytes of one step
     # N (192 + 84 I) + 4 (C + 1) + 16 N_b,active (1 + 2 I), I = solver
