@@ -440,18 +440,78 @@ __device__ __forceinline__ bool stopped_before(const IterCtl* ctl, u32 iter) {
 
 // Keys of the state in slot order, with the rank of each particle among the
 // particles of its cell (atomic, order fixed later) and the per-cell counts.
+// Key range of the particles counted for the next grid build: per block the
+// lowest and highest key go to one of KRANGE_SLOTS word pairs (krange[s] the
+// lows, krange[KRANGE_SLOTS + s] the highs), so that the atomics of all
+// blocks do not meet on one word. An out-of-grid particle (key = the scene's
+// last cell) makes the range the whole array: its stencil is clamped to the
+// grid's faces, anywhere along them.
+constexpr int KRANGE_SLOTS = 32;
+__device__ __forceinline__ void key_bounds(u32 k, u32 cells1, u32& lo, u32& hi) {
+    if (k % cells1 == cells1 - 1) {
+        lo = 0u;
+        hi = ~0u;
+    } else {
+        lo = k;
+        hi = k;
+    }
+}
+template <int BLOCK>
+__device__ __forceinline__ void key_range_block(u32 lo, u32 hi, u32* __restrict__ krange) {
+    __shared__ u32 wlo[BLOCK / 32], whi[BLOCK / 32];
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if ((threadIdx.x & 31) == 0) {
+        wlo[threadIdx.x >> 5] = lo;
+        whi[threadIdx.x >> 5] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        u32 l = ~0u, h = 0u;
+        for (int w = 0; w < int(blockDim.x >> 5); ++w) {
+            l = min(l, wlo[w]);
+            h = max(h, whi[w]);
+        }
+        if (l <= h) {
+            atomicMin(krange + blockIdx.x % KRANGE_SLOTS, l);
+            atomicMax(krange + KRANGE_SLOTS + blockIdx.x % KRANGE_SLOTS, h);
+        }
+    }
+}
+// The cells a grid build must scan: the counted keys widened by the stencil
+// margin (every cell a stencil centred up to one cell off a particle's key
+// cell can read, cell_start[c + 1] included); [a, b) = [0, 0) when nothing
+// was counted. Called by the 32 lanes of one warp (one slot pair each).
+__device__ __forceinline__ void scan_range(const u32* __restrict__ krange, u32 m, u32 margin, u32& a, u32& b) {
+    const u32 lane = threadIdx.x & 31u;
+    const u32 lo = __reduce_min_sync(0xffffffffu, krange[lane]);
+    const u32 hi = __reduce_max_sync(0xffffffffu, krange[KRANGE_SLOTS + lane]);
+    if (lo > hi) {
+        a = b = 0u;
+        return;
+    }
+    a = lo > margin ? lo - margin : 0u;
+    const unsigned long long e = (unsigned long long)hi + margin + 2u;
+    b = e < m ? u32(e) : m;
+}
+
 template <class R>
 __global__ void __launch_bounds__(256) count_kernel(int n, const R4<R>* __restrict__ xk,
                                                     GridDev<R> g, u32* __restrict__ key,
-                                                    u32* __restrict__ rank, u32* __restrict__ count) {
+                                                    u32* __restrict__ rank, u32* __restrict__ count,
+                                                    u32* __restrict__ krange) {
     pdl_wait();
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    const R4<R> p = ld(xk + s);
-    const u32 c = cell_key(p.x, p.y, p.z, g);
-    const u32 k = (g.rank ? __ldg(g.rank + c) : c) + scene_of(g, s) * g.cells1;
-    key[s] = k;
-    rank[s] = atomicAdd(count + k, 1u);
+    u32 lo = ~0u, hi = 0u;
+    if (s < n) {
+        const R4<R> p = ld(xk + s);
+        const u32 c = cell_key(p.x, p.y, p.z, g);
+        const u32 k = (g.rank ? __ldg(g.rank + c) : c) + scene_of(g, s) * g.cells1;
+        key[s] = k;
+        rank[s] = atomicAdd(count + k, 1u);
+        key_bounds(k, g.cells1, lo, hi);
+    }
+    if (krange) key_range_block<256>(lo, hi, krange);
 }
 
 // Exclusive scan of count[0..m) into cell_start[0..m] in three launches without
@@ -462,10 +522,28 @@ constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_BLOCK * SCAN_ITEMS;
 
 static __global__ void __launch_bounds__(SCAN_BLOCK) scan_tile_sums(const u32* __restrict__ count, u32 m,
-                                                             u32* __restrict__ tile_sums) {
+                                                             u32* __restrict__ tile_sums,
+                                                             const u32* __restrict__ krange, u32 margin) {
     pdl_wait();
     __shared__ u32 sh[SCAN_BLOCK / 32];
+    __shared__ u32 range[2];
     const u32 base = blockIdx.x * SCAN_TILE;
+    if (krange) {
+        // tiles outside the counted key range hold only zero counts
+        if (threadIdx.x < 32) {
+            u32 a, b;
+            scan_range(krange, m, margin, a, b);
+            if (threadIdx.x == 0) {
+                range[0] = a;
+                range[1] = b;
+            }
+        }
+        __syncthreads();
+        if (base >= range[1] || base + SCAN_TILE <= range[0]) {
+            if (threadIdx.x == 0) tile_sums[blockIdx.x] = 0u;
+            return;
+        }
+    }
     u32 t = 0;
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k) {
@@ -490,11 +568,22 @@ static __global__ void __launch_bounds__(SCAN_BLOCK) scan_tile_sums(const u32* _
 // once, before any solver kernel).
 static __global__ void __launch_bounds__(1024) scan_tile_offsets(u32* __restrict__ tile_sums, u32 n_tiles,
                                                           u32* __restrict__ total_out, IterCtl* ctl, int n_ctl,
-                                                          u32* __restrict__ maxv_scene, int n_scenes) {
+                                                          u32* __restrict__ maxv_scene, int n_scenes,
+                                                          u32* __restrict__ krange, u32 m, u32 margin,
+                                                          u32* __restrict__ cs_range) {
     pdl_wait();
     __shared__ u32 warp_tot[32];
     __shared__ u32 carry;
     if (threadIdx.x == 0) carry = 0;
+    // the scanned cells, for scan_tiles and for completing cell_start on export
+    if (cs_range && threadIdx.x < 32) {
+        u32 a = 0u, b = m;
+        if (krange) scan_range(krange, m, margin, a, b);
+        if (threadIdx.x == 0) {
+            cs_range[0] = a;
+            cs_range[1] = b;
+        }
+    }
     __syncthreads();
     for (u32 base = 0; base < n_tiles; base += blockDim.x) {
         const u32 i = base + threadIdx.x;
@@ -525,6 +614,8 @@ static __global__ void __launch_bounds__(1024) scan_tile_offsets(u32* __restrict
         __syncthreads();
     }
     for (int s = threadIdx.x; s < n_scenes; s += blockDim.x) maxv_scene[s] = 0u;
+    // the range is consumed: start the next build's from empty
+    if (krange && threadIdx.x < 2 * KRANGE_SLOTS) krange[threadIdx.x] = threadIdx.x < KRANGE_SLOTS ? ~0u : 0u;
     if (threadIdx.x == 0) {
         tile_sums[n_tiles] = carry;
         if (total_out) *total_out = carry;
@@ -547,11 +638,15 @@ __device__ __forceinline__ u32 scan_pad(u32 i) { return i + (i >> 5); }
 
 static __global__ void __launch_bounds__(SCAN_BLOCK) scan_tiles(u32* __restrict__ count, u32 m,
                                                          const u32* __restrict__ tile_offsets,
-                                                         u32* __restrict__ cell_start) {
+                                                         u32* __restrict__ cell_start,
+                                                         const u32* __restrict__ cs_range) {
     pdl_wait();
     __shared__ u32 warp_tot[SCAN_BLOCK / 32];
     __shared__ u32 tile[SCAN_TILE + SCAN_TILE / 32];
     const u32 base = blockIdx.x * SCAN_TILE;
+    // tiles outside the scanned range keep their (never read) entries; their
+    // counts are zero already
+    if (cs_range && (base >= cs_range[1] || base + SCAN_TILE <= cs_range[0])) return;
     // coalesced load of the tile (and clear the counts for the next build)
 #pragma unroll
     for (int k = 0; k < SCAN_ITEMS; ++k) {
@@ -600,6 +695,16 @@ static __global__ void __launch_bounds__(SCAN_BLOCK) scan_tiles(u32* __restrict_
         const u32 c = base + li;
         if (c < m) cell_start[c] = tile[scan_pad(li)];
     }
+}
+
+// cell_start outside the last ranged scan: 0 before it, the total after it
+// (an empty cell starts where the next particle's cell starts).
+static __global__ void __launch_bounds__(256) complete_cell_start_kernel(u32* __restrict__ cell_start, u32 m,
+                                                                         const u32* __restrict__ cs_range) {
+    const u32 c = blockIdx.x * 256u + threadIdx.x;
+    if (c >= m) return;
+    if (c < cs_range[0]) cell_start[c] = 0u;
+    else if (c >= cs_range[1]) cell_start[c] = cell_start[m];
 }
 
 // Provisional slot of every particle: cell start + atomic rank.
@@ -1625,7 +1730,8 @@ __device__ __forceinline__ u32 integrate_particle(int i, R4<R> v, const R4<R>& x
                                                   const GridDev<R>& g, R4<R>* __restrict__ vr, R4<R>* xk_out,
                                                   u32* __restrict__ key, u32* __restrict__ rank,
                                                   u32* __restrict__ count, unsigned char* __restrict__ tape_mask,
-                                                  const u32* __restrict__ id = nullptr, R4<R>* __restrict__ xc = nullptr) {
+                                                  const u32* __restrict__ id, R4<R>* __restrict__ xc, u32& klo,
+                                                  u32& khi) {
     // mask bits (recorded for the adjoint): 0-2 position clamped on x/y/z,
     // 3-5 velocity component zeroed, 6 speed clamped
     u32 mk = 0;
@@ -1670,6 +1776,7 @@ __device__ __forceinline__ u32 integrate_particle(int i, R4<R> v, const R4<R>& x
         const u32 k = sort_key<MORTON>(g, cell_key(px, py, pz, g)) + scene_of(g, i) * g.cells1;
         key[i] = k;
         rank[i] = atomicAdd(count + k, 1u);
+        key_bounds(k, g.cells1, klo, khi);
     }
     return __float_as_uint(float(sqrt(v.x * v.x + v.y * v.y + v.z * v.z)));
 }
@@ -1703,20 +1810,22 @@ __global__ void __launch_bounds__(256) advect_kernel(
     int n, const R4<R>* xk, R4<R>* xk_out, R4<R>* __restrict__ vr, StepDt<R> sd, Domain<R> d, GridDev<R> g,
     u32* __restrict__ key, u32* __restrict__ rank, u32* __restrict__ count, IterCtl* ctl,
     u32* __restrict__ maxv_scene, R4<R>* __restrict__ tape_v, unsigned char* __restrict__ tape_mask,
-    const u32* __restrict__ id, R4<R>* __restrict__ xc) {
+    const u32* __restrict__ id, R4<R>* __restrict__ xc, u32* __restrict__ krange) {
     pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const R dt = step_dt(sd);
     u32 vbits = 0;
     u32 scene = 0xffffffffu;  // lanes past the end form their own group
+    u32 klo = ~0u, khi = 0u;
     if (i < n) {
         const R4<R> v = vr[i];
         if (tape_v) tape_v[i] = v;
         vbits = integrate_particle<R, COUNT, MORTON, COMP>(i, v, xk[i], dt, d, g, vr, xk_out, key, rank, count,
-                                                           tape_mask, id, xc);
+                                                           tape_mask, id, xc, klo, khi);
         scene = scene_of(g, i);
     }
     max_velocity_epilogue<256>(i < n, vbits, scene, ctl, maxv_scene);
+    if (COUNT && krange) key_range_block<256>(klo, khi, krange);
 }
 
 // The last apply pass of a fixed-iteration density solve fused with the
@@ -1729,19 +1838,22 @@ __global__ void __launch_bounds__(LB, fp32_min_blocks<R>(LB)) apply_advect_kerne
     int n, const R4<R>* __restrict__ xk, R4<R>* xk_out, R4<R>* __restrict__ vr, const R* __restrict__ kap,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, StepDt<R> sd, Domain<R> d,
     u32* __restrict__ key, u32* __restrict__ rank, u32* __restrict__ count, IterCtl* ctl,
-    u32* __restrict__ maxv_scene, const u32* __restrict__ id, R4<R>* __restrict__ xc) {
+    u32* __restrict__ maxv_scene, const u32* __restrict__ id, R4<R>* __restrict__ xc,
+    u32* __restrict__ krange) {
     pdl_wait();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const R dt = step_dt(sd);
     u32 vbits = 0;
     u32 scene = 0xffffffffu;
+    u32 klo = ~0u, khi = 0u;
     if (i < n) {
         const R4<R> v = apply_velocity<R, MORTON>(i, xk, vr, kap, cs, g, p, bd, dt);
         vbits = integrate_particle<R, COUNT, MORTON, COMP>(i, v, ld(xk + i), dt, d, g, vr, xk_out, key, rank,
-                                                           count, nullptr, id, xc);
+                                                           count, nullptr, id, xc, klo, khi);
         scene = scene_of(g, i);
     }
     max_velocity_epilogue<LB>(i < n, vbits, scene, ctl, maxv_scene);
+    if (COUNT && krange) key_range_block<LB>(klo, khi, krange);
 }
 
 }  // namespace dfsph

@@ -166,6 +166,16 @@ public:
         }
         bcs_.alloc(size_t(cells1_) + 1);
         bmask_.alloc(std::max<size_t>(geom_.total, 1));
+        krange_.alloc(2 * KRANGE_SLOTS);
+        cs_range_.alloc(2);
+        reset_key_range();
+        DFSPH_CUDA(cudaMemsetAsync(cs_range_.p, 0, 2 * sizeof(u32), stream_));
+        {
+            // a stencil centred up to one cell off a particle's key cell reads
+            // cells up to two cells away on every axis, and cell_start[c + 1]
+            const u32 ny = u32(geom_.dims[1]), nz = u32(geom_.dims[2]);
+            margin_ = 2u * (ny * nz + nz + 1u) + 2u;
+        }
         if (comp_) {
             xc_.alloc(std::max(cap_, 1u));
             DFSPH_CUDA(cudaMemsetAsync(xc_.p, 0, size_t(std::max(cap_, 1u)) * sizeof(V4), stream_));
@@ -259,7 +269,7 @@ public:
         launch_import(n, src, nullptr, xb_[0].p, vr_scratch(), bid_[0].p);
         // sort by cell (the boundary CellGrid built once, dfsph.cu:93-97)
         launch(DFSPH_KERNEL_GRID_COUNT, count_kernel<R>, blocks_for(n, 256), 256, int(n), xb_[0].p, gb_, bkey_.p,
-               brank_.p, count_.p);
+               brank_.p, count_.p, (u32*)nullptr);
         scan(bcs_.p, cells1_, /*step start*/ false);
         launch(DFSPH_KERNEL_GRID_SCATTER, scatter_kernel, blocks_for(n, 256), 256, int(n), bkey_.p, brank_.p, bcs_.p,
                bid_[0].p, btmp_src_.p, btmp_id_.p);
@@ -475,6 +485,7 @@ public:
             case DFSPH_FIELD_SORTED_INDEX:
                 DFSPH_CUDA(cudaMemcpyAsync(out, id, need, cudaMemcpyDeviceToDevice, stream_)); break;
             case DFSPH_FIELD_CELL_START:
+                complete_cell_start();
                 DFSPH_CUDA(cudaMemcpyAsync(out, cell_start_.p, need, cudaMemcpyDeviceToDevice, stream_)); break;
             case DFSPH_FIELD_BOUNDARY_CELL_START:
                 DFSPH_CUDA(cudaMemcpyAsync(out, bcs_.p, need, cudaMemcpyDeviceToDevice, stream_)); break;
@@ -889,7 +900,7 @@ public:
             DFSPH_CUDA(cudaMemcpyAsync(fctl_.p, &h, sizeof(FrameCtl), cudaMemcpyHostToDevice, stream_));
             if (!counts_valid_) {
                 launch(DFSPH_KERNEL_GRID_COUNT, count_kernel<R>, blocks_for(n_, 256), 256, int(n_), xk_[cx_].p, g_,
-                       key_.p, rank_.p, count_.p);
+                       key_.p, rank_.p, count_.p, fluid_krange());
                 counts_valid_ = true;
             }
             ensure_frame_graph();
@@ -1371,6 +1382,22 @@ private:
     // the integrator's compensation carries when this step uses them
     const u32* comp_id() const { return comp_ ? id_[ci_].p : nullptr; }
     V4* comp_xc() const { return comp_ ? xc_.p : nullptr; }
+    void reset_key_range() {
+        DFSPH_CUDA(cudaMemsetAsync(krange_.p, 0xFF, KRANGE_SLOTS * sizeof(u32), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(krange_.p + KRANGE_SLOTS, 0, KRANGE_SLOTS * sizeof(u32), stream_));
+    }
+    // ranged fluid scans only in the x-major order (Morton ranks of
+    // neighbouring cells are not near each other)
+    u32* fluid_krange() const { return g_.rank ? nullptr : krange_.p; }
+    // cell_start in full, for readers beyond the particles' stencils. The
+    // flag stays set: every later ranged scan (graph replays included, which
+    // run no host code) leaves stale entries again.
+    void complete_cell_start() {
+        if (!cs_ranged_) return;
+        const size_t m = keys_;
+        launch(DFSPH_KERNEL_IO, complete_cell_start_kernel, blocks_for(m, 256), 256, cell_start_.p, u32(m),
+               (const u32*)cs_range_.p);
+    }
     void reset_compensation() {
         if (comp_ && cap_) DFSPH_CUDA(cudaMemsetAsync(xc_.p, 0, size_t(cap_) * sizeof(V4), stream_));
     }
@@ -1569,6 +1596,7 @@ private:
     void drop_pending_counts() {
         if (!counts_valid_) return;
         DFSPH_CUDA(cudaMemsetAsync(count_.p, 0, keys_ * sizeof(u32), stream_));
+        reset_key_range();
         counts_valid_ = false;
     }
 
@@ -1601,6 +1629,7 @@ private:
     // algorithmic byte count of the wall terms).
     u32 active_boundary() {
         if (nb_ == 0 || n_ == 0 || !stepped_) return 0;
+        complete_cell_start();  // it walks the stencils of all wall particles
         u32* d = static_cast<u32*>(scratch_bytes(sizeof(u32)));
         DFSPH_CUDA(cudaMemsetAsync(d, 0, sizeof(u32), stream_));
         with_slot_order([&](auto order) {
@@ -1620,13 +1649,20 @@ private:
 
     // Exclusive scan of the counts of m keys into cell_start[0..m] (closing
     // entry included). At a step start it also resets the iteration controls.
-    void scan(u32* cell_start, size_t m, bool step_start) {
+    // ranged: only the tiles within the counted key range (plus the stencil
+    // margin) are scanned; the other entries of cell_start keep stale values
+    // that no stencil reads (complete_cell_start fills them for export)
+    void scan(u32* cell_start, size_t m, bool step_start, u32* krange = nullptr) {
         const u32 tiles = static_cast<u32>((m + SCAN_TILE - 1) / SCAN_TILE);
-        launch(DFSPH_KERNEL_GRID_SCAN, scan_tile_sums, int(tiles), SCAN_BLOCK, count_.p, u32(m), tile_sums_.p);
+        launch(DFSPH_KERNEL_GRID_SCAN, scan_tile_sums, int(tiles), SCAN_BLOCK, count_.p, u32(m), tile_sums_.p,
+               (const u32*)krange, margin_);
         launch(DFSPH_KERNEL_GRID_SCAN, scan_tile_offsets, 1, 1024, tile_sums_.p, tiles, cell_start + m,
                step_start ? ctl_.p : nullptr, step_start ? 3 : 0,
-               step_start && scenes_ > 1 ? maxv_scene_.p : nullptr, step_start && scenes_ > 1 ? int(scenes_) : 0);
-        launch(DFSPH_KERNEL_GRID_SCAN, scan_tiles, int(tiles), SCAN_BLOCK, count_.p, u32(m), tile_sums_.p, cell_start);
+               step_start && scenes_ > 1 ? maxv_scene_.p : nullptr, step_start && scenes_ > 1 ? int(scenes_) : 0,
+               krange, u32(m), margin_, krange ? cs_range_.p : nullptr);
+        launch(DFSPH_KERNEL_GRID_SCAN, scan_tiles, int(tiles), SCAN_BLOCK, count_.p, u32(m), tile_sums_.p, cell_start,
+               krange ? (const u32*)cs_range_.p : nullptr);
+        if (cell_start == cell_start_.p) cs_ranged_ = krange != nullptr;
     }
 
     BoundaryDev bdev() const {
@@ -1703,12 +1739,13 @@ private:
                             launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, apply_advect_kernel<R, true, 128, M, C>,
                                         apply_advect_kernel<R, true, 256, M, C>, n, (const V4*)xout, xk_[cx_ ^ 1].p,
                                         vr_[cv_].p, (const R*)kap_it, cs, g_, phys_, bdev(), sd, fa->d, key_.p,
-                                        rank_.p, count_.p, ctl_.p, fa->mvs, comp_id(), comp_xc());
+                                        rank_.p, count_.p, ctl_.p, fa->mvs, comp_id(), comp_xc(), fluid_krange());
                         else
                             launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, apply_advect_kernel<R, false, 128, M, C>,
                                         apply_advect_kernel<R, false, 256, M, C>, n, (const V4*)xout,
                                         xk_[cx_ ^ 1].p, vr_[cv_].p, (const R*)kap_it, cs, g_, phys_, bdev(), sd, fa->d,
-                                        key_.p, rank_.p, count_.p, ctl_.p, fa->mvs, comp_id(), comp_xc());
+                                        key_.p, rank_.p, count_.p, ctl_.p, fa->mvs, comp_id(), comp_xc(),
+                                        fluid_krange());
                     });
                 });
                 cx_ ^= 1;
@@ -1916,8 +1953,8 @@ private:
         // 1. grid build (CellGrid::build, core/src/cell_grid.cu:73-138)
         if (!counts_valid_)
             launch(DFSPH_KERNEL_GRID_COUNT, count_kernel<R>, blocks_for(n, 256), 256, n, xk_[cx_].p, g_, key_.p,
-                   rank_.p, count_.p);
-        scan(cs, keys_, /*step start*/ true);
+                   rank_.p, count_.p, fluid_krange());
+        scan(cs, keys_, /*step start*/ true, fluid_krange());
         launch(DFSPH_KERNEL_GRID_SCATTER, scatter_kernel, blocks_for(n, 256), 256, n, key_.p, rank_.p, cs,
                id_[ci_].p, tmp_src_.p, tmp_id_.p);
         launch(DFSPH_KERNEL_GRID_REORDER, reorder_kernel<R>, blocks_for(n, 256), 256, n, tmp_src_.p, tmp_id_.p,
@@ -1992,11 +2029,13 @@ private:
                 if (count_next)
                     launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, true, M, C>, blocks_for(n, 256), 256, n, xin, xout,
                            vr_[cv_].p, sd, dom, g_, key_.p, rank_.p, count_.p, ctl_.p, mvs, tp ? tp->va : nullptr,
-                           tp ? tp->amask : nullptr, comp ? comp_id() : nullptr, comp ? comp_xc() : nullptr);
+                           tp ? tp->amask : nullptr, comp ? comp_id() : nullptr, comp ? comp_xc() : nullptr,
+                           fluid_krange());
                 else
                     launch(DFSPH_KERNEL_ADVECT, advect_kernel<R, false, M, C>, blocks_for(n, 256), 256, n, xin, xout,
                            vr_[cv_].p, sd, dom, g_, key_.p, rank_.p, count_.p, ctl_.p, mvs, tp ? tp->va : nullptr,
-                           tp ? tp->amask : nullptr, comp ? comp_id() : nullptr, comp ? comp_xc() : nullptr);
+                           tp ? tp->amask : nullptr, comp ? comp_id() : nullptr, comp ? comp_xc() : nullptr,
+                           fluid_krange());
             });
         });
         if (count_next) counts_valid_ = true;
@@ -2090,6 +2129,13 @@ private:
     // DFSPH_PRECISION_FP32_COMPENSATED: the integrator's per-particle carries
     // (original particle order), zero on every new fluid state
     const bool comp_ = cfg_.precision == DFSPH_PRECISION_FP32_COMPENSATED;
+    // the key range of the particles counted for the next fluid grid build
+    // (KRANGE_SLOTS lows, then highs), the cells its scan covered, and
+    // whether cell_start holds stale entries outside them
+    DevBuf<u32> krange_;
+    DevBuf<u32> cs_range_;
+    u32 margin_ = 0;
+    bool cs_ranged_ = false;
     DevBuf<V4> xc_;
     DevBuf<V4> tune_xc_;
     DevBuf<V4> tune_ck_;

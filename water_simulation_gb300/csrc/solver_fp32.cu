@@ -51,14 +51,14 @@ void build_cell_grid(const float* xyz, u32 n, const float origin[3], const int d
     DFSPH_CUDA(cudaMemsetAsync(ctl, 0, sizeof(IterCtl), st));
     import_kernel<float><<<blocks_for(n, 256), 256, 0, st>>>(int(n), xyz, nullptr, x_in, v_in, id0);
     DFSPH_LAUNCHED();
-    count_kernel<float><<<blocks_for(n, 256), 256, 0, st>>>(int(n), x_in, g, key, rank, count);
+    count_kernel<float><<<blocks_for(n, 256), 256, 0, st>>>(int(n), x_in, g, key, rank, count, nullptr);
     DFSPH_LAUNCHED();
     const u32 m = geo.total + 1;
-    scan_tile_sums<<<n_tiles, SCAN_BLOCK, 0, st>>>(count, m, tiles);
+    scan_tile_sums<<<n_tiles, SCAN_BLOCK, 0, st>>>(count, m, tiles, nullptr, 0u);
     DFSPH_LAUNCHED();
-    scan_tile_offsets<<<1, 1024, 0, st>>>(tiles, n_tiles, starts + m, nullptr, 0, nullptr, 0);
+    scan_tile_offsets<<<1, 1024, 0, st>>>(tiles, n_tiles, starts + m, nullptr, 0, nullptr, 0, nullptr, m, 0u, nullptr);
     DFSPH_LAUNCHED();
-    scan_tiles<<<n_tiles, SCAN_BLOCK, 0, st>>>(count, m, tiles, starts);
+    scan_tiles<<<n_tiles, SCAN_BLOCK, 0, st>>>(count, m, tiles, starts, nullptr);
     DFSPH_LAUNCHED();
     scatter_kernel<<<blocks_for(n, 256), 256, 0, st>>>(int(n), key, rank, starts, id0, tsrc, tid);
     DFSPH_LAUNCHED();

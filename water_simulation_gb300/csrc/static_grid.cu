@@ -139,9 +139,9 @@ extern "C" int dfsph_build_cell_grid_static(const float* xyz_dev, uint32_t n, co
     if (cudaMemsetAsync(count, 0, size_t(m) * sizeof(u32), st) != cudaSuccess) return DFSPH_ERR_CUDA;
     static_count_kernel<<<nb, 256, 0, st>>>(int(n), xyz_dev, g, key, rank, count);
     iota_kernel<<<nb, 256, 0, st>>>(int(n), ids);  // the input order is the original order
-    scan_tile_sums<<<n_tiles, SCAN_BLOCK, 0, st>>>(count, m, tiles);
-    scan_tile_offsets<<<1, 1024, 0, st>>>(tiles, n_tiles, nullptr, nullptr, 0, nullptr, 0);
-    scan_tiles<<<n_tiles, SCAN_BLOCK, 0, st>>>(count, m, tiles, cell_start_dev);
+    scan_tile_sums<<<n_tiles, SCAN_BLOCK, 0, st>>>(count, m, tiles, nullptr, 0u);
+    scan_tile_offsets<<<1, 1024, 0, st>>>(tiles, n_tiles, nullptr, nullptr, 0, nullptr, 0, nullptr, m, 0u, nullptr);
+    scan_tiles<<<n_tiles, SCAN_BLOCK, 0, st>>>(count, m, tiles, cell_start_dev, nullptr);
     scatter_kernel<<<nb, 256, 0, st>>>(int(n), key, rank, cell_start_dev, ids, tsrc, tid);
     static_order_kernel<<<nb, 256, 0, st>>>(int(n), tsrc, tid, key, cell_start_dev, geo.total, sorted_keys_dev,
                                             sorted_indices_dev);
