@@ -60,3 +60,19 @@ def test_exported_cell_start_is_complete_after_graph_replays():
     cs = gpu.field(_lib.FIELD_CELL_START)
     assert np.array_equal(cs, ora.field(O.F_CELL_START))
     assert cs[0] == 0 and cs[-1] == sc.n
+
+
+def test_cell_start_after_an_adjoint_rollout_describes_the_final_state():
+    # the adjoint's taped replays scan into their own copies of cell_start;
+    # the context's own one, completed on export, must be the final state's
+    sc = scenes.adjoint_puddle(steps=6)
+    s = solver_for(sc, diagnostics=True)
+    s.adjoint_set_state(sc.fluid, sc.velocity)
+    s.adjoint_forward(sc.dt, 6, 2)
+    xT, _ = s.adjoint_state()
+    s.adjoint_backward(np.ones_like(xT) * 1e-3)
+    cs = s.field(_lib.FIELD_CELL_START)
+    t = solver_for(sc, diagnostics=True)
+    t.set_fluid(sc.fluid, sc.velocity)
+    t.step(sc.dt, 6)
+    assert np.array_equal(cs, t.field(_lib.FIELD_CELL_START))

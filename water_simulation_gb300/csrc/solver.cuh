@@ -1653,6 +1653,10 @@ private:
     // margin) are scanned; the other entries of cell_start keep stale values
     // that no stencil reads (complete_cell_start fills them for export)
     void scan(u32* cell_start, size_t m, bool step_start, u32* krange = nullptr) {
+        // only the context's own cell_start is scanned by range: cs_range_
+        // describes it (an adjoint replay's per-step copies are scanned whole,
+        // and the key range they leave behind only widens the next one)
+        if (cell_start != cell_start_.p) krange = nullptr;
         const u32 tiles = static_cast<u32>((m + SCAN_TILE - 1) / SCAN_TILE);
         launch(DFSPH_KERNEL_GRID_SCAN, scan_tile_sums, int(tiles), SCAN_BLOCK, count_.p, u32(m), tile_sums_.p,
                (const u32*)krange, margin_);
