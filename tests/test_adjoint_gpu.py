@@ -80,6 +80,34 @@ def test_adjoint_equals_forward_mode_oracle(puddle40, fp64_grad):
         assert abs(adj - jvp) <= 1e-7 * abs(jvp), (kind, adj, jvp)
 
 
+def test_one_lane_reverse_passes_equal_forward_mode_oracle():
+    # scenes of at most 4 x 128 particles per SM run the reverse neighbour
+    # passes with two lanes per particle (the puddle above); this block is
+    # just above that size, so they run one lane per particle
+    import torch
+
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    side = int(np.ceil((4 * 128 * sms + 1) ** (1 / 3)))
+    sc = scenes.falling_block((side,) * 3, seed=41, radius=0.009, corner=(0.1, 0.1, 0.1), velocity_sigma=0.1)
+    sc.max_divergence_iters = 2
+    assert sc.n > 4 * 128 * sms
+    steps = 5
+    s, L, xT, gx, gv, ge = _gradients(sc, _lib.PRECISION_FP64, steps)
+    oc = O.config_from(sc.config(precision=_lib.PRECISION_FP64))
+    rng = np.random.default_rng(18)
+    dx = rng.standard_normal((sc.n, 3)) * 1e-2
+    dv = rng.standard_normal((sc.n, 3))
+    tgt = _target(sc)
+    for kind, kw, adj in (("x0", {"dx": dx}, float((gx * dx).sum())),
+                          ("v0", {"dv": dv}, float((gv * dv).sum())),
+                          ("xsph", {"d_xsph": 1.0}, ge)):
+        d = O.DualOracle(oc, sc.fluid, sc.velocity, sc.boundary, **kw)
+        d.step(sc.dt, steps)
+        x, _, tx, _ = d.state()
+        jvp = float((2.0 * (x - tgt) / sc.n * tx).sum())
+        assert abs(adj - jvp) <= 1e-7 * abs(jvp), (kind, adj, jvp)
+
+
 def test_central_differences_eps_1e3():
     sc = scenes.adjoint_puddle(steps=20)
     s, L, xT, gx, gv, ge = _gradients(sc, _lib.PRECISION_FP64, 20)

@@ -109,25 +109,40 @@ __global__ void __launch_bounds__(256) adjoint_advect_kernel(
     alphabar[i] = R(0);
 }
 
+// Sum of a value over the L lanes (consecutive, L a power of two) that share a
+// particle, by a fixed butterfly: every lane ends with the same bits.
+template <int L, class T> __device__ __forceinline__ T lane_sum(T v) {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
 // Adjoint of the apply half of one Jacobi iteration plus the pointwise part of
 // its rate half. Reads vbar (adjoint of the iteration's output velocity, which
 // is also the adjoint of its input through the identity), writes the rate
 // adjoint rdb into xr = (x, rdb) and accumulates x_bar, rho_bar, alpha_bar.
-template <class R, bool DIVERGENCE>
+// L lanes per particle (1, or 2 for scenes small enough that one lane per
+// particle leaves most SMs idle): lane q takes candidates b + q, b + q + L, ...
+// of every run, and the lanes' partial sums are added by lane_sum.
+template <class R, bool DIVERGENCE, int L>
 __global__ void __launch_bounds__(128) adjoint_apply_kernel(
     int n, const R4<R>* __restrict__ xkf, const R4<R>* __restrict__ tx, const R4<R>* __restrict__ tg,
     const R* __restrict__ kap, const R* __restrict__ adv, const R4<R>* __restrict__ vbar,
     const u32* __restrict__ cs, GridDev<R> g, Phys<R> p, BoundaryDev bd, R dt, R4<R>* __restrict__ xbar,
     R* __restrict__ rhobar, R* __restrict__ alphabar, R4<R>* __restrict__ xr) {
     pdl_wait();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const R4<R> pi = ld(xkf + i);
-    const R4<R> vb = ld(vbar + i);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / L;
+    const u32 q = u32(t % L);
+    if (L == 1 && i >= n) return;
+    const bool valid = i < n;
+    const int ii = valid ? i : 0;
+    const R4<R> pi = ld(xkf + ii);
+    const R4<R> vb = ld(vbar + ii);
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
     R s1 = 0, X = 0, Y = 0, Z = 0;
-    for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
-        for (u32 j = b; j < e; ++j) {
+    if (valid) for_each_run(c, g, cs + scene_of(g, ii) * g.cells1, [&](u32 b, u32 e) {
+        for (u32 j = b + q; j < e; j += L) {
             const R4<R> pj = ld(xkf + j);
             const R4<R> wj = ld(vbar + j);
             const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
@@ -146,10 +161,10 @@ __global__ void __launch_bounds__(128) adjoint_apply_kernel(
         }
     });
     R bgv = 0, JX = 0, JY = 0, JZ = 0;
-    if (bd.has && boundary_near(c, g, bd.mask)) {
+    if (valid && bd.has && boundary_near(c, g, bd.mask)) {
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
         for_each_run(c, wall_grid(g), bd.bcs, [&](u32 b, u32 e) {
-            for (u32 j = b; j < e; ++j) {
+            for (u32 j = b + q; j < e; j += L) {
                 const R4<R> pj = ld(xb + j);
                 const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
                 R rinv;
@@ -164,6 +179,11 @@ __global__ void __launch_bounds__(128) adjoint_apply_kernel(
                 JZ += pj.w * (F * vb.z + t * rz);
             }
         });
+    }
+    if (L > 1) {
+        s1 = lane_sum<L>(s1); X = lane_sum<L>(X); Y = lane_sum<L>(Y); Z = lane_sum<L>(Z);
+        bgv = lane_sum<L>(bgv); JX = lane_sum<L>(JX); JY = lane_sum<L>(JY); JZ = lane_sum<L>(JZ);
+        if (!valid || q != 0) return;
     }
     const R kfb = -dt * (p.mass * s1 + bgv);
     const R kap_i = kap[i];
@@ -202,20 +222,25 @@ __global__ void __launch_bounds__(128) adjoint_apply_kernel(
     xr[i] = {pi.x, pi.y, pi.z, rdb};
 }
 
-// Adjoint of the rate half's neighbour sum: adds to v_bar and x_bar.
-template <class R>
+// Adjoint of the rate half's neighbour sum: adds to v_bar and x_bar. L lanes
+// per particle as in adjoint_apply_kernel.
+template <class R, int L>
 __global__ void __launch_bounds__(128) adjoint_rate_kernel(
     int n, const R4<R>* __restrict__ xr, const R4<R>* __restrict__ vel, const u32* __restrict__ cs, GridDev<R> g,
     Phys<R> p, BoundaryDev bd, R4<R>* __restrict__ vbar, R4<R>* __restrict__ xbar) {
     pdl_wait();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const R4<R> pi = ld(xr + i);
-    const R4<R> vi = ld(vel + i);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / L;
+    const u32 q = u32(t % L);
+    if (L == 1 && i >= n) return;
+    const bool valid = i < n;
+    const int ii = valid ? i : 0;
+    const R4<R> pi = ld(xr + ii);
+    const R4<R> vi = ld(vel + ii);
     const Centre c = stencil_centre(pi.x, pi.y, pi.z, g);
     R VX = 0, VY = 0, VZ = 0, X = 0, Y = 0, Z = 0;
-    for_each_run(c, g, cs + scene_of(g, i) * g.cells1, [&](u32 b, u32 e) {
-        for (u32 j = b; j < e; ++j) {
+    if (valid) for_each_run(c, g, cs + scene_of(g, ii) * g.cells1, [&](u32 b, u32 e) {
+        for (u32 j = b + q; j < e; j += L) {
             const R4<R> pj = ld(xr + j);
             const R4<R> vj = ld(vel + j);
             const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
@@ -234,10 +259,10 @@ __global__ void __launch_bounds__(128) adjoint_rate_kernel(
         }
     });
     R BX = 0, BY = 0, BZ = 0, JX = 0, JY = 0, JZ = 0;
-    if (bd.has && boundary_near(c, g, bd.mask)) {
+    if (valid && bd.has && boundary_near(c, g, bd.mask)) {
         const R4<R>* xb = static_cast<const R4<R>*>(bd.xb);
         for_each_run(c, wall_grid(g), bd.bcs, [&](u32 b, u32 e) {
-            for (u32 j = b; j < e; ++j) {
+            for (u32 j = b + q; j < e; j += L) {
                 const R4<R> pj = ld(xb + j);
                 const R rx = pi.x - pj.x, ry = pi.y - pj.y, rz = pi.z - pj.z;
                 R rinv;
@@ -252,6 +277,13 @@ __global__ void __launch_bounds__(128) adjoint_rate_kernel(
                 JZ += mF * vi.z + t * rz;
             }
         });
+    }
+    if (L > 1) {
+        VX = lane_sum<L>(VX); VY = lane_sum<L>(VY); VZ = lane_sum<L>(VZ);
+        X = lane_sum<L>(X); Y = lane_sum<L>(Y); Z = lane_sum<L>(Z);
+        BX = lane_sum<L>(BX); BY = lane_sum<L>(BY); BZ = lane_sum<L>(BZ);
+        JX = lane_sum<L>(JX); JY = lane_sum<L>(JY); JZ = lane_sum<L>(JZ);
+        if (!valid || q != 0) return;
     }
     const R rdb = pi.w;
     R4<R> vo = vbar[i];

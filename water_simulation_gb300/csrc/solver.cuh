@@ -1140,6 +1140,11 @@ private:
         return ad_staging_.p;
     }
 
+    int sm_count() {
+        if (sm_count_ == 0) DFSPH_CUDA(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device_));
+        return sm_count_;
+    }
+
     void ensure_adjoint_buffers() {
         if (xg_.n >= cap_ && cap_) return;
         const size_t c = std::max(cap_, 1u);
@@ -1305,27 +1310,38 @@ private:
         launch(DFSPH_KERNEL_ADJOINT, adjoint_advect_kernel<R>, b256, 256, n, (const u32*)t.id, (const V4*)t.va,
                (const unsigned char*)t.amask, dt, (const V4*)xg_.p, (const V4*)vg_.p, xbar_.p, vbar_[cur].p,
                rhobar_.p, alphabar_.p);
-        for (u32 it = cfg_.max_density_iters; it-- > 0;) {
-            launch(DFSPH_KERNEL_ADJOINT, adjoint_apply_kernel<R, false>, b128, 128, n, (const V4*)(t.xkf[1] + it * st),
-                   (const V4*)t.x, (const V4*)t.g, (const R*)(t.kap[1] + it * st), (const R*)(t.adv[1] + it * st),
-                   (const V4*)vbar_[cur].p, (const u32*)t.cs, g_, phys_, bd, dt, xbar_.p, rhobar_.p, alphabar_.p,
-                   xr_.p);
-            launch(DFSPH_KERNEL_ADJOINT, adjoint_rate_kernel<R>, b128, 128, n, (const V4*)xr_.p,
-                   (const V4*)(t.v[1] + it * st), (const u32*)t.cs, g_, phys_, bd, vbar_[cur].p, xbar_.p);
-        }
+        // two lanes per particle when one lane would give at most four
+        // 128-thread blocks per SM: those launches are latency-bound, larger
+        // ones lose more to the lanes' shuffles than they gain
+        const bool wide = n <= 4 * 128 * sm_count();
+        const int b2 = blocks_for(2 * n, 128);
+        auto apply_rate = [&](int w, u32 it, auto divergence) {
+            constexpr bool D = decltype(divergence)::value;
+            const V4* xkf = (const V4*)(t.xkf[w] + it * st);
+            const R* kap = (const R*)(t.kap[w] + it * st);
+            const R* adv = (const R*)(t.adv[w] + it * st);
+            const V4* vel = (const V4*)(t.v[w] + it * st);
+            if (wide) {
+                launch(DFSPH_KERNEL_ADJOINT, adjoint_apply_kernel<R, D, 2>, b2, 128, n, xkf, (const V4*)t.x,
+                       (const V4*)t.g, kap, adv, (const V4*)vbar_[cur].p, (const u32*)t.cs, g_, phys_, bd, dt,
+                       xbar_.p, rhobar_.p, alphabar_.p, xr_.p);
+                launch(DFSPH_KERNEL_ADJOINT, adjoint_rate_kernel<R, 2>, b2, 128, n, (const V4*)xr_.p, vel,
+                       (const u32*)t.cs, g_, phys_, bd, vbar_[cur].p, xbar_.p);
+            } else {
+                launch(DFSPH_KERNEL_ADJOINT, adjoint_apply_kernel<R, D, 1>, b128, 128, n, xkf, (const V4*)t.x,
+                       (const V4*)t.g, kap, adv, (const V4*)vbar_[cur].p, (const u32*)t.cs, g_, phys_, bd, dt,
+                       xbar_.p, rhobar_.p, alphabar_.p, xr_.p);
+                launch(DFSPH_KERNEL_ADJOINT, adjoint_rate_kernel<R, 1>, b128, 128, n, (const V4*)xr_.p, vel,
+                       (const u32*)t.cs, g_, phys_, bd, vbar_[cur].p, xbar_.p);
+            }
+        };
+        for (u32 it = cfg_.max_density_iters; it-- > 0;) apply_rate(1, it, std::false_type{});
         launch(DFSPH_KERNEL_ADJOINT, adjoint_xsph_kernel<R>, b128, 128, n, (const V4*)t.x, (const V4*)t.vx,
                (const V4*)vbar_[cur].p, vbar_[cur ^ 1].p, (const u32*)t.cs, g_, phys_, R(cfg_.damping), dt,
                R(ad_eps_), xbar_.p,
                rhobar_.p, eps_part_.p, eps_ctr_.p, eps_acc_.p);
         cur ^= 1;
-        for (u32 it = cfg_.max_divergence_iters; it-- > 0;) {
-            launch(DFSPH_KERNEL_ADJOINT, adjoint_apply_kernel<R, true>, b128, 128, n, (const V4*)(t.xkf[0] + it * st),
-                   (const V4*)t.x, (const V4*)t.g, (const R*)(t.kap[0] + it * st), (const R*)(t.adv[0] + it * st),
-                   (const V4*)vbar_[cur].p, (const u32*)t.cs, g_, phys_, bd, dt, xbar_.p, rhobar_.p, alphabar_.p,
-                   xr_.p);
-            launch(DFSPH_KERNEL_ADJOINT, adjoint_rate_kernel<R>, b128, 128, n, (const V4*)xr_.p,
-                   (const V4*)(t.v[0] + it * st), (const u32*)t.cs, g_, phys_, bd, vbar_[cur].p, xbar_.p);
-        }
+        for (u32 it = cfg_.max_divergence_iters; it-- > 0;) apply_rate(0, it, std::true_type{});
         launch(DFSPH_KERNEL_ADJOINT, adjoint_density_prep_kernel<R>, b256, 256, n, (const V4*)t.x, (const V4*)t.g,
                (const R*)rhobar_.p, (const R*)alphabar_.p, xq_.p, gq_.p);
         launch(DFSPH_KERNEL_ADJOINT, adjoint_density_kernel<R>, b128, 128, n, (const V4*)xq_.p, (const V4*)gq_.p,
@@ -2047,6 +2063,7 @@ private:
 
     dfsph_config cfg_;
     int device_;
+    int sm_count_ = 0;  // queried on first use
     cudaStream_t stream_;
     GridGeom geom_;
     GridDev<R> g_;   // fluid grid (scene-aware)
