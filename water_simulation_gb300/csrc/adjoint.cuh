@@ -314,6 +314,16 @@ static __device__ __forceinline__ void accumulate_partial(double partial, double
     }
 }
 
+// 1 / b as the forward XSPH pass forms its quotient w / b (fast_div): the
+// approximate reciprocal in FP32, so that w * rcp_as_forward(b) is the
+// forward's bits, and a division in FP64.
+__device__ __forceinline__ float rcp_as_forward(float b) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+    return r;
+}
+__device__ __forceinline__ double rcp_as_forward(double b) { return 1.0 / b; }
+
 // Adjoint of gravity + damping + XSPH (forces_xsph_kernel).
 template <class R>
 __global__ void __launch_bounds__(128) adjoint_xsph_kernel(
@@ -343,7 +353,7 @@ __global__ void __launch_bounds__(128) adjoint_xsph_kernel(
                 const R w = kernel_w(r, p);
                 const R f = grad_factor(r, rinv, p);
                 const R ra = R(0.5) * (vi.w + vj.w);
-                const R inv = R(1) / rmax(ra, R(1e-9));
+                const R inv = rcp_as_forward(rmax(ra, R(1e-9)));
                 const R cc = w * inv;
                 AX += cc * (wj.x - wi.x); AY += cc * (wj.y - wi.y); AZ += cc * (wj.z - wi.z);
                 const R ux = vj.x - vi.x, uy = vj.y - vi.y, uz = vj.z - vi.z;
