@@ -109,6 +109,36 @@ def test_particles_on_cell_faces_and_out_of_grid():
     assert_fields_close(gpu, ora, v_tol=1e-3)
 
 
+def test_more_out_of_grid_particles_than_the_ordering_cap():
+    # 5,000 particles outside the grid, more than the 4,096 that the reorder
+    # pass puts in index order: those keep their provisional order inside the
+    # out-of-grid range and raise flag bit 1. No stencil includes the
+    # out-of-grid key, so every other structure field, and every value in
+    # original order, still equals the oracle's.
+    sc = scenes.falling_block((10, 10, 10), seed=34, velocity_sigma=0.1)
+    rng = np.random.default_rng(35)
+    far = rng.uniform(2.0, 3.0, size=(5000, 3)).astype(np.float32)
+    far[:50] = np.float32([-0.5, 0.5, 0.5])
+    x = np.concatenate([sc.fluid, far])
+    v = np.concatenate([sc.velocity, np.zeros_like(far)])
+    sc.fluid, sc.velocity = x, v
+    gpu = solver_for(sc, diagnostics=True)
+    ora = oracle_for(sc, gpu)
+    gpu.step(sc.dt)
+    ora.step(sc.dt)
+    assert int(gpu.scalar(_lib.SCALAR_FLAGS)) & 2
+    inside = 1000
+    for fg, fo in STRUCT:
+        if fg == _lib.FIELD_SORTED_INDEX:
+            continue
+        assert np.array_equal(gpu.field(fg), ora.field(fo)), fg
+    assert gpu.field(_lib.FIELD_CELL_START)[-1] == inside
+    si, so = gpu.field(_lib.FIELD_SORTED_INDEX), ora.field(O.F_SORTED_INDEX)
+    assert np.array_equal(si[:inside], so[:inside])
+    assert np.array_equal(np.sort(si[inside:]), np.sort(so[inside:]))
+    assert_fields_close(gpu, ora)
+
+
 def test_random_cloud_structure_matches():
     rng = np.random.default_rng(123)
     sc = scenes.falling_block((4, 4, 4), seed=1)
