@@ -304,7 +304,13 @@ public:
         const float* v = vel && pos ? pos + 3 * size_t(n) : nullptr;
         if (mem == DFSPH_MEM_DEVICE) { pos = xyz; v = vel; }
         install_counts(n_scenes, counts, n);
-        if (n == 0) return;
+        if (n == 0) {
+            // an empty fluid is a state like any other: steps return at once
+            // (dfsph.cu:121-122), as for an empty ParticleStore
+            counts_valid_ = false;
+            have_state_ = true;
+            return;
+        }
         if (mp) {
             launch(DFSPH_KERNEL_IO, import_mapped_kernel<R>, blocks_for(n, 256), 256, int(n), mp, mv, xk_[cx_].p,
                    vr_[cv_].p, id_[ci_].p);
