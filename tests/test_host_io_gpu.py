@@ -105,3 +105,36 @@ def test_get_state_matches_the_field_reads():
     s.step(sc.dt, 2)
     t.step(sc.dt, 2)
     assert np.array_equal(s.positions(), t.positions())
+
+
+@pytest.mark.parametrize("precision", [_lib.PRECISION_FP64, _lib.PRECISION_FP32_COMPENSATED])
+def test_get_state_in_the_other_precisions(precision):
+    # the export converts the working type to float as dfsph_get_field does
+    sc = scenes.falling_block((17, 59, 1), seed=7, velocity_sigma=0.2)
+    cfg = sc.config(precision=precision)
+    cfg.use_cuda_graph = 0
+    s = Solver(cfg)
+    s.set_boundary(sc.boundary)
+    s.set_fluid(sc.fluid, sc.velocity)
+    s.step(sc.dt, 3)
+    x_ref, v_ref = s.positions(), s.velocities()
+    xp = torch.empty((s.n, 3), dtype=torch.float32).pin_memory()
+    vp = torch.empty((s.n, 3), dtype=torch.float32).pin_memory()
+    s.get_state(xp.numpy(), vp.numpy())
+    assert np.array_equal(xp.numpy(), x_ref) and np.array_equal(vp.numpy(), v_ref)
+    xq, vq = np.empty((s.n, 3), np.float32), np.empty((s.n, 3), np.float32)
+    s.get_state(xq, vq)
+    assert np.array_equal(xq, x_ref) and np.array_equal(vq, v_ref)
+
+
+def test_get_state_of_a_batch():
+    from test_batch_gpu import batch_solver
+
+    scs, eps = scenes.batched_blocks(n_scenes=3, n_min=300, n_max=1000)
+    b = batch_solver(scs, eps)
+    b.step(scs[0].dt, 3)
+    x_ref, v_ref = b.positions(), b.velocities()
+    xp = torch.empty((b.n, 3), dtype=torch.float32).pin_memory()
+    vp = torch.empty((b.n, 3), dtype=torch.float32).pin_memory()
+    b.get_state(xp.numpy(), vp.numpy())
+    assert np.array_equal(xp.numpy(), x_ref) and np.array_equal(vp.numpy(), v_ref)
