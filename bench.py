@@ -14,7 +14,10 @@ value      device time of K steps (CUDA events on the solver's stream), inputs
            resident in HBM; L2 flushed (256 MB write) before every timed step.
 e2e        the same metric through the C ABI with host buffers: every step
            uploads x, v from pinned host memory (dfsph_set_fluid), steps, and
-           reads x, v back (dfsph_get_field).
+           reads x, v back (dfsph_get_state).
+drop_in    DFSPHSolver::step on a ParticleStore, i.e. dfsph_step_store on the
+           caller's device AoS arrays (gather in, one step, scatter x, v and
+           the density / alpha / kappa / density_adv attributes back).
 roofline   the dominant kernel class, timed live with CUDA events over as
            many steps again right after the timed ones (events inside the
            timed steps would slow them); algorithmic bytes per launch from the
@@ -349,8 +352,44 @@ def bench_ours(args, rank, world):
                             for k, v in share.items() if v[1]}}
     if not args.no_e2e:
         res["e2e"] = bench_e2e(s, sc, max(3, min(args.steps, 20)))
+        res["drop_in"] = bench_drop_in(s, sc, max(3, min(args.steps, 20)), ms_max / args.steps)
     s.close()
     return sc, res
+
+
+def bench_drop_in(s, sc, steps, resident_ms):
+    """The reference-facing C++ path: DFSPHSolver::step on the caller's
+    ParticleStore is one dfsph_step_store call on its device AoS arrays
+    (gather into the sorted state, one step, scatter positions, velocities
+    and the density / alpha / kappa / density_adv attributes back). Timed
+    with CUDA events on the solver's stream, inputs resident in HBM."""
+    import ctypes
+
+    import torch
+
+    dev = torch.device("cuda")
+    x = torch.tensor(sc.fluid, device=dev)
+    v = torch.tensor(sc.velocity, device=dev)
+    attrs = [torch.empty(sc.n, dtype=torch.float32, device=dev) for _ in range(4)]
+    stream = torch.cuda.current_stream()
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+    def one():
+        s._check(s._lib.dfsph_step_store(s._ctx, ptr(x), ptr(v), sc.n, ctypes.c_float(sc.dt), *map(ptr, attrs)))
+
+    for _ in range(3):
+        one()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        one()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    return {"value": sc.n / (ms * 1e-3), "unit": "particle-steps/s", "ms_per_step": ms, "steps": steps,
+            "over_resident_step": ms / resident_ms,
+            "path": "DFSPHSolver::step -> dfsph_step_store on device AoS arrays (ParticleStore in place)"}
 
 
 def bench_e2e(s, sc, steps):
@@ -1068,6 +1107,8 @@ def main():
                                  "peak": hbm, "unit": "GB/s", "frac": step_gbs / hbm}
     if "e2e" in res:
         line["e2e"] = res["e2e"]
+    if "drop_in" in res:
+        line["drop_in"] = res["drop_in"]
     if rank == 0 and not args.no_cpu:
         try:
             line["cpu_baseline"] = cpu_sample(sc)
