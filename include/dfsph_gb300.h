@@ -296,9 +296,12 @@ int dfsph_adjoint_backward(dfsph_ctx* ctx, const void* pos_bar, const void* vel_
  * only and cannot be resumed from): a header ("DFSPHST1", version, bytes per
  * real, scene count, fluid and wall counts, the last max |v|), the per-scene fluid counts,
  * positions and velocities in the working type (original particle order) and
- * the wall positions as float (input order). dfsph_load_state replaces the
- * walls and the fluid of a context with the same scene count (reals of the
- * other width are converted); the next step continues the saved run exactly. */
+ * the wall positions as float (input order), then, from a
+ * DFSPH_PRECISION_FP32_COMPENSATED context, its per-particle position carries
+ * (3 floats each, original order; header flag bit 0). dfsph_load_state
+ * replaces the walls and the fluid of a context with the same scene count
+ * (reals of the other width are converted; a context of another precision
+ * skips the carries); the next step continues the saved run exactly. */
 int dfsph_save_state(dfsph_ctx* ctx, const char* path);
 int dfsph_load_state(dfsph_ctx* ctx, const char* path);
 

@@ -11,7 +11,8 @@ from water_simulation_gb300.solver import Solver, solver_for
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("precision", [_lib.PRECISION_FP32, _lib.PRECISION_FP64])
+@pytest.mark.parametrize("precision", [_lib.PRECISION_FP32, _lib.PRECISION_FP64,
+                                       _lib.PRECISION_FP32_COMPENSATED])
 def test_resume_continues_bit_for_bit(tmp_path, precision):
     sc = scenes.falling_block(n_side=(12, 12, 12), velocity_sigma=0.3)
     a = solver_for(sc, precision=precision)
@@ -24,6 +25,27 @@ def test_resume_continues_bit_for_bit(tmp_path, precision):
     b.step(sc.dt, 7)
     assert np.array_equal(a.positions(), b.positions())
     assert np.array_equal(a.velocities(), b.velocities())
+
+
+def test_compensated_state_loads_into_other_precisions(tmp_path):
+    # the position carries are the compensated form's alone: a plain FP32
+    # context skips them and steps as from the same positions and velocities
+    sc = scenes.falling_block(n_side=(10, 10, 10), velocity_sigma=0.3)
+    a = solver_for(sc, precision=_lib.PRECISION_FP32_COMPENSATED)
+    a.step(sc.dt, 5)
+    path = tmp_path / "c.bin"
+    a.save_state(path)
+    b = Solver(sc.config(precision=_lib.PRECISION_FP32))
+    b.load_state(path)
+    c = solver_for(sc, precision=_lib.PRECISION_FP32)
+    c.set_fluid(a.positions(), a.velocities())
+    b.step(sc.dt, 3)
+    c.step(sc.dt, 3)
+    assert np.array_equal(b.positions(), c.positions())
+    d = Solver(sc.config(precision=_lib.PRECISION_FP64))
+    d.load_state(path)
+    d.step(sc.dt, 1)
+    assert np.isfinite(d.positions()).all()
 
 
 def test_resume_batched_scenes(tmp_path):

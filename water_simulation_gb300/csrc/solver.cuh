@@ -673,8 +673,9 @@ public:
         u32 nb;
         u32 stepped;          // 1: max_velocity holds the last step's value
         u32 maxv_bits;        // max |v| after the last step (float bits)
-        u32 reserved;
+        u32 flags;            // bit 0: the position carries of a compensated run follow the walls
     };
+    static constexpr u32 kStateCarries = 1u;
 
     void save_state(const char* path) override {
         const size_t n = n_;
@@ -697,6 +698,14 @@ public:
         }
         std::vector<R> xv(6 * size_t(h.n));
         std::vector<float> xb(3 * size_t(nb_));
+        // a compensated run continues exactly only with its position carries
+        // (original order, x y z per particle)
+        std::vector<V4> carries;
+        if (comp_ && h.n) {
+            h.flags |= kStateCarries;
+            carries.resize(n);
+            DFSPH_CUDA(cudaMemcpyAsync(carries.data(), xc_.p, n * sizeof(V4), cudaMemcpyDeviceToHost, stream_));
+        }
         if (h.n) {
             R* d = static_cast<R*>(scratch_bytes(6 * n * sizeof(R)));
             launch(DFSPH_KERNEL_IO, unsort_vec_kernel<R, R>, blocks_for(n, 256), 256, int(n), id_[ci_].p,
@@ -720,6 +729,10 @@ public:
                   std::fwrite(counts.data(), sizeof(u32), counts.size(), f) == counts.size() &&
                   std::fwrite(xv.data(), sizeof(R), xv.size(), f) == xv.size() &&
                   std::fwrite(xb.data(), sizeof(float), xb.size(), f) == xb.size();
+        for (size_t i = 0; ok && i < carries.size(); ++i) {
+            const R c3[3] = {carries[i].x, carries[i].y, carries[i].z};
+            ok = std::fwrite(c3, sizeof(R), 3, f) == 3;
+        }
         ok = (std::fclose(f) == 0) && ok;
         if (!ok) throw Error(DFSPH_ERR_IO, std::string("short write to ") + path);
     }
@@ -761,6 +774,19 @@ public:
         std::vector<float> xb(3 * size_t(h.nb));
         if (std::fread(xb.data(), sizeof(float), xb.size(), f) != xb.size())
             throw Error(DFSPH_ERR_IO, "truncated state file");
+        // the carries of a compensated run: kept by a compensated context,
+        // skipped by the others (which round every position update)
+        std::vector<V4> carries;
+        if ((h.flags & kStateCarries) && n) {
+            if (h.real_bytes != 4) throw Error(DFSPH_ERR_IO, "position carries of a non-float state file");
+            std::vector<float> t(3 * n);
+            if (std::fread(t.data(), sizeof(float), t.size(), f) != t.size())
+                throw Error(DFSPH_ERR_IO, "truncated state file");
+            if (comp_) {
+                carries.resize(n);
+                for (size_t i = 0; i < n; ++i) carries[i] = {R(t[3 * i]), R(t[3 * i + 1]), R(t[3 * i + 2]), R(0)};
+            }
+        }
         check_counts(h.n_scenes, counts.data());
         set_boundary(xb.data(), h.nb, DFSPH_MEM_HOST);
         install_counts(h.n_scenes, counts.data(), h.n);
@@ -782,6 +808,10 @@ public:
         stepped_ = h.stepped != 0;
         counts_valid_ = false;
         reset_compensation();
+        if (!carries.empty()) {
+            DFSPH_CUDA(cudaMemcpyAsync(xc_.p, carries.data(), n * sizeof(V4), cudaMemcpyHostToDevice, stream_));
+            DFSPH_CUDA(cudaStreamSynchronize(stream_));
+        }
         have_state_ = true;
     }
 
