@@ -206,16 +206,19 @@ def test_isolated_particle_density_and_fall():
     assert p[1] < 0.5 and p[0] == pytest.approx(0.5, rel=0.01) and p[2] == pytest.approx(0.5, rel=0.01)
 
 
-def test_step_store_matches_resident_step():
+@pytest.mark.parametrize("precision", [_lib.PRECISION_FP32, _lib.PRECISION_FP32_COMPENSATED])
+def test_step_store_matches_resident_step(precision):
+    # consecutive dfsph_step_store calls (DFSPHSolver::step on a store) step
+    # as the resident state does; a compensated run keeps its position carries
     import torch
 
     sc = scenes.falling_block((9, 9, 9), seed=15, velocity_sigma=0.1)
-    a = solver_for(sc)
-    b = solver_for(sc)
+    a = solver_for(sc, precision=precision)
+    b = solver_for(sc, precision=precision)
     pos = torch.tensor(sc.fluid, device="cuda")
     vel = torch.tensor(sc.velocity, device="cuda")
     rho = torch.zeros(sc.n, device="cuda")
-    for _ in range(3):
+    for _ in range(12):
         a.step(sc.dt)
         b.step_store(pos.data_ptr(), vel.data_ptr(), sc.n, sc.dt, rho.data_ptr())
     torch.cuda.synchronize()

@@ -290,6 +290,7 @@ public:
     }
 
     void set_fluid_batch(u32 n_scenes, const u32* counts, const float* xyz, const float* vel, int mem) override {
+        store_run_ = false;
         const u32 n = check_counts(n_scenes, counts);
         // page-locked host arrays are read in place by the import kernel;
         // other host memory goes through the staging buffer
@@ -407,6 +408,7 @@ public:
 
     // ------------------------------------------------------------------- step
     void step(float dt, u32 n_steps) override {
+        store_run_ = false;
         u32 k = 0;
         if (graph_ok()) {
             if (!counts_valid_ && k < n_steps) {  // the first step after new input counts itself
@@ -429,17 +431,22 @@ public:
                     float* density_adv) override {
         if (scenes_ != 1) throw Error(DFSPH_ERR_STATE, "dfsph_step_store steps one scene");
         if (n > cap_) throw Error(DFSPH_ERR_OUT_OF_RANGE, "store count exceeds capacity");
+        // a store stepped by consecutive calls holds the positions the
+        // previous call wrote back: a compensated run keeps its carries
+        const bool continuing = store_run_ && n == n_;
+        store_run_ = false;
         n_ = n;
         drop_pending_counts();
         drop_graph();
         if (n == 0) return;  // dfsph.cu:121-122
         launch_import(n, pos, vel, xk_[cx_].p, vr_[cv_].p, id_[ci_].p);
         counts_valid_ = false;
-        reset_compensation();
+        if (!continuing) reset_compensation();
         have_state_ = true;
         step_once(R(dt), /*count_next=*/false);
         launch(DFSPH_KERNEL_IO, export_kernel<R>, blocks_for(n, 256), 256, int(n), id_[ci_].p, xk_[cx_].p,
                vr_[cv_].p, alpha_.p, kap_.p, rho_adv_.p, pos, vel, density, alpha, kappa, density_adv);
+        store_run_ = true;
     }
 
     // -------------------------------------------------------------- readback
@@ -738,6 +745,7 @@ public:
     }
 
     void load_state(const char* path) override {
+        store_run_ = false;
         std::FILE* f = std::fopen(path, "rb");
         if (!f) throw Error(DFSPH_ERR_IO, std::string("cannot open ") + path);
         struct Closer { std::FILE* f; ~Closer() { std::fclose(f); } } closer{f};
@@ -910,6 +918,7 @@ public:
     // whose dt is chosen on the device; otherwise the host runs the
     // reference's loop, reading max |v| back before every substep.
     void step_frames(const dfsph_frame_config& fc, u32 n_frames, u32* substeps) override {
+        store_run_ = false;
         const NvtxRange range("dfsph frames");
         if (!have_state_) throw Error(DFSPH_ERR_STATE, "no fluid state: call dfsph_set_fluid first");
         if (n_frames == 0) return;
@@ -970,6 +979,7 @@ public:
 
     // ------------------------------------------------------------- adjoint
     void adjoint_set_state(const void* pos, const void* vel, u32 n, int mem) override {
+        store_run_ = false;
         if (scenes_ != 1) throw Error(DFSPH_ERR_STATE, "the adjoint steps one scene");
         if (n > cap_) throw Error(DFSPH_ERR_OUT_OF_RANGE, "count " + std::to_string(n) + " exceeds capacity");
         const R* p = static_cast<const R*>(pos);
@@ -2100,6 +2110,7 @@ private:
     dfsph_config cfg_;
     int device_;
     int sm_count_ = 0;  // queried on first use
+    bool store_run_ = false;  // the last state change was a dfsph_step_store call
     cudaStream_t stream_;
     GridGeom geom_;
     GridDev<R> g_;   // fluid grid (scene-aware)
