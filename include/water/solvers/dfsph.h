@@ -144,7 +144,9 @@ public:
     // One frame of CFL substeps on the caller's store: sim_cli's loop
     // (apps/sim_cli/main.cpp:171-181) with TimeStepper::next_dt, each dt from
     // max(max |v|, min_velocity); no counterpart in the reference's library.
-    // Returns the number of substeps taken.
+    // Returns the number of substeps taken. Each frame imports the store as
+    // new state, so with compensated position updates the carries span one
+    // frame's substeps (consecutive step() calls keep them across steps).
     u32 step_frame(const TimeStepper& ts, f32 frame_dt, f32 min_velocity = 0.5f, u32 max_substeps_per_frame = 64) {
         const std::size_t n = fluid_.count();
         const TimeStepper::Config tc = ts.config();
