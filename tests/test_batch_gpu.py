@@ -17,8 +17,8 @@ from water_simulation_gb300.solver import Solver, solver_for
 pytestmark = pytest.mark.gpu
 
 
-def batch_solver(scs, eps, graph=False, steps_scene=None):
-    cfg = scs[0].config(capacity=sum(s.n for s in scs))
+def batch_solver(scs, eps, graph=False, steps_scene=None, precision=_lib.PRECISION_FP32):
+    cfg = scs[0].config(capacity=sum(s.n for s in scs), precision=precision)
     cfg.n_scenes = len(scs)
     cfg.use_cuda_graph = 1 if graph else 0
     b = Solver(cfg)
@@ -86,6 +86,22 @@ def test_batched_graph_equals_batched_plain():
     b.step(scs[0].dt, 7)
     assert np.array_equal(a.positions(), b.positions())
     assert a.kernel_launches() == b.kernel_launches()
+
+
+def test_compensated_batch_equals_compensated_scenes_alone():
+    # each particle's position carry belongs to its index in the concatenated
+    # arrays, so a batch compensates exactly as its scenes do alone
+    scs, eps = scenes.batched_blocks(n_scenes=3, n_min=400, n_max=1500, seed_base=3000)
+    b = batch_solver(scs, eps, precision=_lib.PRECISION_FP32_COMPENSATED)
+    singles = [solver_for(s, precision=_lib.PRECISION_FP32_COMPENSATED) for s in scs]
+    b.step(scs[0].dt, 10)
+    for s in singles:
+        s.step(scs[0].dt, 10)
+    xb = b.positions()
+    o = 0
+    for k, s in enumerate(singles):
+        assert np.array_equal(xb[o:o + scs[k].n], s.positions()), k
+        o += scs[k].n
 
 
 def test_batch_argument_errors():
