@@ -64,3 +64,31 @@ def test_adjoint_refuses_a_compensated_context():
     s = solver_for(sc, precision=_lib.PRECISION_FP32_COMPENSATED)
     with pytest.raises(_lib.DfsphError):
         s.adjoint_forward(sc.dt, 4, 2)
+
+
+def test_compensated_graphs_and_device_frames_match_plain_steps():
+    # the captured step and the graph-resident frame loop pass the carries
+    # buffer as the plain launches do
+    from water_simulation_gb300.solver import Solver
+
+    sc = scenes.falling_block((12, 12, 12), seed=24, velocity_sigma=0.2)
+
+    def make(graph):
+        cfg = sc.config(precision=_lib.PRECISION_FP32_COMPENSATED)
+        cfg.use_cuda_graph = 1 if graph else 0
+        s = Solver(cfg)
+        s.set_boundary(sc.boundary)
+        s.set_fluid(sc.fluid, sc.velocity)
+        return s
+
+    g, p = make(True), make(False)
+    g.step(sc.dt, 9)  # one counting step, then four two-step graph replays
+    p.step(sc.dt, 9)
+    assert np.array_equal(g.positions(), p.positions())
+    assert np.array_equal(g.velocities(), p.velocities())
+    # frames: substeps chosen on the device (graph) and by the host loop
+    gs = g.step_frames(2)
+    ps = p.step_frames(2)
+    assert g.frames_on_device() and not p.frames_on_device()
+    assert np.array_equal(gs, ps)
+    assert np.array_equal(g.positions(), p.positions())
