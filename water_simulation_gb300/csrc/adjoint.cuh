@@ -298,17 +298,26 @@ __global__ void __launch_bounds__(128) adjoint_rate_kernel(
     xbar[i] = xo;
 }
 
-// Adds a block's FP64 partial into *acc; the last block sums the partials in
-// block order, so the result does not depend on scheduling.
+// Adds a block's FP64 partial (valid in thread 0) into *acc; called by every
+// thread of a 128-thread block. The last block to finish adds the partials
+// with all its threads, each a fixed stride of blocks, then a block sum: a
+// fixed order, so the result does not depend on scheduling (and the last
+// block's tail is a few strided loads, not one load per block in sequence).
 static __device__ __forceinline__ void accumulate_partial(double partial, double* partials, u32* counter,
-                                                          double* acc) {
-    partials[blockIdx.x] = partial;
-    __threadfence();
-    const u32 done = atomicAdd(counter, 1u);
-    if (done == gridDim.x - 1) {
+                                                          double* acc, double* sh) {
+    __shared__ int last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = partial;
         __threadfence();
-        double s = 0;
-        for (u32 b = 0; b < gridDim.x; ++b) s += *((volatile double*)&partials[b]);
+        last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double s = 0;
+    for (u32 b = threadIdx.x; b < gridDim.x; b += 128) s += *((volatile const double*)&partials[b]);
+    s = block_sum<128>(s, sh);
+    if (threadIdx.x == 0) {
         *acc += s;
         *counter = 0;
     }
@@ -374,7 +383,7 @@ __global__ void __launch_bounds__(128) adjoint_xsph_kernel(
                (double(wi.x) * double(EX) + double(wi.y) * double(EY) + double(wi.z) * double(EZ));
     }
     const double t = block_sum<128>(part, sh);
-    if (threadIdx.x == 0) accumulate_partial(t, partials, counter, eps_acc);
+    accumulate_partial(t, partials, counter, eps_acc, sh);
 }
 
 // alpha = rho / den: folds alpha_bar into rho_bar and the adjoints of G and of
