@@ -361,19 +361,38 @@ __device__ __forceinline__ bool below_threshold(double s, const StopTest& t) {
     return (t.f32 ? double(float(m)) : m) < t.thr;
 }
 
-// Thread 0 of every block calls this with the block's partial; the last block
-// to arrive sums all partials in block order, so the result does not depend on
-// block scheduling. Decides convergence: stop when (iter >= first_check) and
-// the mean passes the stop test.
+// The order in which the block partials of an error reduction are added, the
+// same in the per-pass last block (finish_reduction) and in the cooperative
+// solve's decision warp: lane l of one warp adds partials l, l + 32, l + 64,
+// ... in turn (from 0), then this shuffle tree adds the 32 lane sums. Valid
+// in lane 0; every lane of the warp calls it.
+__device__ __forceinline__ double lane_sums_total(double s) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    return s;
+}
+
+// Every thread of every block calls this (the block's partial valid in thread
+// 0); the last block to arrive adds all partials in lane_sums_total's order
+// with its first warp, so the result does not depend on block scheduling and
+// the tail is gridDim.x / 32 loads per lane, not gridDim.x in sequence.
+// Decides convergence: stop when (iter >= first_check) and the mean passes
+// the stop test.
 static __device__ __forceinline__ void finish_reduction(double partial, double* partials, IterCtl* ctl,
                                                  u32 iter, u32 first_check, StopTest rule) {
-    partials[blockIdx.x] = partial;
-    __threadfence();
-    const u32 done = atomicAdd(&ctl->blocks_done, 1u);
-    if (done == gridDim.x - 1) {
+    __shared__ int last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = partial;
         __threadfence();
-        double s = 0;
-        for (u32 b = 0; b < gridDim.x; ++b) s += *((volatile double*)&partials[b]);
+        last = atomicAdd(&ctl->blocks_done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x >= 32) return;
+    __threadfence();
+    double s = 0;
+    for (u32 b = threadIdx.x; b < gridDim.x; b += 32) s += *((volatile const double*)&partials[b]);
+    s = lane_sums_total(s);
+    if (threadIdx.x == 0) {
         ctl->err_sum = s;
         ctl->blocks_done = 0;
         if (iter >= first_check && below_threshold(s, rule)) ctl->stop_iter = iter;
@@ -1277,7 +1296,7 @@ __global__ void __launch_bounds__(LB) pressure_rate_kernel(
                                                    tape_v);
     if (REDUCE) {
         const double t = block_sum_dyn(err, sh);
-        if (threadIdx.x == 0) finish_reduction(t, partials, ctl, iter, first_check, rule);
+        finish_reduction(t, partials, ctl, iter, first_check, rule);
     }
 }
 
@@ -1500,8 +1519,8 @@ __device__ __forceinline__ R4<R> apply_velocity_quad(int i, int q, unsigned qmas
 // decision rebuilds that sum exactly: the error terms of every 32 consecutive
 // particles are summed with block_sum_dyn's warp shuffle tree into wsums;
 // after the barrier the decision warp rebuilds the per-pass partials from them
-// (each the sum of its pass_block / 32 warp sums in warp order) and sums those
-// in block order (finish_reduction). The error sum, and with it the iteration
+// (each the sum of its pass_block / 32 warp sums in warp order) and adds those
+// in finish_reduction's order (lane_sums_total). The error sum, and with it the iteration
 // count, is therefore the per-pass solve's bit for bit, and all blocks take the
 // same decision. Records written inside the launch are read with ld_coh; a
 // block whose stencils read at most stage_cap consecutive slots copies them
@@ -1520,7 +1539,6 @@ __global__ void __launch_bounds__(4 * P + 32) jacobi_solve_kernel(
     R4<R>* sx = reinterpret_cast<R4<R>*>(jacobi_stage);
     R4<R>* sv = sx + stage_cap;
     R4<R>* swx = sv + stage_cap;  // wall records, staged once per launch
-    __shared__ double part[JACOBI_SOLVE_MAX_BLOCKS];
     __shared__ double errs[P];
     __shared__ int stop;
     __shared__ u32 span_lo, span_hi;
@@ -1654,19 +1672,18 @@ __global__ void __launch_bounds__(4 * P + 32) jacobi_solve_kernel(
         if (!grid_barrier(&ctl->bar_arrive, bar_k++, wait, &bar_ok)) return;
         if (!worker) {
             // the decision: the per-pass partials, each from its warps' sums
-            // in warp order (warps past the last particle add +0 there), then
-            // their sum in block order
+            // in warp order (warps past the last particle add +0 there),
+            // added in finish_reduction's order (lane_sums_total)
             const u32 lane = threadIdx.x - W;
+            double s = 0;
             for (u32 b = lane; b < n_pass; b += 32) {
                 const u32 w0 = b * wpb, w1 = min(w0 + wpb, n_warps);
                 double t = 0;
                 for (u32 w = w0; w < w1; ++w) t += __ldcg(wsums + w);
-                part[b] = t;
+                s += t;
             }
-            __syncwarp();
+            s = lane_sums_total(s);
             if (lane == 0) {
-                double s = 0;
-                for (u32 b = 0; b < n_pass; ++b) s += part[b];
                 const bool done = it >= first_check && below_threshold(s, rule);
                 stop = done ? 1 : 0;
                 if (blockIdx.x == 0) {
