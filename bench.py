@@ -36,6 +36,9 @@ frames     sim_cli's frame loop on the puddle block: substeps chosen on the
            device inside one graph launch per frame, against the host loop.
 adjoint    the differentiable drop (32,768 particles, 200 steps, checkpoint
            every 20): backward time over forward time.
+dam1m_adaptive  the same dam break with the reference's default solve
+           (adaptive density solve at 0.1 %, at most 100 iterations), against
+           the reference's kernels over the same steps.
 puddle_adaptive  the settled puddle with the reference's adaptive density
            solve (its own CPU-runnable case), against the reference's kernels
            over the same steps.
@@ -103,6 +106,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default 128-thread neighbour passes")
     ap.add_argument("--no-lbvh", action="store_true", help="skip the LBVH build/refit timing")
     ap.add_argument("--no-puddle", action="store_true", help="skip the adaptive-puddle leg")
+    ap.add_argument("--no-dam-adaptive", action="store_true", help="skip the adaptive 1M dam-break leg")
     ap.add_argument("--no-morton", action="store_true", help="skip the Morton slot-order comparison")
     ap.add_argument("--slot-order", default="cell_key", choices=["cell_key", "morton"],
                     help="slot order of the timed context (the reference's is cell_key)")
@@ -121,6 +125,11 @@ def make_scene(name, sampler=None):
         return scenes.dam_break(scale=1, reference_mode=True, sampler=sampler)
     if name == "dam128k_div":  # with 2 divergence-solver iterations (the reference has none)
         return scenes.dam_break(scale=1, reference_mode=False, sampler=sampler)
+    if name == "dam1m_adaptive":  # the reference's default solve: adaptive density at 0.1 %, <= 100 iterations
+        sc = scenes.dam_break(scale=2, reference_mode=True, sampler=sampler)
+        sc.max_density_iters, sc.eta_density = 100, 1e-3
+        sc.name = "dam_break_1024000_adaptive"
+        return sc
     sc = scenes.puddle(sampler=sampler)
     if name == "puddle_adaptive":  # the settled puddle as the reference runs it: adaptive density solve
         sc.max_divergence_iters, sc.eta_divergence = 0, 0.0  # (0.01 %, <= 100 iterations), no divergence solver
@@ -766,6 +775,61 @@ def cpu_sample(sc, seconds=10.0, max_steps=2000, threads=0):
             "ms_per_step": 1e3 * sec / steps}
 
 
+def bench_dam_adaptive(steps=10, warmup=5):
+    """The 1M dam break with the reference's default solve (DFSPHSolver::Config:
+    adaptive density solve at 0.1 %, at most 100 iterations, no divergence
+    solver): steps warmup+1 .. warmup+steps with CUDA events (the context's
+    default plain launches: each solve stops on its own device-side decision,
+    the host reads it back after every iteration as the reference does), and
+    the reference's own kernels over the same steps."""
+    import torch
+
+    from water_simulation_gb300.solver import solver_for
+
+    sc = make_scene("dam1m_adaptive")
+    stream = torch.cuda.current_stream()
+    s = solver_for(sc, stream=stream.cuda_stream)
+    for _ in range(warmup):
+        s.step(sc.dt)
+    torch.cuda.synchronize()
+    ms, iters = 0.0, 0
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.step(sc.dt)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms += e0.elapsed_time(e1)
+        iters += s.last_density_iters()
+    s.close()
+    res = {"workload": sc.name, "particles": sc.n, "steps": f"{warmup + 1}-{warmup + steps}",
+           "ms_per_step": ms / steps, "density_iters_per_step": iters / steps,
+           "ms_per_iteration": ms / max(iters, 1), "particle_steps_per_s": sc.n * steps / (ms * 1e-3)}
+    # the same steps with use_cuda_graph: pairs of steps replay one graph whose
+    # solves loop on the device (WHILE nodes), with no host read-back
+    from water_simulation_gb300.solver import Solver
+
+    cfg = sc.config()
+    cfg.use_cuda_graph = 1
+    g = Solver(cfg, stream=stream.cuda_stream)
+    g.set_boundary(sc.boundary)
+    g.set_fluid(sc.fluid, sc.velocity)
+    g.step(sc.dt, warmup)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    g.step(sc.dt, steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    res["graph_ms_per_step"] = e0.elapsed_time(e1) / steps
+    g.close()
+    ref = bench_ref_cuda(sc, steps, warmup)
+    res["ref_cuda"] = ref
+    if "ms_per_step" in ref:
+        res["speedup_vs_ref_cuda"] = ref["ms_per_step"] / (ms / steps)
+    return res
+
+
 def bench_puddle_adaptive(steps=50, warmup=5):
     """The settled puddle as the reference runs it (adaptive density solve at
     0.01 %, at most 100 iterations, no divergence solver): steps
@@ -1142,6 +1206,11 @@ def main():
             line["puddle_adaptive"] = bench_puddle_adaptive()
         except Exception as e:
             line["puddle_adaptive"] = {"unavailable": str(e)[:200]}
+    if rank == 0 and not args.no_dam_adaptive and args.workload == "dam1m":
+        try:
+            line["dam1m_adaptive"] = bench_dam_adaptive()
+        except Exception as e:
+            line["dam1m_adaptive"] = {"unavailable": str(e)[:200]}
     if rank == 0 and not args.no_lbvh:
         try:
             line["lbvh"] = bench_lbvh(sc)
