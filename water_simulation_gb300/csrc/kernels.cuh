@@ -372,19 +372,34 @@ __device__ __forceinline__ double lane_sums_total(double s) {
     return s;
 }
 
+// The 32 arrival counters of finish_reduction, each on its own 128-byte line,
+// sit in the REDUCE_GROUP_WORDS words in front of the partials (zero between
+// reductions: the block that completes a group clears its counter).
+constexpr u32 REDUCE_GROUP_WORDS = 32 * 32;
+
 // Every thread of every block calls this (the block's partial valid in thread
 // 0); the last block to arrive adds all partials in lane_sums_total's order
 // with its first warp, so the result does not depend on block scheduling and
 // the tail is gridDim.x / 32 loads per lane, not gridDim.x in sequence.
-// Decides convergence: stop when (iter >= first_check) and the mean passes
-// the stop test.
+// Arrivals are counted in two levels (block b on counter b % 32, then the
+// block completing a group on ctl->blocks_done), so no single address takes
+// one atomic per block. Decides convergence: stop when (iter >= first_check)
+// and the mean passes the stop test.
 static __device__ __forceinline__ void finish_reduction(double partial, double* partials, IterCtl* ctl,
                                                  u32 iter, u32 first_check, StopTest rule) {
     __shared__ int last;
     if (threadIdx.x == 0) {
         partials[blockIdx.x] = partial;
         __threadfence();
-        last = atomicAdd(&ctl->blocks_done, 1u) == gridDim.x - 1;
+        u32* group = reinterpret_cast<u32*>(partials) - REDUCE_GROUP_WORDS + 32u * (blockIdx.x & 31u);
+        const u32 members = (gridDim.x - (blockIdx.x & 31u) + 31u) / 32u;
+        int l = 0;
+        if (atomicAdd(group, 1u) == members - 1u) {
+            *group = 0u;  // every member has arrived: ready for the next reduction
+            __threadfence();
+            l = atomicAdd(&ctl->blocks_done, 1u) == min(gridDim.x, 32u) - 1u;
+        }
+        last = l;
     }
     __syncthreads();
     if (!last || threadIdx.x >= 32) return;

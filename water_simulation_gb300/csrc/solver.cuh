@@ -154,8 +154,9 @@ public:
         n_tiles_ = static_cast<u32>((keys_ + SCAN_TILE - 1) / SCAN_TILE);
         tile_sums_.alloc(n_tiles_ + 1);
         // block partials of the per-pass reductions (blocks of >= 64 threads)
-        // and the per-warp sums of the cooperative solve
-        partials_.alloc(std::max<size_t>(1, (std::max(cap_, 1u) + 31) / 32));
+        // and the per-warp sums of the cooperative solve, behind the
+        // reductions' arrival counters (REDUCE_GROUP_WORDS words)
+        partials_.alloc(REDUCE_GROUP_WORDS / 2 + std::max<size_t>(1, (std::max(cap_, 1u) + 31) / 32));
         ctl_.alloc(3);
         dev_err_.alloc(1);
         staging_.alloc(std::max<size_t>(size_t(std::max(cap_, bcap_)) * 6, 6));
@@ -204,6 +205,7 @@ public:
         DFSPH_CUDA(cudaMemsetAsync(cell_start_.p, 0, (keys_ + 1) * sizeof(u32), stream_));
         DFSPH_CUDA(cudaMemsetAsync(bcs_.p, 0, (size_t(cells1_) + 1) * sizeof(u32), stream_));
         DFSPH_CUDA(cudaMemsetAsync(ctl_.p, 0, 3 * sizeof(IterCtl), stream_));
+        DFSPH_CUDA(cudaMemsetAsync(partials_.p, 0, REDUCE_GROUP_WORDS * sizeof(u32), stream_));
         DFSPH_CUDA(cudaMemsetAsync(dev_err_.p, 0, sizeof(u32), stream_));
         DFSPH_CUDA(cudaMemsetAsync(alpha_.p, 0, size_t(cap_) * sizeof(R), stream_));
         DFSPH_CUDA(cudaMemsetAsync(rho_adv_.p, 0, size_t(cap_) * sizeof(R), stream_));
@@ -1186,6 +1188,9 @@ private:
         return ad_staging_.p;
     }
 
+    // the partials (or warp sums) of the error reductions, past their counters
+    double* red_partials() const { return partials_.p + REDUCE_GROUP_WORDS / 2; }
+
     int sm_count() {
         if (sm_count_ == 0) DFSPH_CUDA(cudaDeviceGetAttribute(&sm_count_, cudaDevAttrMultiProcessorCount, device_));
         return sm_count_;
@@ -1784,12 +1789,12 @@ private:
                 if (adaptive)
                     launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true, false, 128, M>,
                                 pressure_rate_kernel<R, DIV, true, false, 256, M>, n, xin, xout, vr_[cv_].p, alpha_.p,
-                                adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl, it, first_check, thr, tv,
+                                adv_it, kap_it, cs, g_, phys_, bdev(), sd, red_partials(), ctl, it, first_check, thr, tv,
                                 (const u32*)nullptr);
                 else
                     launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, false, false, 128, M>,
                                 pressure_rate_kernel<R, DIV, false, false, 256, M>, n, xin, xout, vr_[cv_].p, alpha_.p,
-                                adv_it, kap_it, cs, g_, phys_, bdev(), sd, partials_.p, ctl, it, first_check, thr, tv,
+                                adv_it, kap_it, cs, g_, phys_, bdev(), sd, red_partials(), ctl, it, first_check, thr, tv,
                                 (const u32*)nullptr);
             });
             if (!tp) cx_ ^= 1;
@@ -1921,7 +1926,7 @@ private:
         V4* xb = xk_[cx_ ^ 1].p;
         auto go = [&](auto kernel) {
             return cudaLaunchKernelEx(&lc, kernel, n, xa, xb, vr_[cv_].p, (const R*)alpha_.p, adv_out, kap_out, cs,
-                                      g_, phys_, bdev(), sd, partials_.p, ctl, max_iters, first_check, thr,
+                                      g_, phys_, bdev(), sd, red_partials(), ctl, max_iters, first_check, thr,
                                       stage_cap, wall_cap, u32(lb), WaitCfg{wait_limit_ns_, wait_missing_, dev_err_.p});
         };
         cudaError_t e;
@@ -1982,7 +1987,7 @@ private:
             V4* xb = xk_[cx_ ^ 1].p;
             const u32* dit = &ctl->iters;
             launch_pass(DFSPH_KERNEL_PRESSURE_RATE, pressure_rate_kernel<R, DIV, true, true, 128>, pressure_rate_kernel<R, DIV, true, true, 256>, n,
-                   (const V4*)xa, xb, vr_[cv_].p, alpha_.p, adv_out, kap_out, cs, g_, phys_, bdev(), sd, partials_.p,
+                   (const V4*)xa, xb, vr_[cv_].p, alpha_.p, adv_out, kap_out, cs, g_, phys_, bdev(), sd, red_partials(),
                    ctl, 0u, first_check, thr, (V4*)nullptr, dit);
             launch_pass(DFSPH_KERNEL_PRESSURE_APPLY, pressure_apply_kernel<R, true, 128>, pressure_apply_kernel<R, true, 256>, n, (const V4*)xb,
                    vr_[cv_].p, kap_out, cs, g_, phys_, bdev(), sd, (const IterCtl*)ctl, 0u, (const V4*)xa, dit);
