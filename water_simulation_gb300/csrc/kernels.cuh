@@ -363,9 +363,12 @@ __device__ __forceinline__ bool below_threshold(double s, const StopTest& t) {
 
 // The order in which the block partials of an error reduction are added, the
 // same in the per-pass last block (finish_reduction) and in the cooperative
-// solve's decision warp: lane l of one warp adds partials l, l + 32, l + 64,
-// ... in turn (from 0), then this shuffle tree adds the 32 lane sums. Valid
-// in lane 0; every lane of the warp calls it.
+// solve's decision warp. Up to REDUCE_SERIAL_MAX partials one lane adds them
+// in block order (a few FP64 additions: quicker than a warp-wide tree on
+// this GPU's few FP64 units); beyond, lane l of one warp adds partials l,
+// l + 32, l + 64, ... in turn (from 0), then this shuffle tree adds the 32
+// lane sums. Valid in lane 0; every lane of the warp calls it.
+constexpr u32 REDUCE_SERIAL_MAX = 64;
 __device__ __forceinline__ double lane_sums_total(double s) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -405,8 +408,13 @@ static __device__ __forceinline__ void finish_reduction(double partial, double* 
     if (!last || threadIdx.x >= 32) return;
     __threadfence();
     double s = 0;
-    for (u32 b = threadIdx.x; b < gridDim.x; b += 32) s += *((volatile const double*)&partials[b]);
-    s = lane_sums_total(s);
+    if (gridDim.x <= REDUCE_SERIAL_MAX) {
+        if (threadIdx.x == 0)
+            for (u32 b = 0; b < gridDim.x; ++b) s += *((volatile const double*)&partials[b]);
+    } else {
+        for (u32 b = threadIdx.x; b < gridDim.x; b += 32) s += *((volatile const double*)&partials[b]);
+        s = lane_sums_total(s);
+    }
     if (threadIdx.x == 0) {
         ctl->err_sum = s;
         ctl->blocks_done = 0;
@@ -1554,6 +1562,7 @@ __global__ void __launch_bounds__(4 * P + 32) jacobi_solve_kernel(
     R4<R>* sx = reinterpret_cast<R4<R>*>(jacobi_stage);
     R4<R>* sv = sx + stage_cap;
     R4<R>* swx = sv + stage_cap;  // wall records, staged once per launch
+    __shared__ double part[REDUCE_SERIAL_MAX];  // the decision's partials, when added by one lane
     __shared__ double errs[P];
     __shared__ int stop;
     __shared__ u32 span_lo, span_hi;
@@ -1691,13 +1700,25 @@ __global__ void __launch_bounds__(4 * P + 32) jacobi_solve_kernel(
             // added in finish_reduction's order (lane_sums_total)
             const u32 lane = threadIdx.x - W;
             double s = 0;
-            for (u32 b = lane; b < n_pass; b += 32) {
-                const u32 w0 = b * wpb, w1 = min(w0 + wpb, n_warps);
-                double t = 0;
-                for (u32 w = w0; w < w1; ++w) t += __ldcg(wsums + w);
-                s += t;
+            if (n_pass <= REDUCE_SERIAL_MAX) {
+                for (u32 b = lane; b < n_pass; b += 32) {
+                    const u32 w0 = b * wpb, w1 = min(w0 + wpb, n_warps);
+                    double t = 0;
+                    for (u32 w = w0; w < w1; ++w) t += __ldcg(wsums + w);
+                    part[b] = t;
+                }
+                __syncwarp();
+                if (lane == 0)
+                    for (u32 b = 0; b < n_pass; ++b) s += part[b];
+            } else {
+                for (u32 b = lane; b < n_pass; b += 32) {
+                    const u32 w0 = b * wpb, w1 = min(w0 + wpb, n_warps);
+                    double t = 0;
+                    for (u32 w = w0; w < w1; ++w) t += __ldcg(wsums + w);
+                    s += t;
+                }
+                s = lane_sums_total(s);
             }
-            s = lane_sums_total(s);
             if (lane == 0) {
                 const bool done = it >= first_check && below_threshold(s, rule);
                 stop = done ? 1 : 0;
